@@ -1,0 +1,200 @@
+/*
+ * ligmg_gpu.h — C ABI of the GB300 (sm_103a) LigMG graph-Laplacian multigrid
+ * solver.  Everything here is plain C: pointers, sizes and int status codes.
+ * No call throws or aborts across this boundary.
+ *
+ * The ABI replaces these reference interfaces (paths inside the ligmg project):
+ *   ligmg_create           <- ligmg::Solver(A) / Solver(A, Options)
+ *                             include/ligmg/ligmg.hpp:17-28, which calls
+ *                             make_hierarchy (include/ligmg/multigrid.hpp:162-263)
+ *   ligmg_solve            <- Solver::solve(b)            ligmg.hpp:31-33
+ *   ligmg_solve_from       <- Solver::solve(b, from)      ligmg.hpp:36-38
+ *   ligmg_default_options  <- ligmg::default_options()    options.hpp:136
+ *   ligmg_options          <- struct ligmg::Options       options.hpp:80-134
+ *   ligmg_info             <- ligmg::ConvergenceInfo      util.hpp:143-170
+ *   ligmg_destroy          <- ~Solver / PCDestroy_LIGMG   petsc_shim.hpp:31-38
+ *   ligmg_hierarchy_*      <- print_hierarchy / dump_hierarchy
+ *                             multigrid.hpp:265-292, ligmg.hpp:47-52
+ *   ligmg_cycle            <- vcycle / kcycle             multigrid.hpp:87-130
+ *   ligmg_spmv             <- SpMV_inplace (MatShell MATOP_MULT)  util.hpp:451-476
+ *   ligmg_status_string    <- PETSC_CHECK_ERROR message   util.hpp:653-660
+ * The PETSc plugin PCCreate_LIGMG (petsc_shim.hpp:64-74) is a thin client of
+ * ligmg_create / ligmg_solve; its source is shown in INTEGRATION.md.
+ *
+ * Rules:
+ *   - status 0 (LIGMG_OK) is success; LIGMG_NOT_CONVERGED is a soft status
+ *     (the solution is still written); everything else is an error.
+ *   - matrices are CSR with int64 row pointers, int32 column indices sorted
+ *     ascending inside each row, FP64 values; the graph Laplacian must be
+ *     structurally and numerically symmetric, carry every diagonal entry,
+ *     have non-positive off-diagonals and be connected.
+ *   - functions without a _device suffix take HOST pointers; *_device
+ *     variants take device pointers on the handle's device.
+ *   - one CUDA stream per handle; a handle is not thread-safe, distinct
+ *     handles are.
+ */
+#ifndef LIGMG_GPU_H
+#define LIGMG_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int ligmg_status;
+
+#define LIGMG_OK 0
+#define LIGMG_NOT_CONVERGED 1          /* reached the iteration limit; x written */
+#define LIGMG_ERR_INVALID_ARGUMENT 2   /* null pointer, bad size, bad option */
+#define LIGMG_ERR_NOT_SYMMETRIC 3      /* pattern or values not symmetric */
+#define LIGMG_ERR_BAD_DIAGONAL 4       /* missing or non-positive diagonal */
+#define LIGMG_ERR_POSITIVE_OFFDIAG 5   /* off-diagonal entry > 0 */
+#define LIGMG_ERR_NONFINITE 6          /* NaN or Inf in a matrix or vector */
+#define LIGMG_ERR_DISCONNECTED 7       /* coarse operator singular beyond the constant */
+#define LIGMG_ERR_CUDA 8               /* a CUDA runtime call failed */
+#define LIGMG_ERR_OUT_OF_MEMORY 9      /* device allocation failed */
+#define LIGMG_ERR_BREAKDOWN 10         /* Krylov breakdown / NaN residual */
+#define LIGMG_ERR_UNSUPPORTED 11       /* option combination not built */
+#define LIGMG_ERR_INTERNAL 12          /* a device-side check failed */
+#define LIGMG_ERR_NOT_SORTED 13        /* CSR columns not strictly ascending */
+
+/* enum values follow the reference enums (options.hpp:10-62) */
+#define LIGMG_SMOOTHER_JACOBI 0
+#define LIGMG_SMOOTHER_CHEBYSHEV 1
+#define LIGMG_AFF_NONE 0
+#define LIGMG_AFF_ROW 1
+#define LIGMG_AFF_COLUMN 2
+#define LIGMG_AFF_ROWCOLUMN 3
+#define LIGMG_AFF_SYM 4
+#define LIGMG_AFF_MAX 5
+#define LIGMG_STRENGTH_AFFINITY 0
+#define LIGMG_STRENGTH_ALGEBRAIC_DISTANCE 1
+#define LIGMG_STRENGTH_NONE 2
+#define LIGMG_KSP_CG 0
+#define LIGMG_KSP_FCG 1
+#define LIGMG_PREC_FP64 0   /* hierarchy, smoothers and cycle in FP64 */
+#define LIGMG_PREC_FP32 1   /* FP32 hierarchy/cycle inside the FP64 outer Krylov */
+
+#define LIGMG_LEVEL_ELIM 0
+#define LIGMG_LEVEL_AGG 1
+#define LIGMG_LEVEL_COARSE 2
+
+/* Hot-path fields of ligmg::Options (options.hpp:80-134) plus the GB300
+ * additions at the end.  Fill with ligmg_default_options() first. */
+typedef struct ligmg_options {
+  int32_t max_levels;         /* 50   options.hpp:91 */
+  int32_t always_elim;        /* 1    :84 */
+  int64_t min_size;           /* 4000 (nnz) :92 */
+  int32_t top_elim;           /* 1    :85 */
+  int32_t elim_degree;        /* 4    :93 */
+  double elim_factor;         /* 0.9  :121 */
+  int32_t elim_iters;         /* 1    :123 */
+  int32_t iters;              /* 500  :97 */
+  double tol;                 /* 1e-8 :94 */
+  double thresh;              /* 1e-8 :95 */
+  int32_t agg_iters;          /* 10   :96 */
+  int32_t num_tvs;            /* 10   :102 */
+  double agg_init_factor;     /* 0.5  :115 */
+  double agg_iter_factor;     /* 0.5  :114 */
+  int64_t votes_to_seed;      /* 1    :112 */
+  int64_t max_agg_size;       /* -1   :113 */
+  double rejection_ratio;     /* -1   :124 */
+  int32_t rejection_to_seed;  /* 0    :131 */
+  int32_t neighbor_of_neighbor; /* 0  :130 */
+  int32_t tvs_smooth;         /* 4    :103 */
+  int32_t strength_metric;    /* AFFINITY :89 */
+  int32_t aff_scaling;        /* MAX  :118 */
+  int32_t pre_smooth;         /* 2    :100 */
+  int32_t post_smooth;        /* 2    :101 */
+  int32_t smoother_type;      /* CHEBYSHEV :105 */
+  double cheby_lower;         /* 0.3  :116 */
+  double cheby_upper;         /* 1.1  :117 */
+  int32_t constant_correction;/* 0    :87 */
+  int32_t kcycle;             /* 0    :107 */
+  int32_t kcycle_iters;       /* 2    :111 */
+  int32_t outer_ksp_type;     /* CG   :109 */
+  int32_t kcycle_ksp_type;    /* FCG  :110 */
+  /* ---- additions (no reference counterpart) ---- */
+  int32_t precision;          /* LIGMG_PREC_FP64 */
+  uint32_t seed;              /* srand() seed of the glibc rand() stream that
+                                 feeds the aggregation test vectors */
+  int32_t fcg_mmax;           /* stored directions of truncated FCG (1) */
+  int64_t rng_skip;           /* rand() draws consumed before setup (0) */
+  int32_t verbose;            /* 0 */
+  int32_t device;             /* CUDA device ordinal (0) */
+} ligmg_options;
+
+/* ConvergenceInfo (util.hpp:143-170) of one solve.  For a batched solve the
+ * scalar fields describe the worst column and the per-column arrays (when
+ * non-null, length k) are filled. */
+typedef struct ligmg_info {
+  int32_t iters;              /* outer iterations (max over columns) */
+  int32_t converged;          /* all columns reached tol */
+  double rel_residual;        /* last / first outer residual (worst column) */
+  double true_rel_residual;   /* ||b - L x||_2 / ||b||_2 on the input system, FP64 */
+  double cycle_complexity;    /* multigrid.hpp:372-387 */
+  double work;                /* iters * (1 + cycle_complexity)  cg.hpp:332 */
+  double solve_seconds;       /* wall time of the solve */
+  double setup_seconds;       /* wall time of ligmg_create */
+  double *residual_history;   /* optional caller buffer (column 0) */
+  int32_t history_capacity;   /* its capacity */
+  int32_t history_len;        /* entries written */
+  int32_t *col_iters;         /* optional, length k */
+  double *col_true_rel_residual; /* optional, length k */
+} ligmg_info;
+
+typedef struct ligmg_handle_s *ligmg_handle;
+
+void ligmg_default_options(ligmg_options *opts);
+const char *ligmg_status_string(ligmg_status s);
+
+/* Build the hierarchy on the GPU (setup).  rowptr[n+1], col[nnz], val[nnz]
+ * are host arrays; they are copied and may be freed after the call. */
+ligmg_status ligmg_create(int64_t n, const int64_t *rowptr, const int32_t *col,
+                          const double *val, const ligmg_options *opts,
+                          ligmg_handle *out);
+ligmg_status ligmg_destroy(ligmg_handle h);
+
+/* Solve L x = b (host arrays of length n). */
+ligmg_status ligmg_solve(ligmg_handle h, const double *b, double *x,
+                         ligmg_info *info);
+/* Solve starting from hierarchy level `from` (ligmg.hpp:36-38). */
+ligmg_status ligmg_solve_from(ligmg_handle h, const double *b, double *x,
+                              int32_t from, ligmg_info *info);
+/* Solve k right-hand sides at once: B and X are n x k row-major host arrays. */
+ligmg_status ligmg_solve_batched(ligmg_handle h, const double *B, int32_t k,
+                                 double *X, ligmg_info *info);
+/* Same with device pointers (n x k row-major, FP64). */
+ligmg_status ligmg_solve_batched_device(ligmg_handle h, const double *dB,
+                                        int32_t k, double *dX,
+                                        ligmg_info *info);
+
+/* Hierarchy inspection (print_hierarchy / dump_hierarchy). */
+ligmg_status ligmg_hierarchy_levels(ligmg_handle h, int32_t *num_levels);
+/* type: LIGMG_LEVEL_*; n, nnz of the level's input matrix; nc = size of the
+ * next level (0 for the coarse level). */
+ligmg_status ligmg_level_info(ligmg_handle h, int32_t level, int32_t *type,
+                              int64_t *n, int64_t *nnz, int64_t *nc);
+/* Copy the level's input matrix to host CSR arrays (rowptr n+1, col/val nnz). */
+ligmg_status ligmg_level_matrix(ligmg_handle h, int32_t level, int64_t *rowptr,
+                                int32_t *col, double *val);
+/* Level ids (length n): aggregate id per vertex for an aggregation level,
+ * coarse id (or -1 when eliminated) for an elimination level. */
+ligmg_status ligmg_level_ids(ligmg_handle h, int32_t level, int32_t *ids);
+/* Largest eigenvalue estimate of D^-1 A used by the level's Chebyshev smoother. */
+ligmg_status ligmg_level_lmax(ligmg_handle h, int32_t level, double *lmax);
+
+/* One multigrid cycle x = M(b) starting at `level` with x = 0 on entry
+ * (vcycle/kcycle per the handle's options), host arrays of the level's size. */
+ligmg_status ligmg_cycle(ligmg_handle h, int32_t level, const double *b,
+                         double *x);
+
+/* y = A x with the level's matrix (host arrays).  Debug/measurement entry. */
+ligmg_status ligmg_spmv(ligmg_handle h, int32_t level, const double *x,
+                        double *y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LIGMG_GPU_H */

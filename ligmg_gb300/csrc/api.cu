@@ -1,0 +1,1169 @@
+// api.cu — host driver of the GB300 LigMG solver and its C ABI.
+//
+//   ligmg_create  : make_hierarchy (include/ligmg/multigrid.hpp:162-263) on the
+//                   GPU: elimination, aggregation, Galerkin products, Chebyshev
+//                   eigenvalue estimates and the coarse pseudo-inverse.
+//   ligmg_solve*  : solve (multigrid.hpp:316-370): top elimination, outer
+//                   FP64 CG/FCG (cg.hpp:18-116) preconditioned by a V- or
+//                   K-cycle (multigrid.hpp:87-130) in FP64 or FP32.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+
+#include "prims.cuh"
+#include "setup.cuh"
+#include "solve.cuh"
+
+namespace lg {
+namespace {
+
+// glibc rand() (TYPE_3 additive feedback generator), restated from its
+// published description: r[0] = seed (1 if 0); r[i] = 16807 r[i-1] mod
+// (2^31 - 1) (Schrage) for i < 31; r[i] = r[i-31] for i = 31..33;
+// r[i] = r[i-3] + r[i-31] mod 2^32; output k is r[k + 344] >> 1.
+// The reference draws its test vectors with rand() (combblas_extra.hpp:186-192).
+struct GlibcRand {
+  uint32_t ring[32];
+  i64 i = 0;
+  explicit GlibcRand(uint32_t seed) {
+    int32_t r[34];
+    r[0] = (int32_t)(seed == 0 ? 1u : seed);
+    for (int k = 1; k < 31; k++) {
+      int32_t hi = r[k - 1] / 127773, lo = r[k - 1] % 127773;
+      int32_t word = 16807 * lo - 2836 * hi;
+      if (word < 0) word += 2147483647;
+      r[k] = word;
+    }
+    for (int k = 31; k < 34; k++) r[k] = r[k - 31];
+    for (int k = 0; k < 34; k++) ring[k & 31] = (uint32_t)r[k];
+    i = 34;
+    for (int k = 34; k < 344; k++) raw();
+  }
+  uint32_t raw() {
+    uint32_t v = ring[(i - 31) & 31] + ring[(i - 3) & 31];
+    ring[i & 31] = v;
+    i++;
+    return v;
+  }
+  int32_t next() { return (int32_t)(raw() >> 1); }
+};
+
+// right-hand side of the eigenvalue estimate (hash of the row index)
+inline double est_rhs(i64 i) {
+  uint32_t x = (uint32_t)i * 2654435761u + 0x9E3779B9u;
+  x ^= x >> 16;
+  x *= 0x85EBCA6Bu;
+  x ^= x >> 13;
+  x *= 0xC2B2AE35u;
+  x ^= x >> 16;
+  return (double)x * (1.0 / 4294967296.0) - 0.5;
+}
+
+double tridiag_lmax(const std::vector<double> &d, const std::vector<double> &e) {
+  int m = (int)d.size();
+  if (m == 0) return 0.0;
+  double lo = d[0], hi = d[0];
+  for (int i = 0; i < m; i++) {
+    double r = 0;
+    if (i > 0) r += std::fabs(e[i - 1]);
+    if (i + 1 < m) r += std::fabs(e[i]);
+    lo = std::min(lo, d[i] - r);
+    hi = std::max(hi, d[i] + r);
+  }
+  for (int it = 0; it < 200; it++) {
+    double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    int cnt = 0;
+    double q = 1.0;
+    for (int i = 0; i < m; i++) {
+      double off = (i > 0) ? e[i - 1] * e[i - 1] : 0.0;
+      q = d[i] - mid - ((i > 0) ? off / q : 0.0);
+      if (q == 0.0) q = -1e-300;
+      if (q < 0) cnt++;
+    }
+    if (cnt == m) hi = mid; else lo = mid;
+  }
+  return hi;
+}
+
+__global__ void k_invdiag(const i64 *rp, const i32 *ci, const double *v, i64 n, double *invd) {
+  i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  i64 lo = rp[i], hi = rp[i + 1];
+  while (lo < hi) {
+    i64 mid = (lo + hi) >> 1;
+    if (ci[mid] < i) lo = mid + 1; else hi = mid;
+  }
+  invd[i] = 1.0 / v[lo];
+}
+
+__global__ void k_mul_diag(i64 n, const double *d, const double *x, double *y) {
+  i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = d[i] * x[i];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct Level {
+  int type = LIGMG_LEVEL_AGG;
+  DCsr<double> A;
+  i64 nc = 0;
+  double lmax = 0;
+  DBuf<double> invd;
+  ElimResult elim;
+  AggResult agg;
+  DBuf<double> pinv;
+  // FP32 copies for the FP32 hierarchy
+  bool has32 = false;
+  DBuf<float> Av32, invd32, Pv32, Rv32, Q32, pinv32;
+  // hub-row plans (A and, for elimination levels, R)
+  HubPlan<double> hubA64, hubR64;
+  HubPlan<float> hubA32, hubR32;
+  int lanesA = 32, lanesR = 32, lanesP = 4;
+  // Chebyshev coefficients
+  double theta = 1, delta = 1;
+  std::vector<double> c1, c2;
+
+  bool is_exact() const { return type == LIGMG_LEVEL_ELIM; }
+  i64 work(const ligmg_options &o) const {
+    if (type == LIGMG_LEVEL_AGG)
+      return (i64)(o.pre_smooth + o.post_smooth + 1) * A.nnz + 3 * A.n;
+    if (type == LIGMG_LEVEL_ELIM) return elim.P.nnz + elim.R.nnz + (A.n - elim.nc);
+    return A.nnz;
+  }
+};
+
+int lanes_for(i64 nnz, i64 n) {
+  double m = n ? (double)nnz / (double)n : 0;
+  if (m <= 4.5) return 4;
+  if (m <= 9) return 8;
+  if (m <= 18) return 16;
+  return 32;
+}
+
+constexpr i64 kHubThresh = 2048;
+constexpr i64 kHubChunk = 1024;
+constexpr int kMaxK = 64;
+
+template <typename T>
+MatView<T> viewA(const Level &L);
+template <>
+MatView<double> viewA<double>(const Level &L) {
+  MatView<double> m;
+  m.n = L.A.n; m.rp = L.A.rp.p; m.ci = L.A.ci.p; m.v = L.A.v.p; m.lanes_per_row = L.lanesA;
+  L.hubA64.fill(m);
+  return m;
+}
+template <>
+MatView<float> viewA<float>(const Level &L) {
+  MatView<float> m;
+  m.n = L.A.n; m.rp = L.A.rp.p; m.ci = L.A.ci.p; m.v = L.Av32.p; m.lanes_per_row = L.lanesA;
+  L.hubA32.fill(m);
+  return m;
+}
+template <typename T>
+MatView<T> viewR(const Level &L);
+template <>
+MatView<double> viewR<double>(const Level &L) {
+  MatView<double> m;
+  m.n = L.elim.R.n; m.rp = L.elim.R.rp.p; m.ci = L.elim.R.ci.p; m.v = L.elim.R.v.p;
+  m.lanes_per_row = L.lanesR;
+  L.hubR64.fill(m);
+  return m;
+}
+template <>
+MatView<float> viewR<float>(const Level &L) {
+  MatView<float> m;
+  m.n = L.elim.R.n; m.rp = L.elim.R.rp.p; m.ci = L.elim.R.ci.p; m.v = L.Rv32.p;
+  m.lanes_per_row = L.lanesR;
+  L.hubR32.fill(m);
+  return m;
+}
+template <typename T>
+MatView<T> viewP(const Level &L) {
+  MatView<T> m;
+  m.n = L.elim.P.n; m.rp = L.elim.P.rp.p; m.ci = L.elim.P.ci.p;
+  if constexpr (sizeof(T) == 8) m.v = (const T *)L.elim.P.v.p;
+  else m.v = (const T *)L.Pv32.p;
+  m.lanes_per_row = L.lanesP;
+  return m;
+}
+template <typename T>
+const T *invdT(const Level &L) {
+  if constexpr (sizeof(T) == 8) return (const T *)L.invd.p;
+  else return (const T *)L.invd32.p;
+}
+template <typename T>
+const T *QT(const Level &L) {
+  if constexpr (sizeof(T) == 8) return (const T *)L.elim.Q.p;
+  else return (const T *)L.Q32.p;
+}
+template <typename T>
+const T *pinvT(const Level &L) {
+  if constexpr (sizeof(T) == 8) return (const T *)L.pinv.p;
+  else return (const T *)L.pinv32.p;
+}
+
+// per-level scalar slots (k doubles each)
+enum Slot { S_SUM = 0, S_ZQ, S_BETA, S_ETA0, S_ETA1, S_RHO, S_ALPHA, S_PQR, S_NSLOT };
+
+template <typename T>
+struct LevelWork {
+  i64 n = 0;
+  DBuf<T> in, out, r, d0, d1, xt;           // cycle buffers
+  DBuf<T> fz, fp0, fp1, fq0, fq1;           // K-cycle FCG buffers (fr = in, fx = out)
+  DBuf<double> sc, scratch;
+  i64 scratch_len = 0;
+  double *slot(int s, int k) { return sc.p + (i64)s * k * 2; }
+};
+
+template <typename T>
+struct Work {
+  int k = 0;
+  std::vector<LevelWork<T>> lw;
+};
+
+struct OuterWork {
+  int k = 0;
+  i64 n = 0;
+  DBuf<double> X, R, Z, P0, P1, Q0, Q1, B, Bfull, Xfull, Res, sc, scratch;
+  DBuf<int> frozen;
+  i64 scratch_len = 0;
+  double *slot(int s) { return sc.p + (i64)s * k * 2; }
+};
+
+}  // namespace lg
+
+struct ligmg_handle_s {
+  ligmg_options opts;
+  int device = 0;
+  cudaStream_t s = nullptr;
+  std::vector<std::unique_ptr<lg::Level>> h;
+  lg::i64 nnz0 = 0;
+  double setup_s = 0;
+  std::map<int, std::unique_ptr<lg::Work<float>>> w32;
+  std::map<int, std::unique_ptr<lg::Work<double>>> w64;
+  std::map<int, std::unique_ptr<lg::OuterWork>> ow;
+  ~ligmg_handle_s() {
+    if (s) cudaStreamSynchronize(s);
+    w32.clear();
+    w64.clear();
+    ow.clear();
+    h.clear();
+    if (s) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+  }
+};
+
+namespace lg {
+namespace {
+
+using Handle = ligmg_handle_s;
+
+void ensure_fp32(Handle &H) {
+  cudaStream_t s = H.s;
+  for (auto &Lp : H.h) {
+    Level &L = *Lp;
+    if (L.has32) continue;
+    L.Av32.alloc(L.A.nnz, s);
+    convert<double, float>(L.A.nnz, L.A.v.p, L.Av32.p, s);
+    if (L.invd.n) {
+      L.invd32.alloc(L.invd.n, s);
+      convert<double, float>(L.invd.n, L.invd.p, L.invd32.p, s);
+    }
+    if (L.type == LIGMG_LEVEL_ELIM) {
+      L.Pv32.alloc(L.elim.P.nnz, s);
+      convert<double, float>(L.elim.P.nnz, L.elim.P.v.p, L.Pv32.p, s);
+      L.Rv32.alloc(L.elim.R.nnz, s);
+      convert<double, float>(L.elim.R.nnz, L.elim.R.v.p, L.Rv32.p, s);
+      L.Q32.alloc(L.A.n, s);
+      convert<double, float>(L.A.n, L.elim.Q.p, L.Q32.p, s);
+    }
+    if (L.type == LIGMG_LEVEL_COARSE) {
+      L.pinv32.alloc(L.pinv.n, s);
+      convert<double, float>(L.pinv.n, L.pinv.p, L.pinv32.p, s);
+    }
+    std::vector<i64> rp = L.A.rp.to_host();
+    L.hubA32.build(rp.data(), L.A.n, kHubThresh, kHubChunk, kMaxK, s);
+    if (L.type == LIGMG_LEVEL_ELIM) {
+      std::vector<i64> rr = L.elim.R.rp.to_host();
+      L.hubR32.build(rr.data(), L.elim.R.n, kHubThresh, kHubChunk, kMaxK, s);
+    }
+    L.has32 = true;
+  }
+  LG_CUDA(cudaStreamSynchronize(s));
+}
+
+template <typename T>
+Work<T> &get_work(Handle &H, int k);
+template <>
+Work<float> &get_work<float>(Handle &H, int k) {
+  auto &slot = H.w32[k];
+  if (!slot) slot.reset(new Work<float>());
+  return *slot;
+}
+template <>
+Work<double> &get_work<double>(Handle &H, int k) {
+  auto &slot = H.w64[k];
+  if (!slot) slot.reset(new Work<double>());
+  return *slot;
+}
+
+template <typename T>
+Work<T> &work_for(Handle &H, int k) {
+  Work<T> &W = get_work<T>(H, k);
+  if (W.k == k) return W;
+  cudaStream_t s = H.s;
+  W.k = k;
+  W.lw.resize(H.h.size());
+  for (size_t l = 0; l < H.h.size(); l++) {
+    Level &L = *H.h[l];
+    LevelWork<T> &w = W.lw[l];
+    i64 n = L.A.n;
+    w.n = n;
+    w.in.alloc(n * k, s);
+    w.out.alloc(n * k, s);
+    if (L.type == LIGMG_LEVEL_AGG) {
+      w.r.alloc(n * k, s);
+      w.d0.alloc(n * k, s);
+      w.d1.alloc(n * k, s);
+      w.xt.alloc(n * k, s);
+      w.fz.alloc(n * k, s);
+      w.fp0.alloc(n * k, s);
+      w.fp1.alloc(n * k, s);
+      w.fq0.alloc(n * k, s);
+      w.fq1.alloc(n * k, s);
+    }
+    w.sc.alloc((i64)S_NSLOT * k * 2, s);
+    w.sc.zero();
+    w.scratch_len = col_reduce_scratch(n, k);
+    w.scratch.alloc(w.scratch_len, s);
+  }
+  return W;
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Engine {
+  Handle &H;
+  Work<T> &W;
+  int k;
+  cudaStream_t s;
+  Engine(Handle &h, Work<T> &w) : H(h), W(w), k(w.k), s(h.s) {}
+
+  const ligmg_options &o() const { return H.opts; }
+
+  void smooth(size_t l, T *x, const T *b, int iters, bool x_zero) {
+    Level &L = *H.h[l];
+    LevelWork<T> &w = W.lw[l];
+    i64 n = L.A.n;
+    MatView<T> A = viewA<T>(L);
+    const T *invd = invdT<T>(L);
+    if (o().smoother_type == LIGMG_SMOOTHER_JACOBI)
+      throw Error(LIGMG_ERR_UNSUPPORTED, "jacobi smoother in the solve phase");
+    if (iters <= 0) return;
+    const T *r_cur;
+    const T *x_cur;
+    T *d_cur;
+    T *d_other = w.d1.p;
+    if (x_zero) {
+      if (iters == 1) {
+        cheb_init_zero<T>(n, k, b, invd, L.theta, x, s);
+        return;
+      }
+      cheb_init_zero<T>(n, k, b, invd, L.theta, w.d0.p, s);
+      d_cur = w.d0.p;
+      x_cur = w.d0.p;  // x1 = d0
+      r_cur = b;       // r0 = b
+    } else {
+      EpiArgs a;
+      a.b = b; a.invd = invd; a.xin = x; a.rout = w.r.p; a.dout = w.d0.p; a.xout = w.xt.p;
+      a.theta = L.theta;
+      spmm<T>(A, x, k, Epi::ChebA, a, s);
+      d_cur = w.d0.p;
+      x_cur = w.xt.p;
+      r_cur = w.r.p;
+      if (iters == 1) {
+        LG_CUDA(cudaMemcpyAsync(x, w.xt.p, sizeof(T) * n * k, cudaMemcpyDeviceToDevice, s));
+        return;
+      }
+    }
+    for (int it = 1; it < iters; it++) {
+      bool last = it == iters - 1;
+      EpiArgs a;
+      a.invd = invd;
+      a.rin = r_cur;
+      a.din = d_cur;
+      a.xin = x_cur;
+      a.c1 = L.c1[it - 1];
+      a.c2 = L.c2[it - 1];
+      a.rout = last ? nullptr : w.r.p;
+      a.dout = last ? nullptr : d_other;
+      T *xo = last ? x : w.xt.p;
+      a.xout = xo;
+      spmm<T>(A, d_cur, k, Epi::ChebB, a, s);
+      if (!last) {
+        r_cur = w.r.p;
+        std::swap(d_cur, d_other);
+        x_cur = w.xt.p;
+      }
+    }
+  }
+
+  // x = M_l(b) with zero initial guess
+  void cycle(size_t l, const T *b, T *x) {
+    Level &L = *H.h[l];
+    i64 n = L.A.n;
+    if (L.type == LIGMG_LEVEL_COARSE) {
+      coarse_apply<T>(n, k, pinvT<T>(L), b, x, s);
+      return;
+    }
+    LevelWork<T> &nw = W.lw[l + 1];
+    if (L.type == LIGMG_LEVEL_ELIM) {  // elimination.hpp:33-52
+      EpiArgs a;
+      a.y = nw.in.p;
+      spmm<T>(viewR<T>(L), b, k, Epi::Store, a, s);
+      recurse(l, nw.in.p, nw.out.p);
+      EpiArgs c;
+      c.y = x; c.b = b; c.q = QT<T>(L);
+      spmm<T>(viewP<T>(L), nw.out.p, k, Epi::ElimInterp, c, s);
+      return;
+    }
+    // aggregation.hpp:209-241
+    LevelWork<T> &w = W.lw[l];
+    smooth(l, x, b, o().pre_smooth, true);
+    EpiArgs a;
+    a.y = w.r.p;
+    a.b = b;
+    spmm<T>(viewA<T>(L), x, k, Epi::Resid, a, s);
+    restrict_agg<T>(L.nc, k, L.agg.mrp.p, L.agg.members.p, w.r.p, nw.in.p, s);
+    recurse(l, nw.in.p, nw.out.p);
+    prolong_agg<T>(n, k, L.agg.agg.p, nw.out.p, x, s);
+    smooth(l, x, b, o().post_smooth, false);
+    if (o().constant_correction) scale_vec<T>(n, k, x, 4.0 / 3.0, s);
+  }
+
+  void recurse(size_t l, T *bc, T *xc) {
+    const Level &N = *H.h[l + 1];
+    if (!o().kcycle || N.is_exact() || N.type == LIGMG_LEVEL_COARSE) {
+      cycle(l + 1, bc, xc);
+      return;
+    }
+    fcg_fixed(l + 1, bc, xc, o().kcycle_iters);
+  }
+
+  // K-cycle inner FCG with a fixed number of iterations, x0 = 0; r = b is
+  // updated in place (b is the level's restriction buffer).
+  void fcg_fixed(size_t l, T *b, T *x, int iters) {
+    Level &L = *H.h[l];
+    LevelWork<T> &w = W.lw[l];
+    i64 n = L.A.n;
+    MatView<T> A = viewA<T>(L);
+    LG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * n * k, s));
+    T *r = b;
+    T *p = w.fp0.p, *pp = w.fp1.p, *q = w.fq0.p, *qp = w.fq1.p;
+    double *eta = w.slot(S_ETA0, k), *eta_prev = w.slot(S_ETA1, k);
+    for (int it = 0; it < iters; it++) {
+      cycle(l, r, w.fz.p);
+      col_reduce<T>(n, k, Red::Sum, w.fz.p, nullptr, w.slot(S_SUM, k), w.scratch.p,
+                    w.scratch_len, s);
+      sub_mean<T>(n, k, w.fz.p, w.slot(S_SUM, k), s);
+      if (it > 0) {
+        col_reduce<T>(n, k, Red::Dot, w.fz.p, qp, w.slot(S_ZQ, k), w.scratch.p, w.scratch_len, s);
+        scal_beta(k, w.slot(S_ZQ, k), eta_prev, w.slot(S_BETA, k), s);
+        fcg_direction<T>(n, k, p, w.fz.p, pp, w.slot(S_BETA, k), s);
+      } else {
+        fcg_direction<T>(n, k, p, w.fz.p, nullptr, nullptr, s);
+      }
+      EpiArgs a;
+      a.y = q;
+      spmm<T>(A, p, k, Epi::Store, a, s);
+      col_reduce<T>(n, k, Red::Dot, p, q, eta, w.scratch.p, w.scratch_len, s);
+      col_reduce<T>(n, k, Red::Dot, p, r, w.slot(S_RHO, k), w.scratch.p, w.scratch_len, s);
+      scal_div(k, w.slot(S_RHO, k), eta, w.slot(S_ALPHA, k), nullptr, s);
+      fcg_update<T>(n, k, x, r, p, q, w.slot(S_ALPHA, k), it + 1 < iters, s);
+      std::swap(p, pp);
+      std::swap(q, qp);
+      std::swap(eta, eta_prev);
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// setup
+void estimate_lmax(Handle &H, Level &L) {
+  cudaStream_t s = H.s;
+  i64 n = L.A.n;
+  std::vector<double> rh(n);
+  for (i64 i = 0; i < n; i++) rh[i] = est_rhs(i);
+  DBuf<double> r(n, s), z(n, s), p(n, s), q(n, s), sc(8, s);
+  i64 slen = col_reduce_scratch(n, 1);
+  DBuf<double> scratch(slen, s);
+  r.upload(rh.data(), n);
+  col_reduce<double>(n, 1, Red::Sum, r.p, nullptr, sc.p, scratch.p, slen, s);
+  sub_mean<double>(n, 1, r.p, sc.p, s);
+  k_mul_diag<<<grid_for(n, 256), 256, 0, s>>>(n, L.invd.p, r.p, z.p);
+  LG_LAUNCH();
+  LG_CUDA(cudaMemcpyAsync(p.p, z.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  col_reduce<double>(n, 1, Red::Dot, r.p, z.p, sc.p, scratch.p, slen, s);
+  double rz = read_scalar(sc.p, s);
+  MatView<double> A = viewA<double>(L);
+  std::vector<double> alphas, betas;
+  for (int it = 0; it < 5; it++) {
+    if (!(rz > 0)) break;
+    EpiArgs a;
+    a.y = q.p;
+    spmm<double>(A, p.p, 1, Epi::Store, a, s);
+    col_reduce<double>(n, 1, Red::Dot, p.p, q.p, sc.p, scratch.p, slen, s);
+    double pq = read_scalar(sc.p, s);
+    if (!(pq > 0)) break;
+    double alpha = rz / pq;
+    LG_CUDA(cudaMemcpyAsync(sc.p + 1, &alpha, sizeof(double), cudaMemcpyHostToDevice, s));
+    axpby_cols<double>(n, 1, r.p, q.p, sc.p + 1, -1.0, 1.0, s);
+    k_mul_diag<<<grid_for(n, 256), 256, 0, s>>>(n, L.invd.p, r.p, z.p);
+    LG_LAUNCH();
+    col_reduce<double>(n, 1, Red::Dot, r.p, z.p, sc.p, scratch.p, slen, s);
+    double rz_new = read_scalar(sc.p, s);
+    double beta = rz_new / rz;
+    rz = rz_new;
+    LG_CUDA(cudaMemcpyAsync(sc.p + 2, &beta, sizeof(double), cudaMemcpyHostToDevice, s));
+    cg_direction<double>(n, 1, p.p, z.p, sc.p + 2, s);
+    alphas.push_back(alpha);
+    betas.push_back(beta);
+    LG_CUDA(cudaStreamSynchronize(s));
+  }
+  int m = (int)alphas.size();
+  if (m == 0) {
+    L.lmax = 2.0;
+  } else {
+    std::vector<double> d(m), e(m > 1 ? m - 1 : 0);
+    for (int kk = 0; kk < m; kk++) {
+      d[kk] = 1.0 / alphas[kk] + (kk > 0 ? betas[kk - 1] / alphas[kk - 1] : 0.0);
+      if (kk + 1 < m) e[kk] = std::sqrt(betas[kk]) / alphas[kk];
+    }
+    L.lmax = tridiag_lmax(d, e);
+  }
+}
+
+void setup_smoother_params(const ligmg_options &o, Level &L) {
+  double a = o.cheby_lower * L.lmax, bb = o.cheby_upper * L.lmax;
+  double theta = (bb + a) / 2, delta = (bb - a) / 2;
+  double sigma = theta / delta, rho = 1 / sigma;
+  L.theta = theta;
+  L.delta = delta;
+  int m = std::max(o.pre_smooth, o.post_smooth);
+  L.c1.assign(std::max(m, 1), 0.0);
+  L.c2.assign(std::max(m, 1), 0.0);
+  for (int kk = 0; kk + 1 < m; kk++) {
+    double rho_new = 1 / (2 * sigma - rho);
+    L.c1[kk] = rho_new * rho;
+    L.c2[kk] = 2 * rho_new / delta;
+    rho = rho_new;
+  }
+}
+
+void finish_level(Handle &H, Level &L) {
+  cudaStream_t s = H.s;
+  L.invd.alloc(L.A.n, s);
+  k_invdiag<<<grid_for(L.A.n, 256), 256, 0, s>>>(L.A.rp.p, L.A.ci.p, L.A.v.p, L.A.n, L.invd.p);
+  LG_LAUNCH();
+  L.lanesA = lanes_for(L.A.nnz, L.A.n);
+  std::vector<i64> rp = L.A.rp.to_host();
+  L.hubA64.build(rp.data(), L.A.n, kHubThresh, kHubChunk, kMaxK, s);
+  if (L.type == LIGMG_LEVEL_ELIM) {
+    std::vector<i64> rr = L.elim.R.rp.to_host();
+    L.hubR64.build(rr.data(), L.elim.R.n, kHubThresh, kHubChunk, kMaxK, s);
+    L.lanesR = lanes_for(L.elim.R.nnz, L.elim.R.n);
+    L.lanesP = lanes_for(L.elim.P.nnz, L.elim.P.n);
+  }
+}
+
+void make_hierarchy(Handle &H, i64 n, const i64 *rowptr, const i32 *col, const double *val) {
+  const ligmg_options &o = H.opts;
+  cudaStream_t s = H.s;
+  auto t0 = std::chrono::steady_clock::now();
+  i64 nnz = rowptr[n];
+  DCsr<double> cur;
+  cur.n = cur.m = n;
+  cur.nnz = nnz;
+  cur.rp.alloc(n + 1, s);
+  cur.ci.alloc(nnz, s);
+  cur.v.alloc(nnz, s);
+  cur.rp.upload(rowptr, n + 1);
+  cur.ci.upload(col, nnz);
+  cur.v.upload(val, nnz);
+  ligmg_status st = gpu_validate(cur, s);
+  if (st != LIGMG_OK) throw Error(st, "input validation");
+  H.nnz0 = nnz;
+  GlibcRand rng(o.seed);
+  for (i64 i = 0; i < o.rng_skip; i++) rng.next();
+  AggParams ap;
+  ap.num_tvs = o.num_tvs;
+  ap.tvs_smooth = o.tvs_smooth;
+  ap.agg_iters = o.agg_iters;
+  ap.strength_metric = o.strength_metric;
+  ap.aff_scaling = o.aff_scaling;
+  ap.neighbor_of_neighbor = o.neighbor_of_neighbor != 0;
+  ap.thresh = o.thresh;
+  ap.agg_init_factor = o.agg_init_factor;
+  ap.agg_iter_factor = o.agg_iter_factor;
+  ap.votes_to_seed = (double)o.votes_to_seed;
+  ap.max_agg_size = (double)o.max_agg_size;
+  auto &h = H.h;
+  while ((int)h.size() < o.max_levels && (h.empty() || h.back()->A.nnz > o.min_size)) {
+    if (o.always_elim && o.elim_iters >= 1) {
+      auto E = std::make_unique<Level>();
+      E->type = LIGMG_LEVEL_ELIM;
+      gpu_elimination(cur, o.elim_degree, o.elim_factor, E->elim, s);
+      if (E->elim.accepted) {
+        DCsr<double> next;
+        gpu_galerkin(cur, E->elim.P, next, s);
+        E->A = std::move(cur);
+        E->nc = E->elim.nc;
+        finish_level(H, *E);
+        h.push_back(std::move(E));
+        cur = std::move(next);
+      }
+    }
+    auto G = std::make_unique<Level>();
+    G->type = LIGMG_LEVEL_AGG;
+    i64 cn = cur.n;
+    std::vector<double> tvs;
+    bool need_tvs = o.strength_metric == LIGMG_STRENGTH_AFFINITY ||
+                    o.strength_metric == LIGMG_STRENGTH_ALGEBRAIC_DISTANCE;
+    if (need_tvs) {  // create_tvs (aggregation.hpp:24-36)
+      tvs.resize((size_t)o.num_tvs * cn);
+      for (int t = 0; t < o.num_tvs; t++) {
+        double *x = tvs.data() + (size_t)t * cn;
+        for (i64 i = 0; i < cn; i++) x[i] = double(rng.next()) / 2147483647;
+        double sm = 0.0;
+        for (i64 i = 0; i < cn; i++) sm += x[i];
+        sm = sm / (double)cn;
+        for (i64 i = 0; i < cn; i++) x[i] = x[i] - sm;
+      }
+    }
+    gpu_aggregation(cur, ap, tvs.data(), G->agg, s);
+    G->nc = G->agg.nc;
+    DCsr<double> next;
+    gpu_galerkin_agg(cur, G->agg.agg.p, G->nc, next, s);
+    G->A = std::move(cur);
+    finish_level(H, *G);
+    estimate_lmax(H, *G);
+    setup_smoother_params(o, *G);
+    h.push_back(std::move(G));
+    cur = std::move(next);
+  }
+  auto C = std::make_unique<Level>();
+  C->type = LIGMG_LEVEL_COARSE;
+  C->A = std::move(cur);
+  st = gpu_coarse_pinv(C->A, C->pinv, s);
+  if (st != LIGMG_OK) throw Error(st, "coarse pseudo-inverse");
+  finish_level(H, *C);
+  h.push_back(std::move(C));
+  LG_CUDA(cudaStreamSynchronize(s));
+  H.setup_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+double cycle_complexity(Handle &H, int start) {  // multigrid.hpp:372-387
+  double sm = 0;
+  i64 iters = 1;
+  for (size_t i = start; i < H.h.size(); i++) {
+    sm += (double)(iters * H.h[i]->work(H.opts));
+    if (!H.h[i]->is_exact() && H.opts.kcycle) iters *= H.opts.kcycle_iters;
+  }
+  return sm / (double)H.nnz0;
+}
+
+// ---------------------------------------------------------------------------
+// outer solve on device arrays B (n0 x k, FP64) -> X (n0 x k)
+OuterWork &outer_work(Handle &H, int k, i64 nb, i64 n0) {
+  auto &slot = H.ow[k];
+  if (!slot) slot.reset(new OuterWork());
+  OuterWork &w = *slot;
+  if (w.k == k && w.n == nb) return w;
+  cudaStream_t s = H.s;
+  w.k = k;
+  w.n = nb;
+  for (DBuf<double> *b : {&w.X, &w.R, &w.Z, &w.P0, &w.P1, &w.Q0, &w.Q1, &w.B})
+    b->alloc(nb * k, s);
+  w.Bfull.alloc(n0 * k, s);
+  w.Xfull.alloc(n0 * k, s);
+  w.Res.alloc(n0 * k, s);
+  w.sc.alloc((i64)(S_NSLOT + 4) * k * 2, s);
+  w.sc.zero();
+  w.scratch_len = std::max(col_reduce_scratch(nb, k), col_reduce_scratch(n0, k));
+  w.scratch.alloc(w.scratch_len, s);
+  w.frozen.alloc(k, s);
+  return w;
+}
+
+template <typename T>
+void apply_prec(Handle &H, int k, size_t base, const double *r, double *z) {
+  Level &L = *H.h[base];
+  i64 n = L.A.n;
+  Work<T> &W = work_for<T>(H, k);
+  Engine<T> E(H, W);
+  if constexpr (sizeof(T) == 8) {
+    E.cycle(base, r, z);
+  } else {
+    LevelWork<T> &w = W.lw[base];
+    convert<double, float>(n * k, r, w.in.p, H.s);
+    E.cycle(base, w.in.p, w.out.p);
+    convert<float, double>(n * k, w.out.p, z, H.s);
+  }
+}
+
+struct SolveResult {
+  int iters = 0;
+  bool converged = false;
+  std::vector<double> hist0;
+  std::vector<int> col_iters;
+  std::vector<double> rel;  // last/first per column
+};
+
+// Outer Krylov (petsc_fcg, cg.hpp:18-116) with k columns; r0 = b (x0 = 0).
+template <typename T>
+SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
+  const ligmg_options &o = H.opts;
+  cudaStream_t s = H.s;
+  Level &L = *H.h[base];
+  i64 n = L.A.n;
+  MatView<double> A = viewA<double>(L);
+  SolveResult res;
+  res.col_iters.assign(k, 0);
+  res.rel.assign(k, 1.0);
+  double *sum = w.slot(S_SUM), *tmp = w.slot(S_ZQ), *beta = w.slot(S_BETA);
+  double *eta = w.slot(S_ETA0), *eta_prev = w.slot(S_ETA1), *rho = w.slot(S_RHO);
+  double *alpha = w.slot(S_ALPHA), *rn2 = w.slot(S_PQR), *bcg = w.slot(S_NSLOT),
+         *bcg_old = w.slot(S_NSLOT + 1);
+  // project the constant out of the right-hand side
+  col_reduce<double>(n, k, Red::Sum, w.B.p, nullptr, sum, w.scratch.p, w.scratch_len, s);
+  sub_mean<double>(n, k, w.B.p, sum, s);
+  LG_CUDA(cudaMemsetAsync(w.X.p, 0, sizeof(double) * n * k, s));
+  LG_CUDA(cudaMemcpyAsync(w.R.p, w.B.p, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, s));
+  LG_CUDA(cudaMemsetAsync(w.frozen.p, 0, sizeof(int) * k, s));
+  col_reduce<double>(n, k, Red::Dot, w.R.p, w.R.p, rn2, w.scratch.p, w.scratch_len, s);
+  std::vector<double> h_rn2(k), rn0(k);
+  LG_CUDA(cudaMemcpyAsync(h_rn2.data(), rn2, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  LG_CUDA(cudaStreamSynchronize(s));
+  std::vector<int> frozen(k, 0);
+  int active = 0;
+  for (int c = 0; c < k; c++) {
+    rn0[c] = std::sqrt(h_rn2[c]);
+    if (rn0[c] == 0) frozen[c] = 1; else active++;
+  }
+  res.hist0.push_back(rn0[0]);
+  LG_CUDA(cudaMemcpyAsync(w.frozen.p, frozen.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
+  bool cg = o.outer_ksp_type == LIGMG_KSP_CG;
+  double *P = w.P0.p, *PP = w.P1.p, *Q = w.Q0.p, *QP = w.Q1.p;
+  auto precondition = [&]() {
+    apply_prec<T>(H, k, base, w.R.p, w.Z.p);
+    col_reduce<double>(n, k, Red::Sum, w.Z.p, nullptr, sum, w.scratch.p, w.scratch_len, s);
+    sub_mean<double>(n, k, w.Z.p, sum, s);
+  };
+  if (cg && active) {
+    precondition();
+    col_reduce<double>(n, k, Red::Dot, w.Z.p, w.R.p, bcg, w.scratch.p, w.scratch_len, s);
+  }
+  int it = 0;
+  for (; it < o.iters && active > 0; it++) {
+    if (cg) {  // KSPCG
+      if (it == 0) {
+        LG_CUDA(cudaMemcpyAsync(P, w.Z.p, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, s));
+      } else {
+        scal_div(k, bcg, bcg_old, beta, nullptr, s);
+        cg_direction<double>(n, k, P, w.Z.p, beta, s);
+      }
+      EpiArgs a;
+      a.y = Q;
+      spmm<double>(A, P, k, Epi::Store, a, s);
+      col_reduce<double>(n, k, Red::Dot, P, Q, eta, w.scratch.p, w.scratch_len, s);
+      scal_div(k, bcg, eta, alpha, w.frozen.p, s);
+      fcg_update<double>(n, k, w.X.p, w.R.p, P, Q, alpha, true, s);
+    } else {  // FCG (Notay), one stored direction
+      precondition();
+      if (it > 0) {
+        col_reduce<double>(n, k, Red::Dot, w.Z.p, QP, tmp, w.scratch.p, w.scratch_len, s);
+        scal_beta(k, tmp, eta_prev, beta, s);
+        fcg_direction<double>(n, k, P, w.Z.p, PP, beta, s);
+      } else {
+        fcg_direction<double>(n, k, P, w.Z.p, nullptr, nullptr, s);
+      }
+      EpiArgs a;
+      a.y = Q;
+      spmm<double>(A, P, k, Epi::Store, a, s);
+      col_reduce<double>(n, k, Red::Dot, P, Q, eta, w.scratch.p, w.scratch_len, s);
+      col_reduce<double>(n, k, Red::Dot, P, w.R.p, rho, w.scratch.p, w.scratch_len, s);
+      scal_div(k, rho, eta, alpha, w.frozen.p, s);
+      fcg_update<double>(n, k, w.X.p, w.R.p, P, Q, alpha, true, s);
+      std::swap(P, PP);
+      std::swap(Q, QP);
+      std::swap(eta, eta_prev);
+    }
+    col_reduce<double>(n, k, Red::Dot, w.R.p, w.R.p, rn2, w.scratch.p, w.scratch_len, s);
+    LG_CUDA(cudaMemcpyAsync(h_rn2.data(), rn2, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+    LG_CUDA(cudaStreamSynchronize(s));
+    bool changed = false;
+    for (int c = 0; c < k; c++) {
+      if (frozen[c]) continue;
+      double rn = std::sqrt(h_rn2[c]);
+      res.col_iters[c] = it + 1;
+      res.rel[c] = rn / rn0[c];
+      if (c == 0) res.hist0.push_back(rn);
+      if (!std::isfinite(rn)) throw Error(LIGMG_ERR_BREAKDOWN, "non-finite residual");
+      if (rn <= std::max(o.tol * rn0[c], 1e-60)) {
+        frozen[c] = 1;
+        active--;
+        changed = true;
+      }
+    }
+    if (changed)
+      LG_CUDA(cudaMemcpyAsync(w.frozen.p, frozen.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
+    if (cg && active > 0) {
+      precondition();
+      LG_CUDA(cudaMemcpyAsync(bcg_old, bcg, sizeof(double) * k, cudaMemcpyDeviceToDevice, s));
+      col_reduce<double>(n, k, Red::Dot, w.Z.p, w.R.p, bcg, w.scratch.p, w.scratch_len, s);
+    }
+  }
+  res.iters = it;
+  res.converged = active == 0;
+  return res;
+}
+
+// full solve: B (n0 x k) in w.Bfull -> w.Xfull; fills info
+ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *dX,
+                          ligmg_info *info) {
+  auto t0 = std::chrono::steady_clock::now();
+  cudaStream_t s = H.s;
+  if (from < 0 || from >= (int)H.h.size()) throw Error(LIGMG_ERR_INVALID_ARGUMENT, "from");
+  Level &F = *H.h[from];
+  i64 n0 = F.A.n;
+  bool do_once = H.opts.top_elim && F.type == LIGMG_LEVEL_ELIM;  // multigrid.hpp:322
+  size_t base = do_once ? from + 1 : from;
+  i64 nb = H.h[base]->A.n;
+  if (H.h[base]->type == LIGMG_LEVEL_COARSE && H.h.size() == 1)
+    ;  // single coarse level: the pseudo-inverse is the preconditioner
+  OuterWork &w = outer_work(H, k, nb, n0);
+  LG_CUDA(cudaMemcpyAsync(w.Bfull.p, dB, sizeof(double) * n0 * k, cudaMemcpyDeviceToDevice, s));
+  if (do_once) {
+    EpiArgs a;
+    a.y = w.B.p;
+    spmm<double>(viewR<double>(F), w.Bfull.p, k, Epi::Store, a, s);
+  } else {
+    LG_CUDA(cudaMemcpyAsync(w.B.p, w.Bfull.p, sizeof(double) * n0 * k, cudaMemcpyDeviceToDevice, s));
+  }
+  SolveResult res = (H.opts.precision == LIGMG_PREC_FP32) ? outer_solve<float>(H, base, w, k)
+                                                          : outer_solve<double>(H, base, w, k);
+  if (do_once) {  // x = P x + Q b (:349-354)
+    EpiArgs c;
+    c.y = w.Xfull.p; c.b = w.Bfull.p; c.q = F.elim.Q.p;
+    spmm<double>(viewP<double>(F), w.X.p, k, Epi::ElimInterp, c, s);
+  } else {
+    LG_CUDA(cudaMemcpyAsync(w.Xfull.p, w.X.p, sizeof(double) * n0 * k, cudaMemcpyDeviceToDevice, s));
+  }
+  LG_CUDA(cudaMemcpyAsync(dX, w.Xfull.p, sizeof(double) * n0 * k, cudaMemcpyDeviceToDevice, s));
+  // true residual ||b - L x|| / ||b|| with b's constant projected out
+  double *sum = w.slot(S_SUM), *d1 = w.slot(S_ZQ), *d2 = w.slot(S_BETA);
+  col_reduce<double>(n0, k, Red::Sum, w.Bfull.p, nullptr, sum, w.scratch.p, w.scratch_len, s);
+  sub_mean<double>(n0, k, w.Bfull.p, sum, s);
+  EpiArgs a;
+  a.y = w.Res.p;
+  a.b = w.Bfull.p;
+  spmm<double>(viewA<double>(F), w.Xfull.p, k, Epi::Resid, a, s);
+  col_reduce<double>(n0, k, Red::Dot, w.Res.p, w.Res.p, d1, w.scratch.p, w.scratch_len, s);
+  col_reduce<double>(n0, k, Red::Dot, w.Bfull.p, w.Bfull.p, d2, w.scratch.p, w.scratch_len, s);
+  std::vector<double> h1(k), h2(k);
+  LG_CUDA(cudaMemcpyAsync(h1.data(), d1, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  LG_CUDA(cudaMemcpyAsync(h2.data(), d2, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  LG_CUDA(cudaStreamSynchronize(s));
+  double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (info) {
+    double worst_true = 0, worst_rel = 0;
+    for (int c = 0; c < k; c++) {
+      double tr = h2[c] > 0 ? std::sqrt(h1[c]) / std::sqrt(h2[c]) : 0.0;
+      worst_true = std::max(worst_true, tr);
+      worst_rel = std::max(worst_rel, res.rel[c]);
+      if (info->col_iters) info->col_iters[c] = res.col_iters[c];
+      if (info->col_true_rel_residual) info->col_true_rel_residual[c] = tr;
+    }
+    info->iters = res.iters;
+    info->converged = res.converged ? 1 : 0;
+    info->rel_residual = worst_rel;
+    info->true_rel_residual = worst_true;
+    info->cycle_complexity = cycle_complexity(H, (int)base);
+    info->work = res.iters * (1 + info->cycle_complexity);
+    info->solve_seconds = secs;
+    info->setup_seconds = H.setup_s;
+    info->history_len = 0;
+    if (info->residual_history && info->history_capacity > 0) {
+      int m = std::min((int)res.hist0.size(), info->history_capacity);
+      std::copy(res.hist0.begin(), res.hist0.begin() + m, info->residual_history);
+      info->history_len = m;
+    }
+  }
+  return res.converged ? LIGMG_OK : LIGMG_NOT_CONVERGED;
+}
+
+bool k_supported(int k) {
+  return k == 1 || k == 2 || k == 4 || k == 8 || k == 16 || k == 32 || k == 64;
+}
+
+template <typename F>
+ligmg_status guard(F &&f) {
+  try {
+    return f();
+  } catch (const Error &e) {
+    return e.status;
+  } catch (const std::bad_alloc &) {
+    return LIGMG_ERR_OUT_OF_MEMORY;
+  } catch (...) {
+    return LIGMG_ERR_INTERNAL;
+  }
+}
+
+}  // namespace
+}  // namespace lg
+
+using namespace lg;
+
+extern "C" {
+
+void ligmg_default_options(ligmg_options *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->max_levels = 50;
+  o->always_elim = 1;
+  o->min_size = 4000;
+  o->top_elim = 1;
+  o->elim_degree = 4;
+  o->elim_factor = 0.9;
+  o->elim_iters = 1;
+  o->iters = 500;
+  o->tol = 1e-8;
+  o->thresh = 1e-8;
+  o->agg_iters = 10;
+  o->num_tvs = 10;
+  o->agg_init_factor = 0.5;
+  o->agg_iter_factor = 0.5;
+  o->votes_to_seed = 1;
+  o->max_agg_size = -1;
+  o->rejection_ratio = -1;
+  o->rejection_to_seed = 0;
+  o->neighbor_of_neighbor = 0;
+  o->tvs_smooth = 4;
+  o->strength_metric = LIGMG_STRENGTH_AFFINITY;
+  o->aff_scaling = LIGMG_AFF_MAX;
+  o->pre_smooth = 2;
+  o->post_smooth = 2;
+  o->smoother_type = LIGMG_SMOOTHER_CHEBYSHEV;
+  o->cheby_lower = 0.3;
+  o->cheby_upper = 1.1;
+  o->constant_correction = 0;
+  o->kcycle = 0;
+  o->kcycle_iters = 2;
+  o->outer_ksp_type = LIGMG_KSP_CG;
+  o->kcycle_ksp_type = LIGMG_KSP_FCG;
+  o->precision = LIGMG_PREC_FP64;
+  o->seed = 0;
+  o->fcg_mmax = 1;
+  o->rng_skip = 0;
+  o->verbose = 0;
+  o->device = 0;
+}
+
+const char *ligmg_status_string(ligmg_status s) {
+  switch (s) {
+    case LIGMG_OK: return "ok";
+    case LIGMG_NOT_CONVERGED: return "not converged (iteration limit reached)";
+    case LIGMG_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case LIGMG_ERR_NOT_SYMMETRIC: return "matrix not symmetric";
+    case LIGMG_ERR_BAD_DIAGONAL: return "missing or non-positive diagonal";
+    case LIGMG_ERR_POSITIVE_OFFDIAG: return "positive off-diagonal entry";
+    case LIGMG_ERR_NONFINITE: return "non-finite value";
+    case LIGMG_ERR_DISCONNECTED: return "graph is disconnected";
+    case LIGMG_ERR_CUDA: return "CUDA error";
+    case LIGMG_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case LIGMG_ERR_BREAKDOWN: return "Krylov breakdown";
+    case LIGMG_ERR_UNSUPPORTED: return "unsupported option combination";
+    case LIGMG_ERR_INTERNAL: return "internal error";
+    case LIGMG_ERR_NOT_SORTED: return "CSR columns not sorted";
+    default: return "unknown status";
+  }
+}
+
+ligmg_status ligmg_create(int64_t n, const int64_t *rowptr, const int32_t *col,
+                          const double *val, const ligmg_options *opts, ligmg_handle *out) {
+  if (!out) return LIGMG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (n <= 0 || n >= INT32_MAX || !rowptr || !col || !val) return LIGMG_ERR_INVALID_ARGUMENT;
+  if (rowptr[0] != 0 || rowptr[n] < n) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    std::unique_ptr<Handle> H(new Handle());
+    if (opts) H->opts = *opts; else ligmg_default_options(&H->opts);
+    const ligmg_options &o = H->opts;
+    if (o.kcycle_iters < 1 || o.num_tvs < 0 || o.max_levels < 1 || o.iters < 0 ||
+        (o.precision != LIGMG_PREC_FP64 && o.precision != LIGMG_PREC_FP32))
+      return LIGMG_ERR_INVALID_ARGUMENT;
+    if (o.smoother_type != LIGMG_SMOOTHER_CHEBYSHEV || o.outer_ksp_type > LIGMG_KSP_FCG ||
+        o.kcycle_ksp_type != LIGMG_KSP_FCG || o.max_agg_size > 0 || o.rejection_ratio >= 0 ||
+        o.elim_iters > 1 || (o.aff_scaling != LIGMG_AFF_MAX && o.aff_scaling != LIGMG_AFF_NONE))
+      return LIGMG_ERR_UNSUPPORTED;
+    H->device = o.device;
+    LG_CUDA(cudaSetDevice(H->device));
+    LG_CUDA(cudaStreamCreateWithFlags(&H->s, cudaStreamNonBlocking));
+    make_hierarchy(*H, n, rowptr, col, val);
+    *out = H.release();
+    return LIGMG_OK;
+  });
+}
+
+ligmg_status ligmg_destroy(ligmg_handle h) {
+  if (!h) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    cudaSetDevice(h->device);
+    delete h;
+    return LIGMG_OK;
+  });
+}
+
+ligmg_status ligmg_solve_batched_device(ligmg_handle h, const double *dB, int32_t k, double *dX,
+                                        ligmg_info *info) {
+  if (!h || !dB || !dX || !k_supported(k)) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    if (h->opts.precision == LIGMG_PREC_FP32) ensure_fp32(*h);
+    return solve_device(*h, k, 0, dB, dX, info);
+  });
+}
+
+static ligmg_status solve_host(ligmg_handle h, const double *B, int32_t k, double *X, int from,
+                               ligmg_info *info) {
+  if (!h || !B || !X || !k_supported(k)) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    if (from < 0 || from >= (int)h->h.size()) return LIGMG_ERR_INVALID_ARGUMENT;
+    if (h->opts.precision == LIGMG_PREC_FP32) ensure_fp32(*h);
+    i64 n = h->h[from]->A.n;
+    DBuf<double> dB(n * k, h->s), dX(n * k, h->s);
+    dB.upload(B, n * k);
+    ligmg_status st = solve_device(*h, k, from, dB.p, dX.p, info);
+    dX.download(X, n * k);
+    LG_CUDA(cudaStreamSynchronize(h->s));
+    return st;
+  });
+}
+
+ligmg_status ligmg_solve(ligmg_handle h, const double *b, double *x, ligmg_info *info) {
+  return solve_host(h, b, 1, x, 0, info);
+}
+ligmg_status ligmg_solve_from(ligmg_handle h, const double *b, double *x, int32_t from,
+                              ligmg_info *info) {
+  return solve_host(h, b, 1, x, from, info);
+}
+ligmg_status ligmg_solve_batched(ligmg_handle h, const double *B, int32_t k, double *X,
+                                 ligmg_info *info) {
+  return solve_host(h, B, k, X, 0, info);
+}
+
+ligmg_status ligmg_hierarchy_levels(ligmg_handle h, int32_t *num_levels) {
+  if (!h || !num_levels) return LIGMG_ERR_INVALID_ARGUMENT;
+  *num_levels = (int32_t)h->h.size();
+  return LIGMG_OK;
+}
+
+ligmg_status ligmg_level_info(ligmg_handle h, int32_t level, int32_t *type, int64_t *n,
+                              int64_t *nnz, int64_t *nc) {
+  if (!h || level < 0 || level >= (int)h->h.size()) return LIGMG_ERR_INVALID_ARGUMENT;
+  const Level &L = *h->h[level];
+  if (type) *type = L.type;
+  if (n) *n = L.A.n;
+  if (nnz) *nnz = L.A.nnz;
+  if (nc) *nc = L.nc;
+  return LIGMG_OK;
+}
+
+ligmg_status ligmg_level_matrix(ligmg_handle h, int32_t level, int64_t *rowptr, int32_t *col,
+                                double *val) {
+  if (!h || level < 0 || level >= (int)h->h.size() || !rowptr || !col || !val)
+    return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    const Level &L = *h->h[level];
+    L.A.rp.download(rowptr, L.A.n + 1);
+    L.A.ci.download(col, L.A.nnz);
+    L.A.v.download(val, L.A.nnz);
+    LG_CUDA(cudaStreamSynchronize(h->s));
+    return LIGMG_OK;
+  });
+}
+
+ligmg_status ligmg_level_ids(ligmg_handle h, int32_t level, int32_t *ids) {
+  if (!h || level < 0 || level >= (int)h->h.size() || !ids) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    const Level &L = *h->h[level];
+    if (L.type == LIGMG_LEVEL_ELIM) L.elim.new_id.download(ids, L.A.n);
+    else if (L.type == LIGMG_LEVEL_AGG) L.agg.agg.download(ids, L.A.n);
+    else return LIGMG_ERR_INVALID_ARGUMENT;
+    LG_CUDA(cudaStreamSynchronize(h->s));
+    return LIGMG_OK;
+  });
+}
+
+ligmg_status ligmg_level_lmax(ligmg_handle h, int32_t level, double *lmax) {
+  if (!h || level < 0 || level >= (int)h->h.size() || !lmax) return LIGMG_ERR_INVALID_ARGUMENT;
+  *lmax = h->h[level]->lmax;
+  return LIGMG_OK;
+}
+
+ligmg_status ligmg_cycle(ligmg_handle h, int32_t level, const double *b, double *x) {
+  if (!h || level < 0 || level >= (int)h->h.size() || !b || !x) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    if (h->opts.precision == LIGMG_PREC_FP32) ensure_fp32(*h);
+    i64 n = h->h[level]->A.n;
+    DBuf<double> db(n, h->s), dx(n, h->s);
+    db.upload(b, n);
+    if (h->opts.precision == LIGMG_PREC_FP32) {
+      Work<float> &W = work_for<float>(*h, 1);
+      Engine<float> E(*h, W);
+      LevelWork<float> &w = W.lw[level];
+      convert<double, float>(n, db.p, w.in.p, h->s);
+      E.cycle(level, w.in.p, w.out.p);
+      convert<float, double>(n, w.out.p, dx.p, h->s);
+    } else {
+      Work<double> &W = work_for<double>(*h, 1);
+      Engine<double> E(*h, W);
+      E.cycle(level, db.p, dx.p);
+    }
+    dx.download(x, n);
+    LG_CUDA(cudaStreamSynchronize(h->s));
+    return LIGMG_OK;
+  });
+}
+
+ligmg_status ligmg_spmv(ligmg_handle h, int32_t level, const double *x, double *y) {
+  if (!h || level < 0 || level >= (int)h->h.size() || !x || !y) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    const Level &L = *h->h[level];
+    i64 n = L.A.n;
+    DBuf<double> dx(n, h->s), dy(n, h->s);
+    dx.upload(x, n);
+    EpiArgs a;
+    a.y = dy.p;
+    spmm<double>(viewA<double>(L), dx.p, 1, Epi::Store, a, h->s);
+    dy.download(y, n);
+    LG_CUDA(cudaStreamSynchronize(h->s));
+    return LIGMG_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,611 @@
+// solve.cu — solve-phase kernels for sm_103a.
+//
+// SpMM layout: X is n x k row-major.  A row is processed by a group of G lanes
+// (G = 32 for k > 1).  Inside a group, L = k / VW lanes cover the k columns of
+// one matrix entry with 16-byte vector loads (VW = 4 floats or 2 doubles) and
+// E = G / L entries are in flight per step; partial sums of the E entry slots
+// are combined with warp shuffles and the first L lanes run the fused
+// epilogue on their VW columns.  The matrix is read once per k vectors.
+#include <algorithm>
+
+#include "solve.cuh"
+
+namespace lg {
+
+// ---------------------------------------------------------------------------
+template <typename T>
+void HubPlan<T>::build(const i64 *rp_host, i64 n, i64 thr, i64 chunk, int kmax, cudaStream_t s) {
+  thresh = thr;
+  std::vector<i64> row, beg, end;
+  std::vector<i32> hub, first, cnt;
+  nhubs = 0;
+  for (i64 r = 0; r < n; r++) {
+    i64 len = rp_host[r + 1] - rp_host[r];
+    if (len <= thr) continue;
+    i32 nc = (i32)cdiv(len, chunk);
+    i32 f = (i32)row.size();
+    for (i32 c = 0; c < nc; c++) {
+      row.push_back(r);
+      beg.push_back(rp_host[r] + c * chunk);
+      end.push_back(std::min(rp_host[r + 1], rp_host[r] + (c + 1) * chunk));
+      hub.push_back((i32)nhubs);
+      first.push_back(f);
+      cnt.push_back(nc);
+    }
+    nhubs++;
+  }
+  nchunks = (i64)row.size();
+  kcap = kmax;
+  if (nchunks == 0) {
+    thresh = 0;
+    return;
+  }
+  auto up64 = [&](DBuf<i64> &d, const std::vector<i64> &h) { d.alloc((i64)h.size(), s); d.upload(h.data(), (i64)h.size()); };
+  auto up32 = [&](DBuf<i32> &d, const std::vector<i32> &h) { d.alloc((i64)h.size(), s); d.upload(h.data(), (i64)h.size()); };
+  up64(this->row, row);
+  up64(this->beg, beg);
+  up64(this->end, end);
+  up32(this->hub, hub);
+  up32(this->first, first);
+  up32(this->cnt, cnt);
+  counter.alloc(nhubs, s);
+  counter.zero();
+  partial.alloc(nchunks * kmax, s);
+  LG_CUDA(cudaStreamSynchronize(s));
+}
+
+template <typename T>
+void HubPlan<T>::fill(MatView<T> &m) const {
+  m.hub_thresh = thresh;
+  m.nchunks = nchunks;
+  m.ch_row = row.p;
+  m.ch_beg = beg.p;
+  m.ch_end = end.p;
+  m.ch_hub = hub.p;
+  m.ch_first = first.p;
+  m.ch_cnt = cnt.p;
+  m.hub_counter = counter.p;
+  m.partial = partial.p;
+}
+template struct HubPlan<float>;
+template struct HubPlan<double>;
+
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename T>
+struct VT;
+template <>
+struct VT<float> {
+  static constexpr int W = 4;
+};
+template <>
+struct VT<double> {
+  static constexpr int W = 2;
+};
+
+template <typename T, int VW>
+__device__ __forceinline__ void vload(const T *p, T (&o)[VW]) {
+  if constexpr (VW == 4 && sizeof(T) == 4) {
+    float4 t = *reinterpret_cast<const float4 *>(p);
+    o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+  } else if constexpr (VW == 2 && sizeof(T) == 8) {
+    double2 t = *reinterpret_cast<const double2 *>(p);
+    o[0] = t.x; o[1] = t.y;
+  } else {
+#pragma unroll
+    for (int q = 0; q < VW; q++) o[q] = p[q];
+  }
+}
+template <typename T, int VW>
+__device__ __forceinline__ void vldg(const T *p, T (&o)[VW]) {
+  if constexpr (VW == 4 && sizeof(T) == 4) {
+    float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+    o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+  } else if constexpr (VW == 2 && sizeof(T) == 8) {
+    double2 t = __ldg(reinterpret_cast<const double2 *>(p));
+    o[0] = t.x; o[1] = t.y;
+  } else {
+#pragma unroll
+    for (int q = 0; q < VW; q++) o[q] = __ldg(p + q);
+  }
+}
+template <typename T, int VW>
+__device__ __forceinline__ void vstore(T *p, const T (&o)[VW]) {
+  if constexpr (VW == 4 && sizeof(T) == 4) {
+    *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
+  } else if constexpr (VW == 2 && sizeof(T) == 8) {
+    *reinterpret_cast<double2 *>(p) = make_double2(o[0], o[1]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < VW; q++) p[q] = o[q];
+  }
+}
+
+template <typename T, int K, int VW, Epi E>
+__device__ __forceinline__ void epilogue(const EpiArgs &a, i64 r, int c0, T (&acc)[VW]) {
+  const i64 off = r * K + c0;
+  if constexpr (E == Epi::Store) {
+    vstore<T, VW>((T *)a.y + off, acc);
+  } else if constexpr (E == Epi::Resid) {
+    T b[VW];
+    vload<T, VW>((const T *)a.b + off, b);
+#pragma unroll
+    for (int q = 0; q < VW; q++) b[q] = b[q] - acc[q];
+    vstore<T, VW>((T *)a.y + off, b);
+  } else if constexpr (E == Epi::ChebA) {
+    T b[VW], x[VW], d[VW];
+    vload<T, VW>((const T *)a.b + off, b);
+    vload<T, VW>((const T *)a.xin + off, x);
+    const T iv = ((const T *)a.invd)[r];
+    const T th = (T)a.theta;
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      b[q] = b[q] - acc[q];
+      d[q] = iv * b[q] / th;
+      x[q] = x[q] + d[q];
+    }
+    vstore<T, VW>((T *)a.rout + off, b);
+    vstore<T, VW>((T *)a.dout + off, d);
+    vstore<T, VW>((T *)a.xout + off, x);
+  } else if constexpr (E == Epi::ChebB) {
+    T rr[VW], d[VW], x[VW];
+    vload<T, VW>((const T *)a.rin + off, rr);
+    vload<T, VW>((const T *)a.din + off, d);
+    vload<T, VW>((const T *)a.xin + off, x);
+    const T iv = ((const T *)a.invd)[r];
+    const T c1 = (T)a.c1, c2 = (T)a.c2;
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      rr[q] = rr[q] - acc[q];
+      d[q] = c1 * d[q] + c2 * (iv * rr[q]);
+      x[q] = x[q] + d[q];
+    }
+    if (a.rout) vstore<T, VW>((T *)a.rout + off, rr);
+    if (a.dout) vstore<T, VW>((T *)a.dout + off, d);
+    vstore<T, VW>((T *)a.xout + off, x);
+  } else {  // ElimInterp
+    T b[VW];
+    vload<T, VW>((const T *)a.b + off, b);
+    const T qd = ((const T *)a.q)[r];
+#pragma unroll
+    for (int q = 0; q < VW; q++) b[q] = acc[q] + qd * b[q];
+    vstore<T, VW>((T *)a.y + off, b);
+  }
+}
+
+template <typename T, int K, int VW, int E>
+__device__ __forceinline__ void row_accumulate(const MatView<T> &A, const T *__restrict__ X, i64 k,
+                                               i64 e, int ch, T (&acc)[VW]) {
+  const T *__restrict__ av = A.v;
+  const i32 *__restrict__ ac = A.ci;
+  for (; k + 3 * E < e; k += 4 * E) {
+    T a0 = __ldg(av + k), a1 = __ldg(av + k + E), a2 = __ldg(av + k + 2 * E),
+      a3 = __ldg(av + k + 3 * E);
+    i32 j0 = __ldg(ac + k), j1 = __ldg(ac + k + E), j2 = __ldg(ac + k + 2 * E),
+        j3 = __ldg(ac + k + 3 * E);
+    T x0[VW], x1[VW], x2[VW], x3[VW];
+    vldg<T, VW>(X + (i64)j0 * K + ch * VW, x0);
+    vldg<T, VW>(X + (i64)j1 * K + ch * VW, x1);
+    vldg<T, VW>(X + (i64)j2 * K + ch * VW, x2);
+    vldg<T, VW>(X + (i64)j3 * K + ch * VW, x3);
+#pragma unroll
+    for (int q = 0; q < VW; q++) acc[q] += a0 * x0[q];
+#pragma unroll
+    for (int q = 0; q < VW; q++) acc[q] += a1 * x1[q];
+#pragma unroll
+    for (int q = 0; q < VW; q++) acc[q] += a2 * x2[q];
+#pragma unroll
+    for (int q = 0; q < VW; q++) acc[q] += a3 * x3[q];
+  }
+  for (; k < e; k += E) {
+    T a0 = __ldg(av + k);
+    i32 j0 = __ldg(ac + k);
+    T x0[VW];
+    vldg<T, VW>(X + (i64)j0 * K + ch * VW, x0);
+#pragma unroll
+    for (int q = 0; q < VW; q++) acc[q] += a0 * x0[q];
+  }
+}
+
+template <typename T, int VW, int L, int G>
+__device__ __forceinline__ void reduce_slots(T (&acc)[VW]) {
+#pragma unroll
+  for (int o = L; o < G; o <<= 1)
+#pragma unroll
+    for (int q = 0; q < VW; q++) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+}
+
+template <typename T, int K, int G, Epi EP>
+__global__ void __launch_bounds__(256) k_spmm(const MatView<T> A, const T *__restrict__ X,
+                                              const EpiArgs a) {
+  constexpr int VW = (K % VT<T>::W == 0) ? VT<T>::W : 1;
+  constexpr int L = K / VW;
+  static_assert(L <= G && G <= 32 && (G % L) == 0, "bad SpMM layout");
+  constexpr int E = G / L;
+  constexpr int RPW = 32 / G;
+  const int lane = threadIdx.x & 31;
+  const int g = lane % G, slot = g / L, ch = g % L;
+  const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const i64 nregw = (A.n + RPW - 1) / RPW;
+  T acc[VW];
+#pragma unroll
+  for (int q = 0; q < VW; q++) acc[q] = (T)0;
+  if (warp < nregw) {
+    const i64 r = warp * RPW + lane / G;
+    bool act = r < A.n;
+    i64 b = 0, e = 0;
+    if (act) {
+      b = A.rp[r];
+      e = A.rp[r + 1];
+      if (A.hub_thresh > 0 && e - b > A.hub_thresh) act = false;
+    }
+    if (act) row_accumulate<T, K, VW, E>(A, X, b + slot, e, ch, acc);
+    reduce_slots<T, VW, L, G>(acc);
+    if (act && slot == 0) epilogue<T, K, VW, EP>(a, r, ch * VW, acc);
+    return;
+  }
+  if constexpr (G == 32) {
+    const i64 c = warp - nregw;
+    if (c >= A.nchunks) return;
+    row_accumulate<T, K, VW, E>(A, X, A.ch_beg[c] + slot, A.ch_end[c], ch, acc);
+    reduce_slots<T, VW, L, G>(acc);
+    if (slot == 0) vstore<T, VW>(A.partial + c * K + ch * VW, acc);
+    __threadfence();
+    __syncwarp();
+    int last = 0;
+    if (lane == 0) last = atomicAdd(&A.hub_counter[A.ch_hub[c]], 1) == A.ch_cnt[c] - 1;
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) return;
+    __threadfence();
+    if (slot == 0) {
+      const i64 first = A.ch_first[c];
+      const int cnt = A.ch_cnt[c];
+      T s[VW];
+#pragma unroll
+      for (int q = 0; q < VW; q++) s[q] = (T)0;
+      for (int t = 0; t < cnt; t++) {
+#pragma unroll
+        for (int q = 0; q < VW; q++) s[q] += __ldcg(A.partial + (first + t) * K + ch * VW + q);
+      }
+      epilogue<T, K, VW, EP>(a, A.ch_row[c], ch * VW, s);
+    }
+    if (lane == 0) A.hub_counter[A.ch_hub[c]] = 0;
+  }
+}
+
+template <typename T, int K, int G, Epi EP>
+void launch_spmm(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t s) {
+  constexpr int RPW = 32 / G;
+  i64 warps = cdiv(A.n, RPW) + ((G == 32) ? A.nchunks : 0);
+  if (warps == 0) return;
+  k_spmm<T, K, G, EP><<<grid_for(warps * 32, 256), 256, 0, s>>>(A, X, a);
+  LG_LAUNCH();
+}
+
+template <typename T, int K, Epi EP>
+void dispatch_g(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t s) {
+  if constexpr (K == 1) {
+    int g = A.nchunks > 0 ? 32 : A.lanes_per_row;
+    switch (g) {
+      case 4: return launch_spmm<T, 1, 4, EP>(A, X, a, s);
+      case 8: return launch_spmm<T, 1, 8, EP>(A, X, a, s);
+      case 16: return launch_spmm<T, 1, 16, EP>(A, X, a, s);
+      default: return launch_spmm<T, 1, 32, EP>(A, X, a, s);
+    }
+  } else {
+    launch_spmm<T, K, 32, EP>(A, X, a, s);
+  }
+}
+
+template <typename T, Epi EP>
+void dispatch_k(const MatView<T> &A, const T *X, int k, const EpiArgs &a, cudaStream_t s) {
+  switch (k) {
+    case 1: return dispatch_g<T, 1, EP>(A, X, a, s);
+    case 2: return dispatch_g<T, 2, EP>(A, X, a, s);
+    case 4: return dispatch_g<T, 4, EP>(A, X, a, s);
+    case 8: return dispatch_g<T, 8, EP>(A, X, a, s);
+    case 16: return dispatch_g<T, 16, EP>(A, X, a, s);
+    case 32: return dispatch_g<T, 32, EP>(A, X, a, s);
+    case 64: return dispatch_g<T, 64, EP>(A, X, a, s);
+    default: throw Error(LIGMG_ERR_UNSUPPORTED, "k must be 1,2,4,8,16,32,64");
+  }
+}
+
+}  // namespace
+
+template <typename T>
+void spmm(const MatView<T> &A, const T *X, int k, Epi epi, const EpiArgs &a, cudaStream_t s) {
+  switch (epi) {
+    case Epi::Store: return dispatch_k<T, Epi::Store>(A, X, k, a, s);
+    case Epi::Resid: return dispatch_k<T, Epi::Resid>(A, X, k, a, s);
+    case Epi::ChebA: return dispatch_k<T, Epi::ChebA>(A, X, k, a, s);
+    case Epi::ChebB: return dispatch_k<T, Epi::ChebB>(A, X, k, a, s);
+    case Epi::ElimInterp: return dispatch_k<T, Epi::ElimInterp>(A, X, k, a, s);
+  }
+}
+template void spmm<float>(const MatView<float> &, const float *, int, Epi, const EpiArgs &,
+                          cudaStream_t);
+template void spmm<double>(const MatView<double> &, const double *, int, Epi, const EpiArgs &,
+                           cudaStream_t);
+
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename T>
+__global__ void k_cheb_init_zero(i64 n, int k, const T *b, const T *invd, T theta, T *d) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n * k) d[t] = invd[t / k] * b[t] / theta;
+}
+
+template <typename T>
+__global__ void k_restrict_agg(i64 nc, int k, const i64 *mrp, const i32 *members, const T *r,
+                               T *bc) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nc * k) return;
+  i64 I = t / k;
+  int c = (int)(t % k);
+  T s = 0;
+  for (i64 m = mrp[I]; m < mrp[I + 1]; m++) s += r[(i64)members[m] * k + c];
+  bc[t] = s;
+}
+
+template <typename T>
+__global__ void k_prolong_agg(i64 n, int k, const i32 *agg, const T *xc, T *x) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  i64 i = t / k;
+  x[t] += xc[(i64)agg[i] * k + (t % k)];
+}
+
+template <typename T>
+__global__ void k_coarse_apply(i64 n, int k, const T *pinv, const T *b, T *x) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  i64 i = t / k;
+  int c = (int)(t % k);
+  T s = 0;
+  for (i64 j = 0; j < n; j++) s += pinv[i * n + j] * b[j * k + c];
+  x[t] = s;
+}
+
+template <typename T>
+__global__ void k_scale(i64 nk, T *x, T f) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nk) x[t] = x[t] * f;
+}
+
+template <typename S, typename D>
+__global__ void k_convert(i64 cnt, const S *src, D *dst) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < cnt) dst[t] = (D)src[t];
+}
+
+// column reductions
+template <typename T, int OP>
+__global__ void __launch_bounds__(256) k_colred(i64 n, int k, const T *x, const T *y,
+                                                i64 rows_per_block, double *part) {
+  __shared__ double sh0[256], sh1[256];
+  const int tid = threadIdx.x;
+  const int c = tid % k, rsub = tid / k, rstride = 256 / k;
+  const i64 r0 = (i64)blockIdx.x * rows_per_block;
+  const i64 r1 = min(n, r0 + rows_per_block);
+  double a0 = 0, a1 = 0;
+  for (i64 r = r0 + rsub; r < r1; r += rstride) {
+    double xv = (double)x[r * k + c];
+    if constexpr (OP == 0) {
+      a0 += xv;
+    } else if constexpr (OP == 1) {
+      a0 += xv * (double)y[r * k + c];
+    } else {
+      a0 += xv;
+      a1 += xv * (double)y[r * k + c];
+    }
+  }
+  sh0[tid] = a0;
+  sh1[tid] = a1;
+  __syncthreads();
+  for (int s = 128; s >= k; s >>= 1) {
+    if (tid < s) {
+      sh0[tid] += sh0[tid + s];
+      sh1[tid] += sh1[tid + s];
+    }
+    __syncthreads();
+  }
+  const int nv = (OP == 2) ? 2 : 1;
+  if (tid < k) {
+    part[(i64)blockIdx.x * nv * k + tid] = sh0[tid];
+    if (OP == 2) part[(i64)blockIdx.x * nv * k + k + tid] = sh1[tid];
+  }
+}
+
+__global__ void k_colred_final(int nb, int width, const double *part, double *out) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= width) return;
+  double s = 0;
+  for (int b = 0; b < nb; b++) s += part[(i64)b * width + j];
+  out[j] = s;
+}
+
+int colred_blocks(i64 n, int k) {
+  i64 nb = cdiv(n * k, 256 * 8);
+  return (int)std::max<i64>(1, std::min<i64>(nb, 4 * kSMs));
+}
+
+template <typename T>
+__global__ void k_sub_mean(i64 n, int k, T *x, const double *colsum) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  double mu = colsum[t % k] / (double)n;
+  x[t] = (T)((double)x[t] - mu);
+}
+
+template <typename T>
+__global__ void k_axpby(i64 n, int k, T *y, const T *x, const double *alpha, double sa, double sb) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  double a = alpha ? alpha[t % k] : 1.0;
+  y[t] = (T)(sb * (double)y[t] + sa * a * (double)x[t]);
+}
+
+template <typename T>
+__global__ void k_fcg_direction(i64 n, int k, T *p, const T *z, const T *pp, const double *beta) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  if (pp) p[t] = z[t] - (T)beta[t % k] * pp[t];
+  else p[t] = z[t];
+}
+
+template <typename T>
+__global__ void k_fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, const double *alpha,
+                             int upd_r) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  T a = (T)alpha[t % k];
+  x[t] = x[t] + a * p[t];
+  if (upd_r) r[t] = r[t] - a * q[t];
+}
+
+template <typename T>
+__global__ void k_cg_direction(i64 n, int k, T *p, const T *z, const double *beta) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  p[t] = z[t] + (T)beta[t % k] * p[t];
+}
+
+__global__ void k_scal_div(int k, const double *num, const double *den, double *out,
+                           const int *frozen) {
+  int c = threadIdx.x + blockIdx.x * blockDim.x;
+  if (c >= k) return;
+  double d = den[c];
+  out[c] = (frozen && frozen[c]) || d == 0.0 ? 0.0 : num[c] / d;
+}
+
+__global__ void k_scal_beta(int k, const double *zq, const double *eta_prev, double *beta) {
+  int c = threadIdx.x + blockIdx.x * blockDim.x;
+  if (c >= k) return;
+  double e = eta_prev[c];
+  beta[c] = e == 0.0 ? 0.0 : zq[c] / e;
+}
+
+}  // namespace
+
+template <typename T>
+void cheb_init_zero(i64 n, int k, const T *b, const T *invd, double theta, T *d, cudaStream_t s) {
+  k_cheb_init_zero<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, b, invd, (T)theta, d);
+  LG_LAUNCH();
+}
+template <typename T>
+void restrict_agg(i64 nc, int k, const i64 *mrp, const i32 *members, const T *r, T *bc,
+                  cudaStream_t s) {
+  k_restrict_agg<T><<<grid_for(nc * k, 256), 256, 0, s>>>(nc, k, mrp, members, r, bc);
+  LG_LAUNCH();
+}
+template <typename T>
+void prolong_agg(i64 n, int k, const i32 *agg, const T *xc, T *x, cudaStream_t s) {
+  k_prolong_agg<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, agg, xc, x);
+  LG_LAUNCH();
+}
+template <typename T>
+void coarse_apply(i64 n, int k, const T *pinv, const T *b, T *x, cudaStream_t s) {
+  k_coarse_apply<T><<<grid_for(n * k, 128), 128, 0, s>>>(n, k, pinv, b, x);
+  LG_LAUNCH();
+}
+template <typename T>
+void scale_vec(i64 n, int k, T *x, double f, cudaStream_t s) {
+  k_scale<T><<<grid_for(n * k, 256), 256, 0, s>>>(n * k, x, (T)f);
+  LG_LAUNCH();
+}
+template <typename S, typename D>
+void convert(i64 count, const S *src, D *dst, cudaStream_t s) {
+  if (count <= 0) return;
+  k_convert<S, D><<<grid_for(count, 256), 256, 0, s>>>(count, src, dst);
+  LG_LAUNCH();
+}
+
+i64 col_reduce_scratch(i64 n, int k) { return (i64)colred_blocks(n, k) * 2 * k; }
+
+template <typename T>
+void col_reduce(i64 n, int k, Red op, const T *x, const T *y, double *out, double *scratch,
+                i64 scratch_len, cudaStream_t s) {
+  if (256 % k != 0) throw Error(LIGMG_ERR_UNSUPPORTED, "reduction width");
+  int nb = colred_blocks(n, k);
+  if ((i64)nb * 2 * k > scratch_len) throw Error(LIGMG_ERR_INTERNAL, "reduction scratch");
+  i64 rpb = cdiv(n, nb);
+  int width = k;
+  switch (op) {
+    case Red::Sum: k_colred<T, 0><<<nb, 256, 0, s>>>(n, k, x, y, rpb, scratch); break;
+    case Red::Dot: k_colred<T, 1><<<nb, 256, 0, s>>>(n, k, x, y, rpb, scratch); break;
+    case Red::Sum2Dot:
+      k_colred<T, 2><<<nb, 256, 0, s>>>(n, k, x, y, rpb, scratch);
+      width = 2 * k;
+      break;
+  }
+  LG_LAUNCH();
+  k_colred_final<<<(width + 127) / 128, 128, 0, s>>>(nb, width, scratch, out);
+  LG_LAUNCH();
+}
+
+template <typename T>
+void sub_mean(i64 n, int k, T *x, const double *colsum, cudaStream_t s) {
+  k_sub_mean<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, x, colsum);
+  LG_LAUNCH();
+}
+template <typename T>
+void axpby_cols(i64 n, int k, T *y, const T *x, const double *alpha, double sa, double sb,
+                cudaStream_t s) {
+  k_axpby<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, y, x, alpha, sa, sb);
+  LG_LAUNCH();
+}
+template <typename T>
+void fcg_direction(i64 n, int k, T *p, const T *z, const T *pprev, const double *beta,
+                   cudaStream_t s) {
+  k_fcg_direction<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, p, z, pprev, beta);
+  LG_LAUNCH();
+}
+template <typename T>
+void fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, const double *alpha,
+                bool update_r, cudaStream_t s) {
+  k_fcg_update<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, x, r, p, q, alpha, update_r ? 1 : 0);
+  LG_LAUNCH();
+}
+template <typename T>
+void cg_direction(i64 n, int k, T *p, const T *z, const double *beta, cudaStream_t s) {
+  k_cg_direction<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, p, z, beta);
+  LG_LAUNCH();
+}
+
+void scal_div(int k, const double *num, const double *den, double *out, const int *frozen,
+              cudaStream_t s) {
+  k_scal_div<<<1, 128, 0, s>>>(k, num, den, out, frozen);
+  LG_LAUNCH();
+}
+void scal_beta(int k, const double *zq, const double *eta_prev, double *beta, cudaStream_t s) {
+  k_scal_beta<<<1, 128, 0, s>>>(k, zq, eta_prev, beta);
+  LG_LAUNCH();
+}
+
+#define LG_INST(T)                                                                             \
+  template void cheb_init_zero<T>(i64, int, const T *, const T *, double, T *, cudaStream_t); \
+  template void restrict_agg<T>(i64, int, const i64 *, const i32 *, const T *, T *,          \
+                                cudaStream_t);                                                 \
+  template void prolong_agg<T>(i64, int, const i32 *, const T *, T *, cudaStream_t);         \
+  template void coarse_apply<T>(i64, int, const T *, const T *, T *, cudaStream_t);          \
+  template void scale_vec<T>(i64, int, T *, double, cudaStream_t);                           \
+  template void col_reduce<T>(i64, int, Red, const T *, const T *, double *, double *, i64,  \
+                              cudaStream_t);                                                   \
+  template void sub_mean<T>(i64, int, T *, const double *, cudaStream_t);                    \
+  template void axpby_cols<T>(i64, int, T *, const T *, const double *, double, double,      \
+                              cudaStream_t);                                                   \
+  template void fcg_direction<T>(i64, int, T *, const T *, const T *, const double *,        \
+                                 cudaStream_t);                                                \
+  template void fcg_update<T>(i64, int, T *, T *, const T *, const T *, const double *, bool, \
+                              cudaStream_t);                                                   \
+  template void cg_direction<T>(i64, int, T *, const T *, const double *, cudaStream_t);
+LG_INST(float)
+LG_INST(double)
+template void convert<double, float>(i64, const double *, float *, cudaStream_t);
+template void convert<float, double>(i64, const float *, double *, cudaStream_t);
+template void convert<double, double>(i64, const double *, double *, cudaStream_t);
+
+}  // namespace lg

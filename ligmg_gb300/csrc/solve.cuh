@@ -1,0 +1,111 @@
+// solve.cuh — solve-phase kernels (SpMM with fused epilogues, transfers,
+// column reductions, Krylov updates).  T = float (FP32 hierarchy) or double.
+#pragma once
+#include "common.cuh"
+
+namespace lg {
+
+// Matrix view used by the solve kernels.  Rows longer than hub_thresh are
+// split into chunks processed by separate warps (power-law hub rows); the
+// last chunk to finish sums the partials in chunk order and runs the
+// epilogue, so results do not depend on scheduling.
+template <typename T>
+struct MatView {
+  i64 n = 0;
+  const i64 *rp = nullptr;
+  const i32 *ci = nullptr;
+  const T *v = nullptr;
+  // hub rows
+  i64 hub_thresh = 0;      // 0: no hub handling
+  i64 nchunks = 0;
+  const i64 *ch_row = nullptr, *ch_beg = nullptr, *ch_end = nullptr;
+  const i32 *ch_hub = nullptr, *ch_first = nullptr, *ch_cnt = nullptr;
+  int *hub_counter = nullptr;  // one per hub row, zero between launches
+  T *partial = nullptr;        // nchunks x K
+  int lanes_per_row = 32;      // 4, 8, 16 or 32 (single-RHS layout)
+};
+
+// Hub-row schedule owned by a level (built once at setup).
+template <typename T>
+struct HubPlan {
+  i64 thresh = 0, nchunks = 0, nhubs = 0;
+  DBuf<i64> row, beg, end;
+  DBuf<i32> hub, first, cnt;
+  DBuf<int> counter;
+  DBuf<T> partial;
+  int kcap = 0;
+  void build(const i64 *rp_host, i64 n, i64 thresh, i64 chunk, int kmax, cudaStream_t s);
+  void fill(MatView<T> &m) const;
+};
+
+enum class Epi {
+  Store,       // y = A x
+  Resid,       // y = b - A x
+  ChebA,       // r = b - A x; d = invd r / theta; xo = x + d
+  ChebB,       // r' = r - A d; d' = c1 d + c2 invd r'; xo = xi + d'
+  ElimInterp,  // y = A x + q .* b   (A = P, x = xc)
+};
+
+struct EpiArgs {
+  // generic pointers (type-erased, T*)
+  void *y = nullptr;         // Store/Resid/ElimInterp output
+  const void *b = nullptr;   // Resid/ChebA/ElimInterp rhs
+  const void *invd = nullptr;
+  const void *xin = nullptr; // ChebA: x (own row); ChebB: x_{k+1}
+  void *xout = nullptr;
+  const void *rin = nullptr; // ChebB: r_k (may equal b)
+  void *rout = nullptr;      // ChebA/ChebB (nullable in ChebB)
+  const void *din = nullptr; // ChebB: d_k (own row)
+  void *dout = nullptr;      // ChebA/ChebB (nullable in ChebB)
+  const void *q = nullptr;   // ElimInterp diagonal
+  double theta = 1, c1 = 0, c2 = 0;
+};
+
+// y-epilogue SpMM over k columns (X and all vectors are n x k row-major).
+template <typename T>
+void spmm(const MatView<T> &A, const T *X, int k, Epi epi, const EpiArgs &a, cudaStream_t s);
+
+// elementwise / transfer kernels (n x k row-major)
+template <typename T>
+void cheb_init_zero(i64 n, int k, const T *b, const T *invd, double theta, T *d, cudaStream_t s);
+template <typename T>
+void restrict_agg(i64 nc, int k, const i64 *mrp, const i32 *members, const T *r, T *bc,
+                  cudaStream_t s);
+template <typename T>
+void prolong_agg(i64 n, int k, const i32 *agg, const T *xc, T *x, cudaStream_t s);
+template <typename T>
+void coarse_apply(i64 n, int k, const T *pinv, const T *b, T *x, cudaStream_t s);
+template <typename T>
+void scale_vec(i64 n, int k, T *x, double f, cudaStream_t s);
+template <typename S, typename D>
+void convert(i64 count, const S *src, D *dst, cudaStream_t s);
+
+// Column reductions with FP64 accumulation, deterministic (fixed blocks,
+// fixed tree, block partials summed in order).  out[c] for c < k.
+enum class Red { Sum, Dot, Sum2Dot };  // Sum2Dot: out = [sum(x), x.y] (2k)
+template <typename T>
+void col_reduce(i64 n, int k, Red op, const T *x, const T *y, double *out, double *scratch,
+                i64 scratch_len, cudaStream_t s);
+i64 col_reduce_scratch(i64 n, int k);
+
+// Krylov helpers on device scalars (length k arrays of double)
+template <typename T>
+void sub_mean(i64 n, int k, T *x, const double *colsum, cudaStream_t s);   // x -= sum/n
+template <typename T>
+void axpby_cols(i64 n, int k, T *y, const T *x, const double *alpha, double sa, double sb,
+                cudaStream_t s);  // y = sb*y + sa*alpha[c]*x
+template <typename T>
+void fcg_direction(i64 n, int k, T *p, const T *z, const T *pprev, const double *beta,
+                   cudaStream_t s);  // p = z - beta p_prev (pprev null: p = z)
+template <typename T>
+void fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, const double *alpha,
+                bool update_r, cudaStream_t s);  // x += a p; r -= a q
+template <typename T>
+void cg_direction(i64 n, int k, T *p, const T *z, const double *beta, cudaStream_t s);  // p = z + beta p
+
+// scalar kernels on device (k columns)
+void scal_div(int k, const double *num, const double *den, double *out, const int *frozen,
+              cudaStream_t s);  // out = frozen ? 0 : num/den (0 when den == 0)
+void scal_beta(int k, const double *zq, const double *eta_prev, double *beta, cudaStream_t s);
+
+}  // namespace lg

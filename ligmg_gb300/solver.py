@@ -1,0 +1,196 @@
+"""Python mirror of the reference's solver interface.
+
+  Solver(A) / Solver(A, options)   ligmg::Solver (include/ligmg/ligmg.hpp:17-28)
+  Solver.solve(b)                  ligmg.hpp:31-33
+  Solver.solve(b, from_level)      ligmg.hpp:36-38
+  Solver.print()                   print_hierarchy (multigrid.hpp:265-292)
+  Solver.dump_csv(f, info)         print_csv_header / print_csv (util.hpp:187-205)
+  ConvergenceInfo                  util.hpp:143-170
+
+Everything runs through libligmg_gb300.so on the GPU; there is no CPU path.
+"""
+import ctypes as C
+import math
+import sys
+
+import numpy as np
+
+from . import _abi
+from ._lib import check, lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class ConvergenceInfo:
+    """ConvergenceInfo (util.hpp:143-170) plus the FP64 true residual."""
+
+    def __init__(self, residuals, iters, time, work, solution, true_rel_residual, converged,
+                 col_iters=None, col_true=None, cycle_complexity_value=0.0):
+        self.residuals = np.asarray(residuals)
+        self._iters = int(iters)
+        self._time = float(time)
+        self._work = float(work)
+        self.solution = solution
+        self.true_rel_residual = float(true_rel_residual)
+        self.converged = bool(converged)
+        self.col_iters = col_iters
+        self.col_true_rel_residual = col_true
+        self._cc = cycle_complexity_value
+
+    def iters(self):
+        return self._iters
+
+    def time(self):
+        return self._time
+
+    def work(self):
+        return self._work
+
+    def rel_residual(self):
+        return float(self.residuals[-1] / self.residuals[0]) if len(self.residuals) else 0.0
+
+    def cycle_complexity(self):
+        return self._work / self._iters if self._iters else self._cc
+
+    def cf(self):
+        return self.rel_residual() ** (1.0 / self._iters) if self._iters else 0.0
+
+    def ecf(self):
+        if not self._iters or self.cycle_complexity() == 0:
+            return 0.0
+        return self.rel_residual() ** (1.0 / (self._iters * self.cycle_complexity()))
+
+    def wda(self):
+        e = self.ecf()
+        return -1.0 / math.log10(e) if 0 < e < 1 else float("inf")
+
+    def __str__(self):
+        return ("iters    error  comp  conv econv   wda     time\n"
+                f"{self._iters:5d} {self.rel_residual():.2e} {self.cycle_complexity():5.2f} "
+                f"{self.cf():.3f} {self.ecf():.3f} {self.wda():5.2f} {self._time:.2e}")
+
+
+class Solver:
+    """GPU LigMG solver for a graph Laplacian given as CSR (int64 rowptr,
+    int32 sorted columns, float64 values) or a graphs.Laplacian."""
+
+    def __init__(self, A, options: _abi.Options = None, **kw):
+        if hasattr(A, "rowptr"):
+            n, rp, ci, v = A.n, A.rowptr, A.col, A.val
+        else:
+            n, rp, ci, v = A
+        self.n = int(n)
+        self._rp = np.ascontiguousarray(rp, dtype=np.int64)
+        self._ci = np.ascontiguousarray(ci, dtype=np.int32)
+        self._v = np.ascontiguousarray(v, dtype=np.float64)
+        self.options = options if options is not None else _abi.default_options(**kw)
+        h = C.c_void_p()
+        check(lib().ligmg_create(self.n, _p(self._rp), _p(self._ci), _p(self._v),
+                                 C.byref(self.options), C.byref(h)), "ligmg_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ligmg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- hierarchy ----------------------------------------------------------
+    @property
+    def num_levels(self):
+        x = C.c_int32()
+        check(lib().ligmg_hierarchy_levels(self._h, C.byref(x)))
+        return x.value
+
+    def level_info(self, level):
+        t, n, nnz, nc = C.c_int32(), C.c_int64(), C.c_int64(), C.c_int64()
+        check(lib().ligmg_level_info(self._h, level, C.byref(t), C.byref(n), C.byref(nnz),
+                                     C.byref(nc)))
+        return {"type": _abi.LEVEL_TYPES[t.value], "n": n.value, "nnz": nnz.value, "nc": nc.value}
+
+    def level_matrix(self, level):
+        inf = self.level_info(level)
+        rp = np.empty(inf["n"] + 1, np.int64)
+        ci = np.empty(inf["nnz"], np.int32)
+        v = np.empty(inf["nnz"], np.float64)
+        check(lib().ligmg_level_matrix(self._h, level, _p(rp), _p(ci), _p(v)))
+        return rp, ci, v
+
+    def level_ids(self, level):
+        ids = np.empty(self.level_info(level)["n"], np.int32)
+        check(lib().ligmg_level_ids(self._h, level, _p(ids)))
+        return ids
+
+    def level_lmax(self, level):
+        x = C.c_double()
+        check(lib().ligmg_level_lmax(self._h, level, C.byref(x)))
+        return x.value
+
+    def print(self, file=sys.stdout):
+        """print_hierarchy (multigrid.hpp:265-292) at one GPU."""
+        print(f"{'Level':>5}  {'Size':>10}  {'NNZ':>12}  {'Type':>6}", file=file)
+        for l in range(self.num_levels):
+            i = self.level_info(l)
+            print(f"{l:5d}  {i['n']:10d}  {i['nnz']:12d}  {i['type']:>6}", file=file)
+
+    # ---- solve ----------------------------------------------------------------
+    def _info(self, k, history=1024):
+        info = _abi.Info()
+        hist = np.zeros(history)
+        ci = np.zeros(k, np.int32)
+        ct = np.zeros(k)
+        info.residual_history = hist.ctypes.data_as(C.POINTER(C.c_double))
+        info.history_capacity = history
+        info.col_iters = ci.ctypes.data_as(C.POINTER(C.c_int32))
+        info.col_true_rel_residual = ct.ctypes.data_as(C.POINTER(C.c_double))
+        return info, hist, ci, ct
+
+    def solve(self, b, from_level=None) -> ConvergenceInfo:
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.empty_like(b)
+        info, hist, ci, ct = self._info(1)
+        if from_level is None:
+            st = check(lib().ligmg_solve(self._h, _p(b), _p(x), C.byref(info)), "ligmg_solve")
+        else:
+            st = check(lib().ligmg_solve_from(self._h, _p(b), _p(x), int(from_level),
+                                              C.byref(info)), "ligmg_solve_from")
+        return ConvergenceInfo(hist[: info.history_len].copy(), info.iters, info.solve_seconds,
+                               info.work, x, info.true_rel_residual, st == 0, ci, ct,
+                               info.cycle_complexity)
+
+    def solve_batched(self, B) -> ConvergenceInfo:
+        """k right-hand sides as an n x k row-major block (k in 1,2,4,...,64)."""
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        k = B.shape[1]
+        X = np.empty_like(B)
+        info, hist, ci, ct = self._info(k)
+        st = check(lib().ligmg_solve_batched(self._h, _p(B), k, _p(X), C.byref(info)),
+                   "ligmg_solve_batched")
+        return ConvergenceInfo(hist[: info.history_len].copy(), info.iters, info.solve_seconds,
+                               info.work, X, info.true_rel_residual, st == 0, ci, ct,
+                               info.cycle_complexity)
+
+    def cycle(self, level, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.empty_like(b)
+        check(lib().ligmg_cycle(self._h, level, _p(b), _p(x)), "ligmg_cycle")
+        return x
+
+    def spmv(self, level, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty_like(x)
+        check(lib().ligmg_spmv(self._h, level, _p(x), _p(y)), "ligmg_spmv")
+        return y
+
+    def dump_csv(self, f, info: ConvergenceInfo, graph="graph", setup_time=0.0, nnz=0):
+        """CSV row in the column order of print_csv (util.hpp:187-205)."""
+        f.write("graph,solver,iters,rel_error,cycle_complexity,wda,setup_time,solve_time,nnz,nodes\n")
+        f.write(f"{graph},ligmg,{info.iters()},{info.rel_residual()},{info.cycle_complexity()},"
+                f"{info.wda()},{setup_time},{info.time()},{nnz},1\n")

@@ -1,0 +1,94 @@
+"""CPU tests of the C-ABI library: it builds, loads, exports every symbol that
+include/ligmg_gpu.h declares, its struct layout matches the ctypes mirrors,
+and argument checks that precede any CUDA call behave."""
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def test_library_exports_every_header_symbol(built_lib):
+    from ligmg_gb300._lib import header_functions, lib
+    L = lib()
+    names = header_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(L, n), n
+    out = subprocess.run(["nm", "-D", "--defined-only", built_lib], capture_output=True, text=True)
+    exported = {line.split()[-1] for line in out.stdout.splitlines() if line.strip()}
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+
+
+def _c_layout(struct_name, fields):
+    src = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{ROOT}/include/ligmg_gpu.h"',
+           "int main(void) {", f'printf("%zu\\n", sizeof({struct_name}));']
+    for f in fields:
+        src.append(f'printf("%zu\\n", offsetof({struct_name}, {f}));')
+    src.append("return 0; }")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        open(c, "w").write("\n".join(src))
+        subprocess.run(["gcc", "-std=c99", "-o", exe, c], check=True)
+        vals = [int(x) for x in subprocess.run([exe], capture_output=True, text=True,
+                                               check=True).stdout.split()]
+    return vals[0], vals[1:]
+
+
+@pytest.mark.parametrize("name", ["Options", "Info"])
+def test_struct_layout_matches_ctypes(name):
+    from ligmg_gb300 import _abi
+    cls = getattr(_abi, name)
+    cname = {"Options": "ligmg_options", "Info": "ligmg_info"}[name]
+    fields = [f for f, _ in cls._fields_]
+    size, offs = _c_layout(cname, fields)
+    assert size == C.sizeof(cls)
+    for f, o in zip(fields, offs):
+        assert getattr(cls, f).offset == o, f
+
+
+def test_default_options_match(built_lib):
+    from ligmg_gb300._abi import Options, default_options
+    from ligmg_gb300._lib import lib
+    o = Options()
+    lib().ligmg_default_options(C.byref(o))
+    d = default_options()
+    for f, _ in Options._fields_:
+        assert getattr(o, f) == getattr(d, f), f
+
+
+def test_status_strings(built_lib):
+    from ligmg_gb300._lib import lib
+    for s in range(0, 14):
+        assert lib().ligmg_status_string(s)
+    assert lib().ligmg_status_string(0) == b"ok"
+
+
+def test_argument_checks_before_cuda(built_lib):
+    from ligmg_gb300._abi import default_options
+    from ligmg_gb300._lib import lib
+    L = lib()
+    h = C.c_void_p()
+    o = default_options()
+    rp = np.array([0, 1], np.int64)
+    ci = np.array([0], np.int32)
+    v = np.array([1.0])
+    p = lambda a: a.ctypes.data_as(C.c_void_p)
+    assert L.ligmg_create(0, p(rp), p(ci), p(v), C.byref(o), C.byref(h)) == 2
+    assert L.ligmg_create(1, None, p(ci), p(v), C.byref(o), C.byref(h)) == 2
+    assert L.ligmg_create(1, p(rp), p(ci), p(v), C.byref(o), None) == 2
+    assert L.ligmg_destroy(None) == 2
+    assert L.ligmg_solve(None, p(v), p(v), None) == 2
+
+
+def test_python_solver_fails_loudly_without_library(monkeypatch, tmp_path):
+    import ligmg_gb300._lib as lb
+    monkeypatch.setattr(lb, "_lib", None)
+    with pytest.raises(RuntimeError):
+        lb.lib(str(tmp_path / "missing.so"))

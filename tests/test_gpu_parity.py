@@ -1,0 +1,179 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the oracle.
+
+Bars:
+  * setup (elimination ids, aggregate ids, every level's matrix): bit-exact;
+  * Chebyshev eigenvalue estimate: 1e-12 relative;
+  * one FP64 cycle from the finest level: 1e-12 relative after projecting
+    out the constant;
+  * solves: the FP64-recomputed true residual reaches the tolerance, and the
+    FP64 solution matches the oracle's to 1e-6 relative (both are solved to
+    rtol 1e-8; the difference is bounded by the condition number).
+"""
+import numpy as np
+import pytest
+
+from conftest import my_matrix
+from ligmg_gb300 import Solver
+from ligmg_gb300 import graphs as G
+from ligmg_gb300._lib import LigmgError
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GRAPHS = {
+    "grid32": lambda: G.grid2d(32),
+    "grid48_logn": lambda: G.grid2d(48, weights="lognormal", seed=2),
+    "my_matrix": my_matrix,
+    "rmat12": lambda: G.rmat(12, seed=1),
+    "rmat14": lambda: G.rmat(14, seed=5),
+    "rgg3000": lambda: G.rgg(3000, seed=3),
+    "grid3d_12": lambda: G.grid3d(12, weights="lognormal", seed=1),
+}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _build():
+    from ligmg_gb300 import build
+    build.build()
+
+
+def _proj(x):
+    return x - x.mean()
+
+
+def _relerr(a, b):
+    return np.linalg.norm(_proj(a) - _proj(b)) / max(np.linalg.norm(_proj(b)), 1e-300)
+
+
+@pytest.mark.parametrize("name", list(GRAPHS))
+def test_setup_bit_exact(name):
+    L = GRAPHS[name]()
+    S = Solver(L)
+    R = O.OracleSolver(L)
+    assert S.num_levels == R.num_levels
+    for l in range(R.num_levels):
+        gi, ri = S.level_info(l), R.level_info(l)
+        assert gi == ri, (l, gi, ri)
+        grp, gci, gv = S.level_matrix(l)
+        rrp, rci, rv = R.level_matrix(l)
+        assert (grp == rrp).all() and (gci == rci).all(), l
+        assert (gv.view(np.int64) == rv.view(np.int64)).all(), f"level {l} values differ"
+        if ri["type"] != "coarse":
+            assert (S.level_ids(l) == R.level_ids(l)).all(), f"level {l} ids differ"
+        if ri["type"] == "agg":
+            assert abs(S.level_lmax(l) - R.level_lmax(l)) <= 1e-12 * R.level_lmax(l)
+
+
+@pytest.mark.parametrize("kcycle", [0, 1])
+@pytest.mark.parametrize("name", ["grid48_logn", "my_matrix", "rmat12", "grid3d_12"])
+def test_cycle_fp64_matches_oracle(name, kcycle):
+    L = GRAPHS[name]()
+    S = Solver(L, kcycle=kcycle)
+    R = O.OracleSolver(L, kcycle=kcycle)
+    rng = np.random.default_rng(7)
+    for level in range(R.num_levels):
+        n = R.level_info(level)["n"]
+        b = _proj(rng.standard_normal(n))
+        xg, xr = S.cycle(level, b), R.cycle(level, b)
+        assert _relerr(xg, xr) <= 1e-12, (level, _relerr(xg, xr))
+
+
+@pytest.mark.parametrize("name", ["grid48_logn", "rmat12"])
+def test_cycle_fp32_close_to_oracle(name):
+    L = GRAPHS[name]()
+    S = Solver(L, precision="fp32", kcycle=1)
+    R = O.OracleSolver(L, kcycle=1)
+    b = _proj(np.random.default_rng(3).standard_normal(L.n))
+    assert _relerr(S.cycle(0, b), R.cycle(0, b)) <= 1e-4
+
+
+def test_spmv_matches():
+    L = GRAPHS["rmat14"]()
+    S = Solver(L)
+    x = np.random.default_rng(0).standard_normal(L.n)
+    y = S.spmv(0, x)
+    ref = L.to_scipy() @ x
+    assert np.abs(y - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("cfg", [dict(), dict(outer_ksp_type="fcg"),
+                                 dict(kcycle=1, outer_ksp_type="fcg")])
+@pytest.mark.parametrize("name", ["grid48_logn", "my_matrix", "rmat14", "rgg3000"])
+def test_solve_fp64_matches_oracle(name, cfg):
+    L = GRAPHS[name]()
+    S = Solver(L, **cfg)
+    R = O.OracleSolver(L, **cfg)
+    b = G.rhs(L.n, seed=11)
+    info = S.solve(b)
+    xr, ir = R.solve(b)
+    assert info.converged
+    assert abs(info.iters() - ir["iters"]) <= 1
+    assert info.true_rel_residual <= 1e-7
+    r = b - L.to_scipy() @ info.solution
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 1e-7
+    assert _relerr(info.solution, xr) <= 1e-6
+
+
+@pytest.mark.parametrize("name", ["grid48_logn", "rmat14", "grid3d_12"])
+def test_solve_fp32_hierarchy_reaches_tol(name):
+    L = GRAPHS[name]()
+    S = Solver(L, precision="fp32", kcycle=1, outer_ksp_type="fcg")
+    b = G.rhs(L.n, seed=5)
+    info = S.solve(b)
+    assert info.converged
+    assert info.true_rel_residual <= 2e-8
+    r = b - L.to_scipy() @ info.solution
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 2e-8
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("k", [2, 8, 32])
+def test_batched_matches_single(prec, k):
+    L = GRAPHS["rmat12"]()
+    S = Solver(L, precision=prec, kcycle=1, outer_ksp_type="fcg")
+    B = G.rhs(L.n, k=k, seed=9)
+    info = S.solve_batched(B)
+    assert info.converged
+    assert (info.col_true_rel_residual <= 2e-8).all()
+    for c in (0, k - 1):
+        single = S.solve(B[:, c].copy())
+        assert _relerr(info.solution[:, c], single.solution) <= 1e-6
+
+
+def test_solve_from_level():
+    L = GRAPHS["my_matrix"]()
+    S = Solver(L, outer_ksp_type="fcg")
+    R = O.OracleSolver(L, outer_ksp_type="fcg")
+    n1 = R.level_info(1)["n"]
+    b = _proj(np.random.default_rng(1).standard_normal(n1))
+    info = S.solve(b, from_level=1)
+    xr, ir = R.solve(b, from_level=1)
+    assert info.converged and _relerr(info.solution, xr) <= 1e-6
+
+
+def _bad(L, mutate):
+    rp, ci, v = L.rowptr.copy(), L.col.copy(), L.val.copy()
+    mutate(rp, ci, v)
+    return (L.n, rp, ci, v)
+
+
+def test_invalid_inputs_return_status():
+    L = G.grid2d(6)
+    off = int(np.where(L.col[: L.rowptr[1]] == 1)[0][0])
+    cases = {
+        3: lambda rp, ci, v: v.__setitem__(off, -2.0),            # not symmetric
+        5: lambda rp, ci, v: v.__setitem__(off, 0.5),             # positive off-diagonal
+        6: lambda rp, ci, v: v.__setitem__(0, np.nan),            # non-finite
+        4: lambda rp, ci, v: v.__setitem__(0, -1.0),              # bad diagonal
+    }
+    for code, mut in cases.items():
+        with pytest.raises(LigmgError) as e:
+            Solver(_bad(L, mut))
+        assert e.value.status == code
+
+
+def test_unsupported_k_rejected():
+    L = GRAPHS["grid32"]()
+    S = Solver(L)
+    with pytest.raises(LigmgError):
+        S.solve_batched(np.zeros((L.n, 3)))
