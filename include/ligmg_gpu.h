@@ -194,6 +194,39 @@ ligmg_status ligmg_cycle(ligmg_handle h, int32_t level, const double *b,
 ligmg_status ligmg_spmv(ligmg_handle h, int32_t level, const double *x,
                         double *y);
 
+/* Per-kernel timing (no reference counterpart; the reference only times
+ * setup and solve with MPI_Wtime, multigrid.hpp:183,260 and cg.hpp:23,331).
+ * When enabled, every sparse kernel launch of a solve is bracketed by CUDA
+ * events on the handle's stream and accumulated per (level, kind, k) with
+ * its algorithmic (compulsory) byte count. */
+#define LIGMG_KERNEL_SPMV 0        /* y = A x (outer Krylov / K-cycle) */
+#define LIGMG_KERNEL_RESID 1       /* r = b - A x */
+#define LIGMG_KERNEL_CHEB_A 2      /* first Chebyshev step, nonzero guess */
+#define LIGMG_KERNEL_CHEB_B 3      /* later Chebyshev steps */
+#define LIGMG_KERNEL_ELIM_INTERP 4 /* x = P xc + Q b */
+#define LIGMG_KERNEL_ELIM_RESTRICT 5 /* bc = R b */
+typedef struct ligmg_kernel_stat {
+  int32_t level;
+  int32_t kind;      /* LIGMG_KERNEL_* */
+  int32_t k;         /* right-hand sides per launch */
+  int32_t fp64;      /* 1: FP64 values, 0: FP32 */
+  int64_t launches;
+  double seconds;    /* summed event time */
+  double bytes;      /* summed algorithmic bytes */
+} ligmg_kernel_stat;
+ligmg_status ligmg_profile_enable(ligmg_handle h, int32_t enable);
+/* Stream control (no reference counterpart): the handle's work is issued on
+ * its stream (cudaStream_t passed as void*).  Setting a stream makes the
+ * caller's events on that stream bracket the handle's kernels. */
+ligmg_status ligmg_set_stream(ligmg_handle h, void *stream);
+ligmg_status ligmg_get_stream(ligmg_handle h, void **stream);
+/* Kernels launched by this library in this process so far. */
+ligmg_status ligmg_launch_count(int64_t *count);
+/* Writes up to cap records (sorted by descending time) and the total count;
+ * enabling again clears the statistics. */
+ligmg_status ligmg_kernel_stats(ligmg_handle h, ligmg_kernel_stat *out,
+                                int32_t cap, int32_t *count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -150,3 +150,19 @@ def default_options(**overrides) -> Options:
             raise AttributeError(f"unknown option {k}")
         setattr(o, k, v)
     return o
+
+
+KERNEL_KINDS = {0: "spmv", 1: "resid", 2: "cheb_a", 3: "cheb_b", 4: "elim_interp",
+                5: "elim_restrict"}
+
+
+class KernelStat(C.Structure):
+    _fields_ = [
+        ("level", C.c_int32),
+        ("kind", C.c_int32),
+        ("k", C.c_int32),
+        ("fp64", C.c_int32),
+        ("launches", C.c_int64),
+        ("seconds", C.c_double),
+        ("bytes", C.c_double),
+    ]

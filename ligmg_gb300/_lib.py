@@ -8,7 +8,7 @@ import os
 import re
 
 from . import build as _build
-from ._abi import Info, Options
+from ._abi import Info, KernelStat, Options
 
 HEADER = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "include", "ligmg_gpu.h")
 
@@ -65,6 +65,11 @@ def lib(path=None):
     L.ligmg_level_lmax.argtypes = [vp, C.c_int32, P(C.c_double)]
     L.ligmg_cycle.argtypes = [vp, C.c_int32, vp, vp]
     L.ligmg_spmv.argtypes = [vp, C.c_int32, vp, vp]
+    L.ligmg_profile_enable.argtypes = [vp, C.c_int32]
+    L.ligmg_kernel_stats.argtypes = [vp, P(KernelStat), C.c_int32, P(C.c_int32)]
+    L.ligmg_set_stream.argtypes = [vp, vp]
+    L.ligmg_get_stream.argtypes = [vp, P(vp)]
+    L.ligmg_launch_count.argtypes = [P(C.c_int64)]
     for name in header_functions():
         if name not in ("ligmg_default_options", "ligmg_status_string"):
             getattr(L, name).restype = C.c_int

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <memory>
 #include <new>
 
@@ -237,12 +238,63 @@ struct OuterWork {
   double *slot(int s) { return sc.p + (i64)s * k * 2; }
 };
 
+// per-kernel event timing (ligmg_profile_enable / ligmg_kernel_stats)
+struct ProfRec {
+  int level, kind, k, fp64;
+  cudaEvent_t a, b;
+  double bytes;
+};
+struct Profiler {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<ProfRec> pending;
+  std::map<std::tuple<int, int, int, int>, ligmg_kernel_stat> stats;
+  cudaEvent_t get() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    LG_CUDA(cudaEventCreate(&e));
+    return e;
+  }
+  void collect() {
+    if (pending.empty()) return;
+    LG_CUDA(cudaEventSynchronize(pending.back().b));
+    for (auto &r : pending) {
+      float ms = 0;
+      LG_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+      auto key = std::make_tuple(r.level, r.kind, r.k, r.fp64);
+      auto it = stats.find(key);
+      if (it == stats.end()) {
+        ligmg_kernel_stat z{};
+        z.level = r.level; z.kind = r.kind; z.k = r.k; z.fp64 = r.fp64;
+        it = stats.emplace(key, z).first;
+      }
+      it->second.launches += 1;
+      it->second.seconds += ms * 1e-3;
+      it->second.bytes += r.bytes;
+      pool.push_back(r.a);
+      pool.push_back(r.b);
+    }
+    pending.clear();
+  }
+  ~Profiler() {
+    for (auto &r : pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
 }  // namespace lg
 
 struct ligmg_handle_s {
+  lg::Profiler prof;
   ligmg_options opts;
   int device = 0;
   cudaStream_t s = nullptr;
+  bool own_stream = true;
+  std::vector<cudaStream_t> old_streams;
   std::vector<std::unique_ptr<lg::Level>> h;
   lg::i64 nnz0 = 0;
   double setup_s = 0;
@@ -255,10 +307,12 @@ struct ligmg_handle_s {
     w64.clear();
     ow.clear();
     h.clear();
-    if (s) {
-      cudaStreamSynchronize(s);
-      cudaStreamDestroy(s);
+    if (s) cudaStreamSynchronize(s);
+    for (auto o : old_streams) {
+      cudaStreamSynchronize(o);
+      cudaStreamDestroy(o);
     }
+    if (s && own_stream) cudaStreamDestroy(s);
   }
 };
 
@@ -266,6 +320,24 @@ namespace lg {
 namespace {
 
 using Handle = ligmg_handle_s;
+
+template <typename F>
+void timed(Handle &H, int level, int kind, int k, int fp64, double bytes, F &&f) {
+  if (!H.prof.on) {
+    f();
+    return;
+  }
+  cudaEvent_t a = H.prof.get(), b = H.prof.get();
+  LG_CUDA(cudaEventRecord(a, H.s));
+  f();
+  LG_CUDA(cudaEventRecord(b, H.s));
+  H.prof.pending.push_back({level, kind, k, fp64, a, b, bytes});
+}
+
+// algorithmic (compulsory) bytes: every array element read or written once
+inline double core_bytes(i64 rows, i64 nnz, i64 xrows, int k, int sv) {
+  return 8.0 * (rows + 1) + (double)nnz * (4 + sv) + (double)xrows * k * sv;
+}
 
 void ensure_fp32(Handle &H) {
   cudaStream_t s = H.s;
@@ -386,7 +458,9 @@ struct Engine {
       EpiArgs a;
       a.b = b; a.invd = invd; a.xin = x; a.rout = w.r.p; a.dout = w.d0.p; a.xout = w.xt.p;
       a.theta = L.theta;
-      spmm<T>(A, x, k, Epi::ChebA, a, s);
+      timed(H, (int)l, LIGMG_KERNEL_CHEB_A, k, sizeof(T) == 8,
+            core_bytes(n, L.A.nnz, n, k, sizeof(T)) + (5.0 * n * k + n) * sizeof(T),
+            [&] { spmm<T>(A, x, k, Epi::ChebA, a, s); });
       d_cur = w.d0.p;
       x_cur = w.xt.p;
       r_cur = w.r.p;
@@ -408,7 +482,9 @@ struct Engine {
       a.dout = last ? nullptr : d_other;
       T *xo = last ? x : w.xt.p;
       a.xout = xo;
-      spmm<T>(A, d_cur, k, Epi::ChebB, a, s);
+      timed(H, (int)l, LIGMG_KERNEL_CHEB_B, k, sizeof(T) == 8,
+            core_bytes(n, L.A.nnz, n, k, sizeof(T)) + ((last ? 4.0 : 6.0) * n * k + n) * sizeof(T),
+            [&] { spmm<T>(A, d_cur, k, Epi::ChebB, a, s); });
       if (!last) {
         r_cur = w.r.p;
         std::swap(d_cur, d_other);
@@ -429,11 +505,15 @@ struct Engine {
     if (L.type == LIGMG_LEVEL_ELIM) {  // elimination.hpp:33-52
       EpiArgs a;
       a.y = nw.in.p;
-      spmm<T>(viewR<T>(L), b, k, Epi::Store, a, s);
+      timed(H, (int)l, LIGMG_KERNEL_ELIM_RESTRICT, k, sizeof(T) == 8,
+            core_bytes(L.elim.R.n, L.elim.R.nnz, n, k, sizeof(T)) + (double)L.elim.R.n * k * sizeof(T),
+            [&] { spmm<T>(viewR<T>(L), b, k, Epi::Store, a, s); });
       recurse(l, nw.in.p, nw.out.p);
       EpiArgs c;
       c.y = x; c.b = b; c.q = QT<T>(L);
-      spmm<T>(viewP<T>(L), nw.out.p, k, Epi::ElimInterp, c, s);
+      timed(H, (int)l, LIGMG_KERNEL_ELIM_INTERP, k, sizeof(T) == 8,
+            core_bytes(n, L.elim.P.nnz, L.nc, k, sizeof(T)) + (2.0 * n * k + n) * sizeof(T),
+            [&] { spmm<T>(viewP<T>(L), nw.out.p, k, Epi::ElimInterp, c, s); });
       return;
     }
     // aggregation.hpp:209-241
@@ -442,7 +522,9 @@ struct Engine {
     EpiArgs a;
     a.y = w.r.p;
     a.b = b;
-    spmm<T>(viewA<T>(L), x, k, Epi::Resid, a, s);
+    timed(H, (int)l, LIGMG_KERNEL_RESID, k, sizeof(T) == 8,
+          core_bytes(n, L.A.nnz, n, k, sizeof(T)) + 2.0 * n * k * sizeof(T),
+          [&] { spmm<T>(viewA<T>(L), x, k, Epi::Resid, a, s); });
     restrict_agg<T>(L.nc, k, L.agg.mrp.p, L.agg.members.p, w.r.p, nw.in.p, s);
     recurse(l, nw.in.p, nw.out.p);
     prolong_agg<T>(n, k, L.agg.agg.p, nw.out.p, x, s);
@@ -484,7 +566,9 @@ struct Engine {
       }
       EpiArgs a;
       a.y = q;
-      spmm<T>(A, p, k, Epi::Store, a, s);
+      timed(H, (int)l, LIGMG_KERNEL_SPMV, k, sizeof(T) == 8,
+            core_bytes(n, L.A.nnz, n, k, sizeof(T)) + 1.0 * n * k * sizeof(T),
+            [&] { spmm<T>(A, p, k, Epi::Store, a, s); });
       col_reduce<T>(n, k, Red::Dot, p, q, eta, w.scratch.p, w.scratch_len, s);
       col_reduce<T>(n, k, Red::Dot, p, r, w.slot(S_RHO, k), w.scratch.p, w.scratch_len, s);
       scal_div(k, w.slot(S_RHO, k), eta, w.slot(S_ALPHA, k), nullptr, s);
@@ -783,7 +867,8 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
       }
       EpiArgs a;
       a.y = Q;
-      spmm<double>(A, P, k, Epi::Store, a, s);
+      timed(H, (int)base, LIGMG_KERNEL_SPMV, k, 1, core_bytes(n, L.A.nnz, n, k, 8) + 8.0 * n * k,
+            [&] { spmm<double>(A, P, k, Epi::Store, a, s); });
       col_reduce<double>(n, k, Red::Dot, P, Q, eta, w.scratch.p, w.scratch_len, s);
       scal_div(k, bcg, eta, alpha, w.frozen.p, s);
       fcg_update<double>(n, k, w.X.p, w.R.p, P, Q, alpha, true, s);
@@ -798,7 +883,8 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
       }
       EpiArgs a;
       a.y = Q;
-      spmm<double>(A, P, k, Epi::Store, a, s);
+      timed(H, (int)base, LIGMG_KERNEL_SPMV, k, 1, core_bytes(n, L.A.nnz, n, k, 8) + 8.0 * n * k,
+            [&] { spmm<double>(A, P, k, Epi::Store, a, s); });
       col_reduce<double>(n, k, Red::Dot, P, Q, eta, w.scratch.p, w.scratch_len, s);
       col_reduce<double>(n, k, Red::Dot, P, w.R.p, rho, w.scratch.p, w.scratch_len, s);
       scal_div(k, rho, eta, alpha, w.frozen.p, s);
@@ -855,7 +941,9 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
   if (do_once) {
     EpiArgs a;
     a.y = w.B.p;
-    spmm<double>(viewR<double>(F), w.Bfull.p, k, Epi::Store, a, s);
+    timed(H, from, LIGMG_KERNEL_ELIM_RESTRICT, k, 1,
+          core_bytes(F.elim.R.n, F.elim.R.nnz, n0, k, 8) + 8.0 * F.elim.R.n * k,
+          [&] { spmm<double>(viewR<double>(F), w.Bfull.p, k, Epi::Store, a, s); });
   } else {
     LG_CUDA(cudaMemcpyAsync(w.B.p, w.Bfull.p, sizeof(double) * n0 * k, cudaMemcpyDeviceToDevice, s));
   }
@@ -864,7 +952,9 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
   if (do_once) {  // x = P x + Q b (:349-354)
     EpiArgs c;
     c.y = w.Xfull.p; c.b = w.Bfull.p; c.q = F.elim.Q.p;
-    spmm<double>(viewP<double>(F), w.X.p, k, Epi::ElimInterp, c, s);
+    timed(H, from, LIGMG_KERNEL_ELIM_INTERP, k, 1,
+          core_bytes(n0, F.elim.P.nnz, nb, k, 8) + (2.0 * n0 * k + n0) * 8,
+          [&] { spmm<double>(viewP<double>(F), w.X.p, k, Epi::ElimInterp, c, s); });
   } else {
     LG_CUDA(cudaMemcpyAsync(w.Xfull.p, w.X.p, sizeof(double) * n0 * k, cudaMemcpyDeviceToDevice, s));
   }
@@ -876,7 +966,8 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
   EpiArgs a;
   a.y = w.Res.p;
   a.b = w.Bfull.p;
-  spmm<double>(viewA<double>(F), w.Xfull.p, k, Epi::Resid, a, s);
+  timed(H, from, LIGMG_KERNEL_RESID, k, 1, core_bytes(n0, F.A.nnz, n0, k, 8) + 16.0 * n0 * k,
+        [&] { spmm<double>(viewA<double>(F), w.Xfull.p, k, Epi::Resid, a, s); });
   col_reduce<double>(n0, k, Red::Dot, w.Res.p, w.Res.p, d1, w.scratch.p, w.scratch_len, s);
   col_reduce<double>(n0, k, Red::Dot, w.Bfull.p, w.Bfull.p, d2, w.scratch.p, w.scratch_len, s);
   std::vector<double> h1(k), h2(k);
@@ -884,6 +975,7 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
   LG_CUDA(cudaMemcpyAsync(h2.data(), d2, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
   LG_CUDA(cudaStreamSynchronize(s));
   double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  H.prof.collect();
   if (info) {
     double worst_true = 0, worst_rel = 0;
     for (int c = 0; c < k; c++) {
@@ -1162,6 +1254,61 @@ ligmg_status ligmg_spmv(ligmg_handle h, int32_t level, const double *x, double *
     spmm<double>(viewA<double>(L), dx.p, 1, Epi::Store, a, h->s);
     dy.download(y, n);
     LG_CUDA(cudaStreamSynchronize(h->s));
+    return LIGMG_OK;
+  });
+}
+
+ligmg_status ligmg_set_stream(ligmg_handle h, void *stream) {
+  if (!h || !stream) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    LG_CUDA(cudaStreamSynchronize(h->s));
+    if (h->own_stream) {
+      // buffers were allocated stream-ordered on the old stream; keep it alive
+      h->old_streams.push_back(h->s);
+      h->own_stream = false;
+    }
+    h->s = (cudaStream_t)stream;
+    return LIGMG_OK;
+  });
+}
+
+ligmg_status ligmg_get_stream(ligmg_handle h, void **stream) {
+  if (!h || !stream) return LIGMG_ERR_INVALID_ARGUMENT;
+  *stream = (void *)h->s;
+  return LIGMG_OK;
+}
+
+ligmg_status ligmg_launch_count(int64_t *count) {
+  if (!count) return LIGMG_ERR_INVALID_ARGUMENT;
+  *count = __atomic_load_n(&lg::g_launches, __ATOMIC_RELAXED);
+  return LIGMG_OK;
+}
+
+ligmg_status ligmg_profile_enable(ligmg_handle h, int32_t enable) {
+  if (!h) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    h->prof.collect();
+    h->prof.on = enable != 0;
+    if (enable) h->prof.stats.clear();
+    return LIGMG_OK;
+  });
+}
+
+ligmg_status ligmg_kernel_stats(ligmg_handle h, ligmg_kernel_stat *out, int32_t cap,
+                                int32_t *count) {
+  if (!h || !count || (cap > 0 && !out)) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    h->prof.collect();
+    std::vector<ligmg_kernel_stat> v;
+    for (auto &kv : h->prof.stats) v.push_back(kv.second);
+    std::sort(v.begin(), v.end(), [](const ligmg_kernel_stat &a, const ligmg_kernel_stat &b) {
+      return a.seconds > b.seconds;
+    });
+    *count = (int32_t)v.size();
+    for (int i = 0; i < cap && i < (int)v.size(); i++) out[i] = v[i];
     return LIGMG_OK;
   });
 }

@@ -29,8 +29,14 @@ inline void cuda_check(cudaError_t e, const char *what) {
     throw Error(LIGMG_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
   throw Error(LIGMG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
+// kernels launched by the library (every launch site calls LG_LAUNCH once)
+extern int64_t g_launches;
 #define LG_CUDA(x) ::lg::cuda_check((x), #x)
-#define LG_LAUNCH() ::lg::cuda_check(cudaGetLastError(), "kernel launch")
+#define LG_LAUNCH()                                             \
+  do {                                                          \
+    __atomic_fetch_add(&::lg::g_launches, 1, __ATOMIC_RELAXED); \
+    ::lg::cuda_check(cudaGetLastError(), "kernel launch");      \
+  } while (0)
 
 constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
 

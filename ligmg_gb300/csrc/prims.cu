@@ -3,6 +3,8 @@
 
 namespace lg {
 
+int64_t g_launches = 0;
+
 namespace {
 
 constexpr int kScanThreads = 256;

@@ -914,6 +914,9 @@ void gpu_aggregation(const DCsr<double> &A, const AggParams &p, const double *tv
 
 ligmg_status gpu_coarse_pinv(const DCsr<double> &A, DBuf<double> &out, cudaStream_t s) {
   i64 n = A.n;
+  // dense n x n factor; the coarsening loop stops near nnz <= min_size, so a
+  // coarse level this large means min_size was set far outside its range
+  if (n > 16384) throw Error(LIGMG_ERR_UNSUPPORTED, "coarse level too large for a dense inverse");
   DBuf<double> M(n * n, s), fac(n, s);
   out.alloc(n * n, s);
   DBuf<int> bad(1, s);

@@ -189,6 +189,41 @@ class Solver:
         check(lib().ligmg_spmv(self._h, level, _p(x), _p(y)), "ligmg_spmv")
         return y
 
+    # ---- measurement ---------------------------------------------------------
+    def profile(self, enable=True):
+        check(lib().ligmg_profile_enable(self._h, 1 if enable else 0))
+
+    def kernel_stats(self):
+        n = C.c_int32()
+        check(lib().ligmg_kernel_stats(self._h, None, 0, C.byref(n)))
+        arr = (_abi.KernelStat * max(n.value, 1))()
+        check(lib().ligmg_kernel_stats(self._h, arr, n.value, C.byref(n)))
+        out = []
+        for r in arr[: n.value]:
+            out.append({"level": r.level, "kind": _abi.KERNEL_KINDS.get(r.kind, str(r.kind)),
+                        "k": r.k, "fp64": bool(r.fp64), "launches": r.launches,
+                        "seconds": r.seconds, "bytes": r.bytes})
+        return out
+
+    def set_stream(self, stream_ptr):
+        check(lib().ligmg_set_stream(self._h, C.c_void_p(stream_ptr)))
+
+    @staticmethod
+    def launch_count():
+        x = C.c_int64()
+        check(lib().ligmg_launch_count(C.byref(x)))
+        return x.value
+
+    def solve_batched_device(self, b_ptr, k, x_ptr):
+        """Device pointers (n x k row-major FP64) on the handle's device."""
+        info, hist, ci, ct = self._info(k)
+        st = check(lib().ligmg_solve_batched_device(self._h, C.c_void_p(b_ptr), k,
+                                                    C.c_void_p(x_ptr), C.byref(info)),
+                   "ligmg_solve_batched_device")
+        return ConvergenceInfo(hist[: info.history_len].copy(), info.iters, info.solve_seconds,
+                               info.work, None, info.true_rel_residual, st == 0, ci, ct,
+                               info.cycle_complexity)
+
     def dump_csv(self, f, info: ConvergenceInfo, graph="graph", setup_time=0.0, nnz=0):
         """CSV row in the column order of print_csv (util.hpp:187-205)."""
         f.write("graph,solver,iters,rel_error,cycle_complexity,wda,setup_time,solve_time,nnz,nodes\n")

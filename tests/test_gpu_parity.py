@@ -159,10 +159,16 @@ def _bad(L, mutate):
 
 def test_invalid_inputs_return_status():
     L = G.grid2d(6)
-    off = int(np.where(L.col[: L.rowptr[1]] == 1)[0][0])
+    off = int(np.where(L.col[: L.rowptr[1]] == 1)[0][0])          # entry (0, 1)
+    mirror = int(L.rowptr[1] + np.where(L.col[L.rowptr[1]: L.rowptr[2]] == 0)[0][0])  # (1, 0)
+
+    def positive(rp, ci, v):
+        v[off] = 0.5
+        v[mirror] = 0.5
+
     cases = {
         3: lambda rp, ci, v: v.__setitem__(off, -2.0),            # not symmetric
-        5: lambda rp, ci, v: v.__setitem__(off, 0.5),             # positive off-diagonal
+        5: positive,                                              # positive off-diagonal
         6: lambda rp, ci, v: v.__setitem__(0, np.nan),            # non-finite
         4: lambda rp, ci, v: v.__setitem__(0, -1.0),              # bad diagonal
     }
