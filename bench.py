@@ -26,7 +26,11 @@ import sys
 import threading
 import time
 
+import faulthandler
+
 import numpy as np
+
+faulthandler.enable()
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -35,6 +39,10 @@ METRIC = "per-RHS time to rtol 1e-8: FP32/batched vs plain FP64 GPU; SpMV GB/s v
 SCALE = 20
 EDGE_FACTOR = 16
 GRAPH_SEED = 0
+
+
+def log(*a):
+    print("[bench]", *a, file=sys.stderr, flush=True)
 
 
 def parse():
@@ -199,6 +207,7 @@ def run_ours(args):
     k = args.k
     L = workload_graph(args.scale)
     n = L.n
+    log(f"graph n={n} nnz={L.nnz}")
     stream = torch.cuda.Stream(device=dev)
 
     def barrier():
@@ -210,6 +219,7 @@ def run_ours(args):
     t0 = time.perf_counter()
     S = Solver(L, **solver_kw("fp32"), device=local)
     setup_s = time.perf_counter() - t0
+    log(f"fp32 setup {setup_s:.2f}s levels={S.num_levels}")
     S.set_stream(stream.cuda_stream)
     nblk = 4
     rng_seed = 100 + 1000 * rank
@@ -236,6 +246,7 @@ def run_ours(args):
     barrier()
     clocks = sampler.stop()
     elapsed_ms = ev0.elapsed_time(ev1)
+    log(f"timed {elapsed_ms:.2f} ms for {args.steps} steps")
     stats = S.kernel_stats()
     S.profile(False)
     iters = [i.iters() for i in timed_infos]
@@ -250,7 +261,7 @@ def run_ours(args):
     from ligmg_gb300._lib import check, lib
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    info_e = S._info(k)[0]
+    info_e, keep_hist, keep_ci, keep_ct = S._info(k)  # arrays must outlive the calls
     e0.record(stream)
     for s in range(args.steps):
         check(lib().ligmg_solve_batched(S._h, C.c_void_p(Bh.data_ptr()), k,
@@ -258,6 +269,7 @@ def run_ours(args):
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
+    log(f"e2e {e2e_ms:.2f} ms")
     # ---- plain FP64 single-RHS GPU solve (spec comparison) ------------------
     fp64 = {}
     if not args.no_fp64:
@@ -289,6 +301,7 @@ def run_ours(args):
             fp64["spmv_gbs"] = top["bytes"] / top["seconds"] / 1e9
             fp64["spmv_level"] = top["level"]
         S64.close()
+        log(f"fp64 single {fp64['ms_per_rhs']:.2f} ms/RHS")
     # ---- aggregate over ranks ----------------------------------------------------
     if ws > 1:
         import torch.distributed as dist

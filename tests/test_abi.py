@@ -92,3 +92,22 @@ def test_python_solver_fails_loudly_without_library(monkeypatch, tmp_path):
     monkeypatch.setattr(lb, "_lib", None)
     with pytest.raises(RuntimeError):
         lb.lib(str(tmp_path / "missing.so"))
+
+
+def test_cpp_facade_compiles_and_links(built_lib, tmp_path):
+    src = tmp_path / "t.cpp"
+    src.write_text(f'''#include "{ROOT}/include/ligmg_gpu.hpp"
+int main() {{
+  ligmg::gpu::Options o;
+  o.kcycle = 1;
+  // no GPU is needed to reach the argument check
+  try {{ ligmg::gpu::Solver s(0, nullptr, nullptr, nullptr, o); }}
+  catch (const std::runtime_error &e) {{ return std::string(e.what()).find("invalid") == std::string::npos; }}
+  return 2;
+}}
+''')
+    exe = tmp_path / "t"
+    libdir = os.path.dirname(built_lib)
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-o", str(exe), str(src), f"-L{libdir}",
+                    "-lligmg_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    assert subprocess.run([str(exe)]).returncode == 0
