@@ -222,6 +222,25 @@ ligmg_status ligmg_set_stream(ligmg_handle h, void *stream);
 ligmg_status ligmg_get_stream(ligmg_handle h, void **stream);
 /* Kernels launched by this library in this process so far. */
 ligmg_status ligmg_launch_count(int64_t *count);
+
+/* y = A x with the level's FP64 matrix, device pointers, allocating nothing.
+ * This entry point has no counterpart in the reference.  It exists for
+ * callers that cannot allocate device memory at the point of the call: code
+ * recording a CUDA graph (an allocation during stream capture invalidates
+ * the capture) and applications whose memory is owned by their own pool
+ * allocator.  ligmg_spmv allocates temporary buffers on every call; this
+ * variant reads dx[n] and writes dy[n] (caller-owned) and keeps the
+ * split-row partial sums of power-law hub rows in a fixed static device
+ * array: at most 65536 row chunks and 16384 split rows per level (512 KiB +
+ * 64 KiB, held by every GPU that loads the library until exit).  A level
+ * beyond those limits returns LIGMG_ERR_UNSUPPORTED.  The work is queued on
+ * the handle's stream and the call returns without synchronising.  The
+ * first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  All calls share the one array, so
+ * calls that overlap on the GPU (other streams or handles) race; serialise
+ * them. */
+ligmg_status ligmg_spmv_device_noalloc(ligmg_handle h, int32_t level,
+                                       const double *dx, double *dy);
 /* Writes up to cap records (sorted by descending time) and the total count;
  * enabling again clears the statistics. */
 ligmg_status ligmg_kernel_stats(ligmg_handle h, ligmg_kernel_stat *out,

@@ -70,6 +70,7 @@ def lib(path=None):
     L.ligmg_set_stream.argtypes = [vp, vp]
     L.ligmg_get_stream.argtypes = [vp, P(vp)]
     L.ligmg_launch_count.argtypes = [P(C.c_int64)]
+    L.ligmg_spmv_device_noalloc.argtypes = [vp, C.c_int32, vp, vp]
     for name in header_functions():
         if name not in ("ligmg_default_options", "ligmg_status_string"):
             getattr(L, name).restype = C.c_int

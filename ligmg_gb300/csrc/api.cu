@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <tuple>
 #include <memory>
 #include <new>
@@ -1314,3 +1315,55 @@ ligmg_status ligmg_kernel_stats(ligmg_handle h, ligmg_kernel_stat *out, int32_t 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// ligmg_spmv_device_noalloc: the level SpMV without any allocation.  Its only
+// scratch (split hub-row partial sums and their completion counters) lives in
+// this fixed device array instead of buffers owned by the handle.
+namespace {
+constexpr i64 kNoallocMaxChunks = 65536;
+constexpr i64 kNoallocMaxHubs = 16384;
+constexpr size_t kNoallocCounterOffset = sizeof(double) * kNoallocMaxChunks;
+static __device__ __align__(256) unsigned char
+    g_spmv_scratch[sizeof(double) * kNoallocMaxChunks + sizeof(int) * kNoallocMaxHubs];
+
+// device address of g_spmv_scratch, looked up once per device with that
+// device current (the host-side symbol is only a stand-in)
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[128] = {nullptr};
+
+void *noalloc_scratch(int device) {
+  if (device < 0 || device >= 128) throw Error(LIGMG_ERR_INVALID_ARGUMENT, "device ordinal");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[device]) {
+    void *p = nullptr;
+    LG_CUDA(cudaGetSymbolAddress(&p, g_spmv_scratch));
+    g_noalloc_addr[device] = p;
+  }
+  return g_noalloc_addr[device];
+}
+}  // namespace
+
+extern "C" ligmg_status ligmg_spmv_device_noalloc(ligmg_handle h, int32_t level,
+                                                  const double *dx, double *dy) {
+  if (!h || !dx || !dy || level < 0 || level >= (int)h->h.size())
+    return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    const Level &L = *h->h[level];
+    if (L.hubA64.nchunks > kNoallocMaxChunks || L.hubA64.nhubs > kNoallocMaxHubs)
+      throw Error(LIGMG_ERR_UNSUPPORTED,
+                  "level has more split hub rows than the no-allocation scratch holds");
+    unsigned char *base = (unsigned char *)noalloc_scratch(h->device);
+    MatView<double> A = viewA<double>(L);
+    A.partial = (double *)base;
+    A.hub_counter = (int *)(base + kNoallocCounterOffset);
+    // the counters must start at zero; the array keeps the previous call's state
+    if (L.hubA64.nhubs > 0)
+      LG_CUDA(cudaMemsetAsync(A.hub_counter, 0, sizeof(int) * L.hubA64.nhubs, h->s));
+    EpiArgs a;
+    a.y = dy;
+    spmm<double>(A, dx, 1, Epi::Store, a, h->s);
+    return LIGMG_OK;
+  });
+}
