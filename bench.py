@@ -45,6 +45,22 @@ def log(*a):
     print("[bench]", *a, file=sys.stderr, flush=True)
 
 
+def nvtx_push(name):
+    try:
+        import torch
+        torch.cuda.nvtx.range_push(name)
+    except Exception:
+        pass
+
+
+def nvtx_pop():
+    try:
+        import torch
+        torch.cuda.nvtx.range_pop()
+    except Exception:
+        pass
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -236,12 +252,14 @@ def run_ours(args):
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = Solver.launch_count()
+    nvtx_push("timed_region")
     ev0.record(stream)
     timed_infos = []
     for s in range(args.steps):
         timed_infos.append(S.solve_batched_device(Bd[s % nblk].data_ptr(), k, Xd.data_ptr()))
     ev1.record(stream)
     torch.cuda.synchronize()
+    nvtx_pop()
     launches = Solver.launch_count() - l0
     barrier()
     clocks = sampler.stop()

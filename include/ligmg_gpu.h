@@ -123,6 +123,8 @@ typedef struct ligmg_options {
   int64_t rng_skip;           /* rand() draws consumed before setup (0) */
   int32_t verbose;            /* 0 */
   int32_t device;             /* CUDA device ordinal (0) */
+  int32_t use_graphs;         /* 1: replay each preconditioner application
+                                 from a captured CUDA graph (default 1) */
 } ligmg_options;
 
 /* ConvergenceInfo (util.hpp:143-170) of one solve.  For a batched solve the

@@ -73,6 +73,7 @@ class Options(C.Structure):
         ("rng_skip", C.c_int64),
         ("verbose", C.c_int32),
         ("device", C.c_int32),
+        ("use_graphs", C.c_int32),
     ]
 
 
@@ -135,6 +136,7 @@ def default_options(**overrides) -> Options:
     o.rng_skip = 0
     o.verbose = 0
     o.device = 0
+    o.use_graphs = 1
     for k, v in overrides.items():
         if k in ("smoother_type",) and isinstance(v, str):
             v = SMOOTHER[v]

@@ -123,9 +123,12 @@ struct Level {
   // FP32 copies for the FP32 hierarchy
   bool has32 = false;
   DBuf<float> Av32, invd32, Pv32, Rv32, Q32, pinv32;
-  // hub-row plans (A and, for elimination levels, R)
-  HubPlan<double> hubA64, hubR64;
-  HubPlan<float> hubA32, hubR32;
+  // hub-row plans: hubA64 (FP64, k = 1) is built at setup; the others are
+  // built on first use per (precision, k) from the cached host row pointers
+  HubPlan<double> hubA64;
+  mutable std::map<int, HubPlan<double>> hA64k, hR64k;
+  mutable std::map<int, HubPlan<float>> hA32k, hR32k;
+  std::vector<i64> rp_host, rrp_host;
   int lanesA = 32, lanesR = 32, lanesP = 4;
   // Chebyshev coefficients
   double theta = 1, delta = 1;
@@ -148,42 +151,56 @@ int lanes_for(i64 nnz, i64 n) {
   return 32;
 }
 
-constexpr i64 kHubThresh = 2048;
-constexpr i64 kHubChunk = 1024;
-constexpr int kMaxK = 64;
 
 template <typename T>
-MatView<T> viewA(const Level &L);
+std::map<int, HubPlan<T>> &plans(const Level &L, bool isR);
 template <>
-MatView<double> viewA<double>(const Level &L) {
-  MatView<double> m;
-  m.n = L.A.n; m.rp = L.A.rp.p; m.ci = L.A.ci.p; m.v = L.A.v.p; m.lanes_per_row = L.lanesA;
-  L.hubA64.fill(m);
-  return m;
+std::map<int, HubPlan<double>> &plans<double>(const Level &L, bool isR) {
+  return isR ? L.hR64k : L.hA64k;
 }
 template <>
-MatView<float> viewA<float>(const Level &L) {
-  MatView<float> m;
-  m.n = L.A.n; m.rp = L.A.rp.p; m.ci = L.A.ci.p; m.v = L.Av32.p; m.lanes_per_row = L.lanesA;
-  L.hubA32.fill(m);
+std::map<int, HubPlan<float>> &plans<float>(const Level &L, bool isR) {
+  return isR ? L.hR32k : L.hA32k;
+}
+
+template <typename T>
+const HubPlan<T> &plan_for(const Level &L, bool isR, int k, cudaStream_t s) {
+  if constexpr (sizeof(T) == 8) {
+    if (!isR && k == 1) return L.hubA64;
+  }
+  HubPlan<T> &p = plans<T>(L, isR)[k];
+  if (!p.built) {
+    const std::vector<i64> &rp = isR ? L.rrp_host : L.rp_host;
+    i64 n = isR ? L.elim.R.n : L.A.n;
+    p.build(rp.data(), n, entries_per_step(sizeof(T), k), k, s);
+  }
+  return p;
+}
+
+template <typename T>
+const T *valsA(const Level &L) {
+  if constexpr (sizeof(T) == 8) return (const T *)L.A.v.p;
+  else return (const T *)L.Av32.p;
+}
+template <typename T>
+const T *valsR(const Level &L) {
+  if constexpr (sizeof(T) == 8) return (const T *)L.elim.R.v.p;
+  else return (const T *)L.Rv32.p;
+}
+
+template <typename T>
+MatView<T> viewA(const Level &L, int k, cudaStream_t s) {
+  MatView<T> m;
+  m.n = L.A.n; m.rp = L.A.rp.p; m.ci = L.A.ci.p; m.v = valsA<T>(L); m.lanes_per_row = L.lanesA;
+  plan_for<T>(L, false, k, s).fill(m);
   return m;
 }
 template <typename T>
-MatView<T> viewR(const Level &L);
-template <>
-MatView<double> viewR<double>(const Level &L) {
-  MatView<double> m;
-  m.n = L.elim.R.n; m.rp = L.elim.R.rp.p; m.ci = L.elim.R.ci.p; m.v = L.elim.R.v.p;
+MatView<T> viewR(const Level &L, int k, cudaStream_t s) {
+  MatView<T> m;
+  m.n = L.elim.R.n; m.rp = L.elim.R.rp.p; m.ci = L.elim.R.ci.p; m.v = valsR<T>(L);
   m.lanes_per_row = L.lanesR;
-  L.hubR64.fill(m);
-  return m;
-}
-template <>
-MatView<float> viewR<float>(const Level &L) {
-  MatView<float> m;
-  m.n = L.elim.R.n; m.rp = L.elim.R.rp.p; m.ci = L.elim.R.ci.p; m.v = L.Rv32.p;
-  m.lanes_per_row = L.lanesR;
-  L.hubR32.fill(m);
+  plan_for<T>(L, true, k, s).fill(m);
   return m;
 }
 template <typename T>
@@ -244,9 +261,12 @@ struct ProfRec {
   int level, kind, k, fp64;
   cudaEvent_t a, b;
   double bytes;
+  bool graph_owned;  // events belong to a captured graph (re-recorded per replay)
 };
 struct Profiler {
   bool on = false;
+  bool capturing = false;
+  std::vector<ProfRec> capture_tmpl;
   std::vector<cudaEvent_t> pool;
   std::vector<ProfRec> pending;
   std::map<std::tuple<int, int, int, int>, ligmg_kernel_stat> stats;
@@ -276,20 +296,43 @@ struct Profiler {
       it->second.launches += 1;
       it->second.seconds += ms * 1e-3;
       it->second.bytes += r.bytes;
-      pool.push_back(r.a);
-      pool.push_back(r.b);
+      if (!r.graph_owned) {
+        pool.push_back(r.a);
+        pool.push_back(r.b);
+      }
     }
     pending.clear();
   }
   ~Profiler() {
-    for (auto &r : pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    for (auto &r : pending)
+      if (!r.graph_owned) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
+// A preconditioner application captured as a CUDA graph (one per k,
+// precision, base level and profiling state).
+struct PrecGraph {
+  cudaGraphExec_t exec = nullptr;
+  const double *r = nullptr;
+  double *z = nullptr;
+  bool prof = false;
+  std::vector<ProfRec> tmpl;
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    for (auto &t : tmpl) {
+      cudaEventDestroy(t.a);
+      cudaEventDestroy(t.b);
+    }
+    tmpl.clear();
   }
 };
 
 }  // namespace lg
 
 struct ligmg_handle_s {
+  std::map<std::tuple<int, int, int>, lg::PrecGraph> pgraphs;
   lg::Profiler prof;
   ligmg_options opts;
   int device = 0;
@@ -304,6 +347,8 @@ struct ligmg_handle_s {
   std::map<int, std::unique_ptr<lg::OuterWork>> ow;
   ~ligmg_handle_s() {
     if (s) cudaStreamSynchronize(s);
+    for (auto &g : pgraphs) g.second.reset();
+    pgraphs.clear();
     w32.clear();
     w64.clear();
     ow.clear();
@@ -328,11 +373,21 @@ void timed(Handle &H, int level, int kind, int k, int fp64, double bytes, F &&f)
     f();
     return;
   }
+  if (H.prof.capturing) {  // event-record nodes owned by the graph
+    cudaEvent_t a, b;
+    LG_CUDA(cudaEventCreate(&a));
+    LG_CUDA(cudaEventCreate(&b));
+    LG_CUDA(cudaEventRecord(a, H.s));
+    f();
+    LG_CUDA(cudaEventRecord(b, H.s));
+    H.prof.capture_tmpl.push_back({level, kind, k, fp64, a, b, bytes, true});
+    return;
+  }
   cudaEvent_t a = H.prof.get(), b = H.prof.get();
   LG_CUDA(cudaEventRecord(a, H.s));
   f();
   LG_CUDA(cudaEventRecord(b, H.s));
-  H.prof.pending.push_back({level, kind, k, fp64, a, b, bytes});
+  H.prof.pending.push_back({level, kind, k, fp64, a, b, bytes, false});
 }
 
 // algorithmic (compulsory) bytes: every array element read or written once
@@ -362,12 +417,6 @@ void ensure_fp32(Handle &H) {
     if (L.type == LIGMG_LEVEL_COARSE) {
       L.pinv32.alloc(L.pinv.n, s);
       convert<double, float>(L.pinv.n, L.pinv.p, L.pinv32.p, s);
-    }
-    std::vector<i64> rp = L.A.rp.to_host();
-    L.hubA32.build(rp.data(), L.A.n, kHubThresh, kHubChunk, kMaxK, s);
-    if (L.type == LIGMG_LEVEL_ELIM) {
-      std::vector<i64> rr = L.elim.R.rp.to_host();
-      L.hubR32.build(rr.data(), L.elim.R.n, kHubThresh, kHubChunk, kMaxK, s);
     }
     L.has32 = true;
   }
@@ -437,7 +486,7 @@ struct Engine {
     Level &L = *H.h[l];
     LevelWork<T> &w = W.lw[l];
     i64 n = L.A.n;
-    MatView<T> A = viewA<T>(L);
+    MatView<T> A = viewA<T>(L, k, s);
     const T *invd = invdT<T>(L);
     if (o().smoother_type == LIGMG_SMOOTHER_JACOBI)
       throw Error(LIGMG_ERR_UNSUPPORTED, "jacobi smoother in the solve phase");
@@ -508,7 +557,7 @@ struct Engine {
       a.y = nw.in.p;
       timed(H, (int)l, LIGMG_KERNEL_ELIM_RESTRICT, k, sizeof(T) == 8,
             core_bytes(L.elim.R.n, L.elim.R.nnz, n, k, sizeof(T)) + (double)L.elim.R.n * k * sizeof(T),
-            [&] { spmm<T>(viewR<T>(L), b, k, Epi::Store, a, s); });
+            [&] { spmm<T>(viewR<T>(L, k, s), b, k, Epi::Store, a, s); });
       recurse(l, nw.in.p, nw.out.p);
       EpiArgs c;
       c.y = x; c.b = b; c.q = QT<T>(L);
@@ -525,7 +574,7 @@ struct Engine {
     a.b = b;
     timed(H, (int)l, LIGMG_KERNEL_RESID, k, sizeof(T) == 8,
           core_bytes(n, L.A.nnz, n, k, sizeof(T)) + 2.0 * n * k * sizeof(T),
-          [&] { spmm<T>(viewA<T>(L), x, k, Epi::Resid, a, s); });
+          [&] { spmm<T>(viewA<T>(L, k, s), x, k, Epi::Resid, a, s); });
     restrict_agg<T>(L.nc, k, L.agg.mrp.p, L.agg.members.p, w.r.p, nw.in.p, s);
     recurse(l, nw.in.p, nw.out.p);
     prolong_agg<T>(n, k, L.agg.agg.p, nw.out.p, x, s);
@@ -548,7 +597,7 @@ struct Engine {
     Level &L = *H.h[l];
     LevelWork<T> &w = W.lw[l];
     i64 n = L.A.n;
-    MatView<T> A = viewA<T>(L);
+    MatView<T> A = viewA<T>(L, k, s);
     LG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * n * k, s));
     T *r = b;
     T *p = w.fp0.p, *pp = w.fp1.p, *q = w.fq0.p, *qp = w.fq1.p;
@@ -599,7 +648,7 @@ void estimate_lmax(Handle &H, Level &L) {
   LG_CUDA(cudaMemcpyAsync(p.p, z.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   col_reduce<double>(n, 1, Red::Dot, r.p, z.p, sc.p, scratch.p, slen, s);
   double rz = read_scalar(sc.p, s);
-  MatView<double> A = viewA<double>(L);
+  MatView<double> A = viewA<double>(L, 1, s);
   std::vector<double> alphas, betas;
   for (int it = 0; it < 5; it++) {
     if (!(rz > 0)) break;
@@ -660,11 +709,10 @@ void finish_level(Handle &H, Level &L) {
   k_invdiag<<<grid_for(L.A.n, 256), 256, 0, s>>>(L.A.rp.p, L.A.ci.p, L.A.v.p, L.A.n, L.invd.p);
   LG_LAUNCH();
   L.lanesA = lanes_for(L.A.nnz, L.A.n);
-  std::vector<i64> rp = L.A.rp.to_host();
-  L.hubA64.build(rp.data(), L.A.n, kHubThresh, kHubChunk, kMaxK, s);
+  L.rp_host = L.A.rp.to_host();
+  L.hubA64.build(L.rp_host.data(), L.A.n, entries_per_step(8, 1), 1, s);
   if (L.type == LIGMG_LEVEL_ELIM) {
-    std::vector<i64> rr = L.elim.R.rp.to_host();
-    L.hubR64.build(rr.data(), L.elim.R.n, kHubThresh, kHubChunk, kMaxK, s);
+    L.rrp_host = L.elim.R.rp.to_host();
     L.lanesR = lanes_for(L.elim.R.nnz, L.elim.R.n);
     L.lanesP = lanes_for(L.elim.P.nnz, L.elim.P.n);
   }
@@ -789,8 +837,11 @@ OuterWork &outer_work(Handle &H, int k, i64 nb, i64 n0) {
   return w;
 }
 
+// z = M(r) with the constant projected out of z.  `sum`, `scratch` are the
+// outer workspace's reduction slots.
 template <typename T>
-void apply_prec(Handle &H, int k, size_t base, const double *r, double *z) {
+void apply_prec_body(Handle &H, int k, size_t base, const double *r, double *z, double *sum,
+                     double *scratch, i64 scratch_len) {
   Level &L = *H.h[base];
   i64 n = L.A.n;
   Work<T> &W = work_for<T>(H, k);
@@ -803,6 +854,52 @@ void apply_prec(Handle &H, int k, size_t base, const double *r, double *z) {
     E.cycle(base, w.in.p, w.out.p);
     convert<float, double>(n * k, w.out.p, z, H.s);
   }
+  col_reduce<double>(n, k, Red::Sum, z, nullptr, sum, scratch, scratch_len, H.s);
+  sub_mean<double>(n, k, z, sum, H.s);
+}
+
+// The K-cycle issues thousands of small kernels per application; after one
+// direct run (which also creates every lazily built plan and buffer) the
+// sequence is captured once into a CUDA graph and replayed.
+template <typename T>
+void apply_prec(Handle &H, int k, size_t base, const double *r, double *z, double *sum,
+                double *scratch, i64 scratch_len) {
+  auto body = [&] { apply_prec_body<T>(H, k, base, r, z, sum, scratch, scratch_len); };
+  if (!H.opts.use_graphs) {
+    body();
+    return;
+  }
+  PrecGraph &g = H.pgraphs[std::make_tuple(k, (int)sizeof(T), (int)base)];
+  if (g.exec && g.r == r && g.z == z && g.prof == H.prof.on) {
+    LG_CUDA(cudaGraphLaunch(g.exec, H.s));
+    if (H.prof.on)
+      for (const ProfRec &t : g.tmpl) H.prof.pending.push_back(t);
+    return;
+  }
+  g.reset();
+  body();  // direct run: produces this application's result
+  cudaGraph_t graph = nullptr;
+  H.prof.capture_tmpl.clear();
+  H.prof.capturing = H.prof.on;
+  LG_CUDA(cudaStreamBeginCapture(H.s, cudaStreamCaptureModeThreadLocal));
+  try {
+    body();
+  } catch (...) {
+    cudaStreamEndCapture(H.s, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    H.prof.capturing = false;
+    throw;
+  }
+  H.prof.capturing = false;
+  LG_CUDA(cudaStreamEndCapture(H.s, &graph));
+  cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  LG_CUDA(e);
+  g.r = r;
+  g.z = z;
+  g.prof = H.prof.on;
+  g.tmpl = H.prof.capture_tmpl;
+  H.prof.capture_tmpl.clear();
 }
 
 struct SolveResult {
@@ -820,7 +917,7 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
   cudaStream_t s = H.s;
   Level &L = *H.h[base];
   i64 n = L.A.n;
-  MatView<double> A = viewA<double>(L);
+  MatView<double> A = viewA<double>(L, k, s);
   SolveResult res;
   res.col_iters.assign(k, 0);
   res.rel.assign(k, 1.0);
@@ -849,9 +946,7 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
   bool cg = o.outer_ksp_type == LIGMG_KSP_CG;
   double *P = w.P0.p, *PP = w.P1.p, *Q = w.Q0.p, *QP = w.Q1.p;
   auto precondition = [&]() {
-    apply_prec<T>(H, k, base, w.R.p, w.Z.p);
-    col_reduce<double>(n, k, Red::Sum, w.Z.p, nullptr, sum, w.scratch.p, w.scratch_len, s);
-    sub_mean<double>(n, k, w.Z.p, sum, s);
+    apply_prec<T>(H, k, base, w.R.p, w.Z.p, sum, w.scratch.p, w.scratch_len);
   };
   if (cg && active) {
     precondition();
@@ -897,6 +992,7 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
     col_reduce<double>(n, k, Red::Dot, w.R.p, w.R.p, rn2, w.scratch.p, w.scratch_len, s);
     LG_CUDA(cudaMemcpyAsync(h_rn2.data(), rn2, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
     LG_CUDA(cudaStreamSynchronize(s));
+    if (H.prof.on) H.prof.collect();  // graph replays re-record the same events
     bool changed = false;
     for (int c = 0; c < k; c++) {
       if (frozen[c]) continue;
@@ -944,7 +1040,7 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
     a.y = w.B.p;
     timed(H, from, LIGMG_KERNEL_ELIM_RESTRICT, k, 1,
           core_bytes(F.elim.R.n, F.elim.R.nnz, n0, k, 8) + 8.0 * F.elim.R.n * k,
-          [&] { spmm<double>(viewR<double>(F), w.Bfull.p, k, Epi::Store, a, s); });
+          [&] { spmm<double>(viewR<double>(F, k, s), w.Bfull.p, k, Epi::Store, a, s); });
   } else {
     LG_CUDA(cudaMemcpyAsync(w.B.p, w.Bfull.p, sizeof(double) * n0 * k, cudaMemcpyDeviceToDevice, s));
   }
@@ -968,7 +1064,7 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
   a.y = w.Res.p;
   a.b = w.Bfull.p;
   timed(H, from, LIGMG_KERNEL_RESID, k, 1, core_bytes(n0, F.A.nnz, n0, k, 8) + 16.0 * n0 * k,
-        [&] { spmm<double>(viewA<double>(F), w.Xfull.p, k, Epi::Resid, a, s); });
+        [&] { spmm<double>(viewA<double>(F, k, s), w.Xfull.p, k, Epi::Resid, a, s); });
   col_reduce<double>(n0, k, Red::Dot, w.Res.p, w.Res.p, d1, w.scratch.p, w.scratch_len, s);
   col_reduce<double>(n0, k, Red::Dot, w.Bfull.p, w.Bfull.p, d2, w.scratch.p, w.scratch_len, s);
   std::vector<double> h1(k), h2(k);
@@ -1069,6 +1165,7 @@ void ligmg_default_options(ligmg_options *o) {
   o->rng_skip = 0;
   o->verbose = 0;
   o->device = 0;
+  o->use_graphs = 1;
 }
 
 const char *ligmg_status_string(ligmg_status s) {
@@ -1252,7 +1349,7 @@ ligmg_status ligmg_spmv(ligmg_handle h, int32_t level, const double *x, double *
     dx.upload(x, n);
     EpiArgs a;
     a.y = dy.p;
-    spmm<double>(viewA<double>(L), dx.p, 1, Epi::Store, a, h->s);
+    spmm<double>(viewA<double>(L, 1, h->s), dx.p, 1, Epi::Store, a, h->s);
     dy.download(y, n);
     LG_CUDA(cudaStreamSynchronize(h->s));
     return LIGMG_OK;
@@ -1355,7 +1452,7 @@ extern "C" ligmg_status ligmg_spmv_device_noalloc(ligmg_handle h, int32_t level,
       throw Error(LIGMG_ERR_UNSUPPORTED,
                   "level has more split hub rows than the no-allocation scratch holds");
     unsigned char *base = (unsigned char *)noalloc_scratch(h->device);
-    MatView<double> A = viewA<double>(L);
+    MatView<double> A = viewA<double>(L, 1, h->s);
     A.partial = (double *)base;
     A.hub_counter = (int *)(base + kNoallocCounterOffset);
     // the counters must start at zero; the array keeps the previous call's state

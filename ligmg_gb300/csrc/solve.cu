@@ -13,15 +13,27 @@
 namespace lg {
 
 // ---------------------------------------------------------------------------
+int entries_per_step(int value_bytes, int k) {
+  int W = value_bytes == 4 ? 4 : 2;
+  int VW = (k % W == 0) ? W : 1;
+  int L = std::max(1, k / VW);
+  return std::max(1, 32 / L);
+}
+
 template <typename T>
-void HubPlan<T>::build(const i64 *rp_host, i64 n, i64 thr, i64 chunk, int kmax, cudaStream_t s) {
-  thresh = thr;
+void HubPlan<T>::build(const i64 *rp_host, i64 n, int E, int kmax, cudaStream_t s) {
+  built = true;
+  kcap = kmax;
+  thresh = 64 * (i64)E;
+  i64 thr = thresh;
   std::vector<i64> row, beg, end;
   std::vector<i32> hub, first, cnt;
   nhubs = 0;
   for (i64 r = 0; r < n; r++) {
     i64 len = rp_host[r + 1] - rp_host[r];
     if (len <= thr) continue;
+    i64 want = std::min<i64>(std::max<i64>(cdiv(len, 32 * (i64)E), 2), 256);
+    i64 chunk = cdiv(len, want);
     i32 nc = (i32)cdiv(len, chunk);
     i32 f = (i32)row.size();
     for (i32 c = 0; c < nc; c++) {
@@ -35,7 +47,6 @@ void HubPlan<T>::build(const i64 *rp_host, i64 n, i64 thr, i64 chunk, int kmax, 
     nhubs++;
   }
   nchunks = (i64)row.size();
-  kcap = kmax;
   if (nchunks == 0) {
     thresh = 0;
     return;
@@ -258,17 +269,21 @@ __global__ void __launch_bounds__(256) k_spmm(const MatView<T> A, const T *__res
     last = __shfl_sync(0xffffffffu, last, 0);
     if (!last) return;
     __threadfence();
-    if (slot == 0) {
+    {
+      // every slot sums a strided subset of the chunk partials; the slot
+      // partials are combined in a fixed shuffle tree (deterministic)
       const i64 first = A.ch_first[c];
       const int cnt = A.ch_cnt[c];
       T s[VW];
 #pragma unroll
       for (int q = 0; q < VW; q++) s[q] = (T)0;
-      for (int t = 0; t < cnt; t++) {
+#pragma unroll 4
+      for (int t = slot; t < cnt; t += E) {
 #pragma unroll
         for (int q = 0; q < VW; q++) s[q] += __ldcg(A.partial + (first + t) * K + ch * VW + q);
       }
-      epilogue<T, K, VW, EP>(a, A.ch_row[c], ch * VW, s);
+      reduce_slots<T, VW, L, G>(s);
+      if (slot == 0) epilogue<T, K, VW, EP>(a, A.ch_row[c], ch * VW, s);
     }
     if (lane == 0) A.hub_counter[A.ch_hub[c]] = 0;
   }

@@ -26,6 +26,8 @@ struct MatView {
 };
 
 // Hub-row schedule owned by a level (built once at setup).
+// A row is split when it needs more than 64 warp steps (E nonzeros per step),
+// into at most 256 chunks of at least 32 steps.
 template <typename T>
 struct HubPlan {
   i64 thresh = 0, nchunks = 0, nhubs = 0;
@@ -34,9 +36,12 @@ struct HubPlan {
   DBuf<int> counter;
   DBuf<T> partial;
   int kcap = 0;
-  void build(const i64 *rp_host, i64 n, i64 thresh, i64 chunk, int kmax, cudaStream_t s);
+  bool built = false;
+  void build(const i64 *rp_host, i64 n, int entries_per_step, int kmax, cudaStream_t s);
   void fill(MatView<T> &m) const;
 };
+// nonzeros a 32-lane group advances per step for k right-hand sides
+int entries_per_step(int value_bytes, int k);
 
 enum class Epi {
   Store,       // y = A x

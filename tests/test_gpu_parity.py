@@ -140,6 +140,28 @@ def test_batched_matches_single(prec, k):
         assert _relerr(info.solution[:, c], single.solution) <= 1e-6
 
 
+def test_graph_replay_matches_direct_launches():
+    L = GRAPHS["rmat14"]()
+    B = G.rhs(L.n, k=8, seed=3)
+    kw = dict(precision="fp32", kcycle=1, outer_ksp_type="fcg")
+    a = Solver(L, **kw).solve_batched(B)
+    b = Solver(L, use_graphs=0, **kw).solve_batched(B)
+    assert a.iters() == b.iters()
+    assert np.array_equal(a.solution, b.solution)
+
+
+def test_profiled_solve_reports_kernels():
+    L = GRAPHS["rmat14"]()
+    S = Solver(L, precision="fp32", kcycle=1, outer_ksp_type="fcg")
+    S.profile(True)
+    info = S.solve_batched(G.rhs(L.n, k=32, seed=4))
+    st = S.kernel_stats()
+    assert info.converged and st
+    assert all(r["seconds"] > 0 and r["bytes"] > 0 and r["launches"] > 0 for r in st)
+    kinds = {r["kind"] for r in st}
+    assert {"cheb_b", "resid", "spmv"} <= kinds
+
+
 def test_solve_from_level():
     L = GRAPHS["my_matrix"]()
     S = Solver(L, outer_ksp_type="fcg")
