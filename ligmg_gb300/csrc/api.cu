@@ -123,6 +123,7 @@ struct Level {
   // FP32 copies for the FP32 hierarchy
   bool has32 = false;
   DBuf<float> Av32, invd32, Pv32, Rv32, Q32, pinv32;
+  DBuf<float2> Adf;  // (hi, lo) float pairs of A's FP64 values (outer product)
   // hub-row plans: hubA64 (FP64, k = 1) is built at setup; the others are
   // built on first use per (precision, k) from the cached host row pointers
   HubPlan<double> hubA64;
@@ -236,7 +237,7 @@ struct LevelWork {
   i64 n = 0;
   DBuf<T> in, out, r, d0, d1, xt;           // cycle buffers
   DBuf<T> fz, fp0, fp1, fq0, fq1;           // K-cycle FCG buffers (fr = in, fx = out)
-  DBuf<double> sc, scratch;
+  DBuf<double> sc, scratch, fscratch;
   i64 scratch_len = 0;
   double *slot(int s, int k) { return sc.p + (i64)s * k * 2; }
 };
@@ -250,7 +251,8 @@ struct Work {
 struct OuterWork {
   int k = 0;
   i64 n = 0;
-  DBuf<double> X, R, Z, P0, P1, Q0, Q1, B, Bfull, Xfull, Res, sc, scratch;
+  DBuf<double> X, R, Z, P0, P1, Q0, Q1, B, Bfull, Xfull, Res, sc, scratch, fscratch;
+  DBuf<float2> Pdf;
   DBuf<int> frozen;
   i64 scratch_len = 0;
   double *slot(int s) { return sc.p + (i64)s * k * 2; }
@@ -377,9 +379,11 @@ void timed(Handle &H, int level, int kind, int k, int fp64, double bytes, F &&f)
     cudaEvent_t a, b;
     LG_CUDA(cudaEventCreate(&a));
     LG_CUDA(cudaEventCreate(&b));
-    LG_CUDA(cudaEventRecord(a, H.s));
+    // inside a capture a plain record is only a dependency marker; External
+    // makes it an event-record node that every replay re-records
+    LG_CUDA(cudaEventRecordWithFlags(a, H.s, cudaEventRecordExternal));
     f();
-    LG_CUDA(cudaEventRecord(b, H.s));
+    LG_CUDA(cudaEventRecordWithFlags(b, H.s, cudaEventRecordExternal));
     H.prof.capture_tmpl.push_back({level, kind, k, fp64, a, b, bytes, true});
     return;
   }
@@ -467,6 +471,8 @@ Work<T> &work_for(Handle &H, int k) {
     w.sc.zero();
     w.scratch_len = col_reduce_scratch(n, k);
     w.scratch.alloc(w.scratch_len, s);
+    w.fscratch.alloc(fused_scratch_len(n, k), s);
+    w.fscratch.zero();  // reduction ticket starts at zero
   }
   return W;
 }
@@ -592,7 +598,9 @@ struct Engine {
   }
 
   // K-cycle inner FCG with a fixed number of iterations, x0 = 0; r = b is
-  // updated in place (b is the level's restriction buffer).
+  // updated in place (b is the level's restriction buffer).  Five launches
+  // per iteration: cycle, beta (fused reduction), direction, SpMM, alpha
+  // (fused reduction), update.
   void fcg_fixed(size_t l, T *b, T *x, int iters) {
     Level &L = *H.h[l];
     LevelWork<T> &w = W.lw[l];
@@ -601,31 +609,22 @@ struct Engine {
     LG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * n * k, s));
     T *r = b;
     T *p = w.fp0.p, *pp = w.fp1.p, *q = w.fq0.p, *qp = w.fq1.p;
-    double *eta = w.slot(S_ETA0, k), *eta_prev = w.slot(S_ETA1, k);
+    FcgScalars sc{w.slot(S_SUM, k), w.slot(S_BETA, k), w.slot(S_ETA0, k), w.slot(S_ETA1, k),
+                  w.slot(S_ALPHA, k), nullptr};
     for (int it = 0; it < iters; it++) {
       cycle(l, r, w.fz.p);
-      col_reduce<T>(n, k, Red::Sum, w.fz.p, nullptr, w.slot(S_SUM, k), w.scratch.p,
-                    w.scratch_len, s);
-      sub_mean<T>(n, k, w.fz.p, w.slot(S_SUM, k), s);
-      if (it > 0) {
-        col_reduce<T>(n, k, Red::Dot, w.fz.p, qp, w.slot(S_ZQ, k), w.scratch.p, w.scratch_len, s);
-        scal_beta(k, w.slot(S_ZQ, k), eta_prev, w.slot(S_BETA, k), s);
-        fcg_direction<T>(n, k, p, w.fz.p, pp, w.slot(S_BETA, k), s);
-      } else {
-        fcg_direction<T>(n, k, p, w.fz.p, nullptr, nullptr, s);
-      }
+      fcg_beta<T>(n, k, w.fz.p, it > 0 ? qp : nullptr, sc, w.fscratch.p, s);
+      fcg_dir<T>(n, k, p, w.fz.p, it > 0 ? pp : nullptr, sc, s);
       EpiArgs a;
       a.y = q;
       timed(H, (int)l, LIGMG_KERNEL_SPMV, k, sizeof(T) == 8,
             core_bytes(n, L.A.nnz, n, k, sizeof(T)) + 1.0 * n * k * sizeof(T),
             [&] { spmm<T>(A, p, k, Epi::Store, a, s); });
-      col_reduce<T>(n, k, Red::Dot, p, q, eta, w.scratch.p, w.scratch_len, s);
-      col_reduce<T>(n, k, Red::Dot, p, r, w.slot(S_RHO, k), w.scratch.p, w.scratch_len, s);
-      scal_div(k, w.slot(S_RHO, k), eta, w.slot(S_ALPHA, k), nullptr, s);
-      fcg_update<T>(n, k, x, r, p, q, w.slot(S_ALPHA, k), it + 1 < iters, s);
+      fcg_alpha<T>(n, k, p, q, r, sc, w.fscratch.p, s);
+      fcg_update<T>(n, k, x, r, p, q, sc.alpha, it + 1 < iters, s);
       std::swap(p, pp);
       std::swap(q, qp);
-      std::swap(eta, eta_prev);
+      std::swap(sc.eta, sc.eta_prev);
     }
   }
 };
@@ -833,7 +832,10 @@ OuterWork &outer_work(Handle &H, int k, i64 nb, i64 n0) {
   w.sc.zero();
   w.scratch_len = std::max(col_reduce_scratch(nb, k), col_reduce_scratch(n0, k));
   w.scratch.alloc(w.scratch_len, s);
+  w.fscratch.alloc(std::max(fused_scratch_len(nb, k), fused_scratch_len(n0, k)), s);
+  w.fscratch.zero();
   w.frozen.alloc(k, s);
+  w.Pdf.alloc(nb * k, s);
   return w;
 }
 
@@ -944,6 +946,13 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
   res.hist0.push_back(rn0[0]);
   LG_CUDA(cudaMemcpyAsync(w.frozen.p, frozen.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
   bool cg = o.outer_ksp_type == LIGMG_KSP_CG;
+  // FP32 hierarchy: the outer product A p runs in double-float (48-bit
+  // significand at FP32 throughput); the FP64 hierarchy keeps native FP64
+  bool dfprod = sizeof(T) == 4;
+  if (dfprod && L.Adf.n != L.A.nnz) {
+    L.Adf.alloc(L.A.nnz, s);
+    split_df(L.A.nnz, L.A.v.p, L.Adf.p, s);
+  }
   double *P = w.P0.p, *PP = w.P1.p, *Q = w.Q0.p, *QP = w.Q1.p;
   auto precondition = [&]() {
     apply_prec<T>(H, k, base, w.R.p, w.Z.p, sum, w.scratch.p, w.scratch_len);
@@ -968,28 +977,25 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
       col_reduce<double>(n, k, Red::Dot, P, Q, eta, w.scratch.p, w.scratch_len, s);
       scal_div(k, bcg, eta, alpha, w.frozen.p, s);
       fcg_update<double>(n, k, w.X.p, w.R.p, P, Q, alpha, true, s);
-    } else {  // FCG (Notay), one stored direction
+    } else {  // FCG (Notay), one stored direction; fused scalar reductions
       precondition();
-      if (it > 0) {
-        col_reduce<double>(n, k, Red::Dot, w.Z.p, QP, tmp, w.scratch.p, w.scratch_len, s);
-        scal_beta(k, tmp, eta_prev, beta, s);
-        fcg_direction<double>(n, k, P, w.Z.p, PP, beta, s);
-      } else {
-        fcg_direction<double>(n, k, P, w.Z.p, nullptr, nullptr, s);
-      }
+      FcgScalars sc{tmp, beta, eta, eta_prev, alpha, w.frozen.p};
+      fcg_beta<double>(n, k, w.Z.p, it > 0 ? QP : nullptr, sc, w.fscratch.p, s);
+      fcg_dir<double>(n, k, P, w.Z.p, it > 0 ? PP : nullptr, sc, s, dfprod ? w.Pdf.p : nullptr);
       EpiArgs a;
       a.y = Q;
       timed(H, (int)base, LIGMG_KERNEL_SPMV, k, 1, core_bytes(n, L.A.nnz, n, k, 8) + 8.0 * n * k,
-            [&] { spmm<double>(A, P, k, Epi::Store, a, s); });
-      col_reduce<double>(n, k, Red::Dot, P, Q, eta, w.scratch.p, w.scratch_len, s);
-      col_reduce<double>(n, k, Red::Dot, P, w.R.p, rho, w.scratch.p, w.scratch_len, s);
-      scal_div(k, rho, eta, alpha, w.frozen.p, s);
+            [&] {
+              if (dfprod) spmm_df(A, L.Adf.p, w.Pdf.p, k, Q, s);
+              else spmm<double>(A, P, k, Epi::Store, a, s);
+            });
+      fcg_alpha<double>(n, k, P, Q, w.R.p, sc, w.fscratch.p, s);
       fcg_update<double>(n, k, w.X.p, w.R.p, P, Q, alpha, true, s);
       std::swap(P, PP);
       std::swap(Q, QP);
       std::swap(eta, eta_prev);
     }
-    col_reduce<double>(n, k, Red::Dot, w.R.p, w.R.p, rn2, w.scratch.p, w.scratch_len, s);
+    col_dot1<double>(n, k, w.R.p, w.R.p, rn2, w.fscratch.p, s);
     LG_CUDA(cudaMemcpyAsync(h_rn2.data(), rn2, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
     LG_CUDA(cudaStreamSynchronize(s));
     if (H.prof.on) H.prof.collect();  // graph replays re-record the same events
@@ -1107,6 +1113,7 @@ bool k_supported(int k) {
 template <typename F>
 ligmg_status guard(F &&f) {
   try {
+    (void)cudaGetLastError();  // a failed earlier call must not leak into this one
     return f();
   } catch (const Error &e) {
     return e.status;

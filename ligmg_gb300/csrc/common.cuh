@@ -25,6 +25,7 @@ struct Error : std::runtime_error {
 
 inline void cuda_check(cudaError_t e, const char *what) {
   if (e == cudaSuccess) return;
+  (void)cudaGetLastError();  // clear a non-sticky error so later calls start clean
   if (e == cudaErrorMemoryAllocation)
     throw Error(LIGMG_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
   throw Error(LIGMG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));

@@ -503,7 +503,332 @@ __global__ void k_scal_beta(int k, const double *zq, const double *eta_prev, dou
   beta[c] = e == 0.0 ? 0.0 : zq[c] / e;
 }
 
+// ---- fused reductions ------------------------------------------------------
+// OP 0: [sum x]            OP 1: [sum x.y]
+// OP 2: [sum x, sum x.y, sum y]   (FCG beta)     OP 3: [sum x.y, sum x.w]  (alpha)
+template <typename T, int OP>
+__global__ void __launch_bounds__(256)
+    k_fused_red(i64 n, int k, const T *x, const T *y, const T *w, i64 rows_per_block,
+                double *scratch, FcgScalars sc, double *out) {
+  constexpr int NV = (OP == 2) ? 3 : (OP == 3 ? 2 : 1);
+  __shared__ double sh[NV][256];
+  __shared__ int last;
+  const int tid = threadIdx.x;
+  const int c = tid % k, rsub = tid / k, rstride = 256 / k;
+  const i64 r0 = (i64)blockIdx.x * rows_per_block;
+  const i64 r1 = min(n, r0 + rows_per_block);
+  double a[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) a[v] = 0;
+  for (i64 r = r0 + rsub; r < r1; r += rstride) {
+    const i64 o = r * k + c;
+    double xv = (double)x[o];
+    if constexpr (OP == 0) {
+      a[0] += xv;
+    } else if constexpr (OP == 1) {
+      a[0] += xv * (double)y[o];
+    } else if constexpr (OP == 2) {
+      a[0] += xv;
+      if (y) {
+        double yv = (double)y[o];
+        a[1] += xv * yv;
+        a[2] += yv;
+      }
+    } else {
+      a[0] += xv * (double)y[o];
+      a[1] += xv * (double)w[o];
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NV; v++) sh[v][tid] = a[v];
+  __syncthreads();
+  for (int st = 128; st >= k; st >>= 1) {
+    if (tid < st)
+#pragma unroll
+      for (int v = 0; v < NV; v++) sh[v][tid] += sh[v][tid + st];
+    __syncthreads();
+  }
+  double *part = scratch + 2;  // scratch[0]: ticket
+  if (tid < k)
+#pragma unroll
+    for (int v = 0; v < NV; v++) part[((i64)blockIdx.x * NV + v) * k + tid] = sh[v][tid];
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    unsigned t = atomicAdd((unsigned *)scratch, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (tid < k) {
+    double tot[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) tot[v] = 0;
+    for (unsigned b = 0; b < gridDim.x; b++)
+#pragma unroll
+      for (int v = 0; v < NV; v++) tot[v] += __ldcg(part + ((i64)b * NV + v) * k + tid);
+    if constexpr (OP == 0 || OP == 1) {
+      out[tid] = tot[0];
+    } else if constexpr (OP == 2) {
+      double mu = tot[0] / (double)n;
+      sc.mu[tid] = mu;
+      if (y) {
+        double e = sc.eta_prev[tid];
+        sc.beta[tid] = e == 0.0 ? 0.0 : (tot[1] - mu * tot[2]) / e;
+      } else {
+        sc.beta[tid] = 0.0;
+      }
+    } else {
+      double eta = tot[0];
+      sc.eta[tid] = eta;
+      bool fz = sc.frozen && sc.frozen[tid];
+      sc.alpha[tid] = (fz || eta == 0.0) ? 0.0 : tot[1] / eta;
+    }
+  }
+  if (tid == 0) *(unsigned *)scratch = 0u;
+}
+
+template <typename T>
+__global__ void k_fcg_dir(i64 n, int k, T *p, const T *z, const T *pp, FcgScalars sc,
+                          float2 *pdf) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  int c = (int)(t % k);
+  T v = z[t] - (T)sc.mu[c];
+  if (pp) v = v - (T)sc.beta[c] * pp[t];
+  p[t] = v;
+  if (pdf) {
+    float h = (float)v;
+    pdf[t] = make_float2(h, (float)((double)v - (double)h));
+  }
+}
+
+// ---- double-float SpMM ------------------------------------------------------
+__device__ __forceinline__ void df_fma(float ah, float al, float xh, float xl, float &sh,
+                                       float &sl) {
+  float ph = __fmul_rn(ah, xh);
+  float pl = __fmaf_rn(ah, xh, -ph);  // exact error of ah*xh
+  pl = __fmaf_rn(ah, xl, pl);
+  pl = __fmaf_rn(al, xh, pl);
+  float s = __fadd_rn(sh, ph);        // TwoSum(sh, ph)
+  float v = __fsub_rn(s, sh);
+  float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, v)), __fsub_rn(ph, v));
+  sl = __fadd_rn(sl, __fadd_rn(e, pl));
+  sh = s;
+}
+__device__ __forceinline__ void df_add(float &sh, float &sl, float oh, float ol) {
+  float s = __fadd_rn(sh, oh);
+  float v = __fsub_rn(s, sh);
+  float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, v)), __fsub_rn(oh, v));
+  sl = __fadd_rn(__fadd_rn(sl, ol), e);
+  sh = s;
+}
+template <int VW>
+__device__ __forceinline__ void df_ldg(const float2 *p, float (&h)[VW], float (&l)[VW]) {
+  if constexpr (VW == 2) {
+    float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+    h[0] = t.x; l[0] = t.y; h[1] = t.z; l[1] = t.w;
+  } else {
+    float2 t = __ldg(p);
+    h[0] = t.x; l[0] = t.y;
+  }
+}
+
+template <int K, int VW, int E>
+__device__ __forceinline__ void df_row(const MatView<double> &A, const float2 *__restrict__ vdf,
+                                       const float2 *__restrict__ X, i64 k, i64 e, int ch,
+                                       float (&sh)[VW], float (&sl)[VW]) {
+  const i32 *__restrict__ ac = A.ci;
+  for (; k + 3 * E < e; k += 4 * E) {
+    float2 a0 = __ldg(vdf + k), a1 = __ldg(vdf + k + E), a2 = __ldg(vdf + k + 2 * E),
+           a3 = __ldg(vdf + k + 3 * E);
+    i32 j0 = __ldg(ac + k), j1 = __ldg(ac + k + E), j2 = __ldg(ac + k + 2 * E),
+        j3 = __ldg(ac + k + 3 * E);
+    float h0[VW], l0[VW], h1[VW], l1[VW], h2[VW], l2[VW], h3[VW], l3[VW];
+    df_ldg<VW>(X + (i64)j0 * K + ch * VW, h0, l0);
+    df_ldg<VW>(X + (i64)j1 * K + ch * VW, h1, l1);
+    df_ldg<VW>(X + (i64)j2 * K + ch * VW, h2, l2);
+    df_ldg<VW>(X + (i64)j3 * K + ch * VW, h3, l3);
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      df_fma(a0.x, a0.y, h0[q], l0[q], sh[q], sl[q]);
+      df_fma(a1.x, a1.y, h1[q], l1[q], sh[q], sl[q]);
+      df_fma(a2.x, a2.y, h2[q], l2[q], sh[q], sl[q]);
+      df_fma(a3.x, a3.y, h3[q], l3[q], sh[q], sl[q]);
+    }
+  }
+  for (; k < e; k += E) {
+    float2 a0 = __ldg(vdf + k);
+    i32 j0 = __ldg(ac + k);
+    float h0[VW], l0[VW];
+    df_ldg<VW>(X + (i64)j0 * K + ch * VW, h0, l0);
+#pragma unroll
+    for (int q = 0; q < VW; q++) df_fma(a0.x, a0.y, h0[q], l0[q], sh[q], sl[q]);
+  }
+}
+
+template <int VW, int L, int G>
+__device__ __forceinline__ void df_reduce_slots(float (&sh)[VW], float (&sl)[VW]) {
+#pragma unroll
+  for (int o = L; o < G; o <<= 1)
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      float oh = __shfl_xor_sync(0xffffffffu, sh[q], o);
+      float ol = __shfl_xor_sync(0xffffffffu, sl[q], o);
+      df_add(sh[q], sl[q], oh, ol);
+    }
+}
+
+template <int K, int G>
+__global__ void __launch_bounds__(256) k_spmm_df(const MatView<double> A,
+                                                 const float2 *__restrict__ vdf,
+                                                 const float2 *__restrict__ X, double *Y) {
+  constexpr int VW = (K % 2 == 0) ? 2 : 1;
+  constexpr int L = K / VW;
+  static_assert(L <= G && G <= 32 && (G % L) == 0, "bad layout");
+  constexpr int E = G / L;
+  constexpr int RPW = 32 / G;
+  const int lane = threadIdx.x & 31;
+  const int g = lane % G, slot = g / L, ch = g % L;
+  const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const i64 nregw = (A.n + RPW - 1) / RPW;
+  float sh[VW], sl[VW];
+#pragma unroll
+  for (int q = 0; q < VW; q++) sh[q] = sl[q] = 0.f;
+  if (warp < nregw) {
+    const i64 r = warp * RPW + lane / G;
+    bool act = r < A.n;
+    i64 b = 0, e = 0;
+    if (act) {
+      b = A.rp[r];
+      e = A.rp[r + 1];
+      if (A.hub_thresh > 0 && e - b > A.hub_thresh) act = false;
+    }
+    if (act) df_row<K, VW, E>(A, vdf, X, b + slot, e, ch, sh, sl);
+    df_reduce_slots<VW, L, G>(sh, sl);
+    if (act && slot == 0)
+#pragma unroll
+      for (int q = 0; q < VW; q++) Y[r * K + ch * VW + q] = (double)sh[q] + (double)sl[q];
+    return;
+  }
+  if constexpr (G == 32) {
+    const i64 c = warp - nregw;
+    if (c >= A.nchunks) return;
+    df_row<K, VW, E>(A, vdf, X, A.ch_beg[c] + slot, A.ch_end[c], ch, sh, sl);
+    df_reduce_slots<VW, L, G>(sh, sl);
+    double *part = A.partial;
+    if (slot == 0)
+#pragma unroll
+      for (int q = 0; q < VW; q++) part[c * K + ch * VW + q] = (double)sh[q] + (double)sl[q];
+    __threadfence();
+    __syncwarp();
+    int last = 0;
+    if (lane == 0) last = atomicAdd(&A.hub_counter[A.ch_hub[c]], 1) == A.ch_cnt[c] - 1;
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) return;
+    __threadfence();
+    const i64 first = A.ch_first[c];
+    const int cnt = A.ch_cnt[c];
+    double t[VW];
+#pragma unroll
+    for (int q = 0; q < VW; q++) t[q] = 0.0;
+    for (int u = slot; u < cnt; u += E)
+#pragma unroll
+      for (int q = 0; q < VW; q++) t[q] += __ldcg(part + (first + u) * K + ch * VW + q);
+#pragma unroll
+    for (int o = L; o < G; o <<= 1)
+#pragma unroll
+      for (int q = 0; q < VW; q++) t[q] += __shfl_xor_sync(0xffffffffu, t[q], o);
+    if (slot == 0)
+#pragma unroll
+      for (int q = 0; q < VW; q++) Y[A.ch_row[c] * K + ch * VW + q] = t[q];
+    if (lane == 0) A.hub_counter[A.ch_hub[c]] = 0;
+  }
+}
+
+template <int K, int G>
+void launch_df(const MatView<double> &A, const float2 *vdf, const float2 *X, double *Y,
+               cudaStream_t s) {
+  constexpr int RPW = 32 / G;
+  i64 warps = cdiv(A.n, RPW) + ((G == 32) ? A.nchunks : 0);
+  if (warps == 0) return;
+  k_spmm_df<K, G><<<grid_for(warps * 32, 256), 256, 0, s>>>(A, vdf, X, Y);
+  LG_LAUNCH();
+}
+
+__global__ void k_split_df(i64 cnt, const double *v, float2 *o) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cnt) return;
+  double x = v[t];
+  float h = (float)x;
+  o[t] = make_float2(h, (float)(x - (double)h));
+}
+
+int fused_blocks(i64 n, int k) {
+  i64 nb = cdiv(n * k, 256 * 8);
+  return (int)std::max<i64>(1, std::min<i64>(nb, 2 * kSMs));
+}
+
 }  // namespace
+
+i64 fused_scratch_len(i64 n, int k) { return 2 + (i64)fused_blocks(n, k) * 3 * k; }
+
+template <typename T>
+void fcg_beta(i64 n, int k, const T *z, const T *qp, FcgScalars sc, double *scratch,
+              cudaStream_t s) {
+  int nb = fused_blocks(n, k);
+  k_fused_red<T, 2><<<nb, 256, 0, s>>>(n, k, z, qp, nullptr, cdiv(n, nb), scratch, sc, nullptr);
+  LG_LAUNCH();
+}
+template <typename T>
+void fcg_dir(i64 n, int k, T *p, const T *z, const T *pp, FcgScalars sc, cudaStream_t s,
+             float2 *pdf) {
+  k_fcg_dir<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, p, z, pp, sc, pdf);
+  LG_LAUNCH();
+}
+
+void spmm_df(const MatView<double> &A, const float2 *vdf, const float2 *X, int k, double *Y,
+             cudaStream_t s) {
+  bool hub = A.nchunks > 0;
+  int g = hub ? 32 : A.lanes_per_row;
+  switch (k) {
+    case 1:
+      switch (g) {
+        case 4: return launch_df<1, 4>(A, vdf, X, Y, s);
+        case 8: return launch_df<1, 8>(A, vdf, X, Y, s);
+        case 16: return launch_df<1, 16>(A, vdf, X, Y, s);
+        default: return launch_df<1, 32>(A, vdf, X, Y, s);
+      }
+    case 2: return launch_df<2, 32>(A, vdf, X, Y, s);
+    case 4: return launch_df<4, 32>(A, vdf, X, Y, s);
+    case 8: return launch_df<8, 32>(A, vdf, X, Y, s);
+    case 16: return launch_df<16, 32>(A, vdf, X, Y, s);
+    case 32: return launch_df<32, 32>(A, vdf, X, Y, s);
+    case 64: return launch_df<64, 32>(A, vdf, X, Y, s);
+    default: throw Error(LIGMG_ERR_UNSUPPORTED, "k must be 1,2,4,8,16,32,64");
+  }
+}
+
+void split_df(i64 count, const double *v, float2 *out, cudaStream_t s) {
+  if (count <= 0) return;
+  k_split_df<<<grid_for(count, 256), 256, 0, s>>>(count, v, out);
+  LG_LAUNCH();
+}
+template <typename T>
+void fcg_alpha(i64 n, int k, const T *p, const T *q, const T *r, FcgScalars sc,
+               double *scratch, cudaStream_t s) {
+  int nb = fused_blocks(n, k);
+  k_fused_red<T, 3><<<nb, 256, 0, s>>>(n, k, p, q, r, cdiv(n, nb), scratch, sc, nullptr);
+  LG_LAUNCH();
+}
+template <typename T>
+void col_dot1(i64 n, int k, const T *x, const T *y, double *out, double *scratch, cudaStream_t s) {
+  int nb = fused_blocks(n, k);
+  FcgScalars none{};
+  k_fused_red<T, 1><<<nb, 256, 0, s>>>(n, k, x, y, nullptr, cdiv(n, nb), scratch, none, out);
+  LG_LAUNCH();
+}
 
 template <typename T>
 void cheb_init_zero(i64 n, int k, const T *b, const T *invd, double theta, T *d, cudaStream_t s) {
@@ -601,6 +926,12 @@ void scal_beta(int k, const double *zq, const double *eta_prev, double *beta, cu
 }
 
 #define LG_INST(T)                                                                             \
+  template void fcg_beta<T>(i64, int, const T *, const T *, FcgScalars, double *, cudaStream_t); \
+  template void fcg_dir<T>(i64, int, T *, const T *, const T *, FcgScalars, cudaStream_t,     \
+                           float2 *);                                                          \
+  template void fcg_alpha<T>(i64, int, const T *, const T *, const T *, FcgScalars, double *,  \
+                             cudaStream_t);                                                    \
+  template void col_dot1<T>(i64, int, const T *, const T *, double *, double *, cudaStream_t); \
   template void cheb_init_zero<T>(i64, int, const T *, const T *, double, T *, cudaStream_t); \
   template void restrict_agg<T>(i64, int, const i64 *, const i32 *, const T *, T *,          \
                                 cudaStream_t);                                                 \

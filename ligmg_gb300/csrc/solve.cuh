@@ -70,6 +70,16 @@ struct EpiArgs {
 template <typename T>
 void spmm(const MatView<T> &A, const T *X, int k, Epi epi, const EpiArgs &a, cudaStream_t s);
 
+// Double-float SpMM for the outer FP64 Krylov product y = A x.  GB300's FP64
+// rate makes a k-column FP64 SpMM compute-bound; here every FP64 value is held
+// as an unevaluated float pair (hi + lo, 48-bit significand) and products are
+// accumulated with error-free transformations (Dekker/Knuth TwoProd/TwoSum via
+// FMA) at FP32 throughput.  vdf: nnz (hi, lo) pairs of A's values; X: n x k
+// (hi, lo) pairs; Y: n x k doubles.  Hub rows use A's FP64 plan for k.
+void spmm_df(const MatView<double> &A, const float2 *vdf, const float2 *X, int k, double *Y,
+             cudaStream_t s);
+void split_df(i64 count, const double *v, float2 *out, cudaStream_t s);
+
 // elementwise / transfer kernels (n x k row-major)
 template <typename T>
 void cheb_init_zero(i64 n, int k, const T *b, const T *invd, double theta, T *d, cudaStream_t s);
@@ -107,6 +117,36 @@ void fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, const double *
                 bool update_r, cudaStream_t s);  // x += a p; r -= a q
 template <typename T>
 void cg_direction(i64 n, int k, T *p, const T *z, const double *beta, cudaStream_t s);  // p = z + beta p
+
+// Fused FCG steps with one-launch reductions.  A reduction writes one
+// partial per block into `scratch`; the last block to finish (ticket counter
+// at scratch[0], reset by that block) sums the partials in block order and
+// computes the step's scalars, so no second launch and no host round trip.
+struct FcgScalars {
+  double *mu;        // k: mean of z
+  double *beta;      // k
+  double *eta;       // k: p.(A p) of this iteration
+  double *eta_prev;  // k
+  double *alpha;     // k
+  const int *frozen; // k or null: alpha forced to 0
+};
+i64 fused_scratch_len(i64 n, int k);
+// mu = sum(z)/n; beta = (z.qp - mu sum(qp)) / eta_prev (beta = 0 if qp null)
+template <typename T>
+void fcg_beta(i64 n, int k, const T *z, const T *qp, FcgScalars sc, double *scratch,
+              cudaStream_t s);
+// p = (z - mu) - beta pp   (pp null: p = z - mu); pdf (optional, FP64 only):
+// the same p as (hi, lo) float pairs for spmm_df
+template <typename T>
+void fcg_dir(i64 n, int k, T *p, const T *z, const T *pp, FcgScalars sc, cudaStream_t s,
+             float2 *pdf = nullptr);
+// eta = p.q; alpha = (p.r)/eta (0 when frozen or eta == 0)
+template <typename T>
+void fcg_alpha(i64 n, int k, const T *p, const T *q, const T *r, FcgScalars sc,
+               double *scratch, cudaStream_t s);
+// out = sum(x.y) per column, one launch
+template <typename T>
+void col_dot1(i64 n, int k, const T *x, const T *y, double *out, double *scratch, cudaStream_t s);
 
 // scalar kernels on device (k columns)
 void scal_div(int k, const double *num, const double *den, double *out, const int *frozen,
