@@ -225,6 +225,22 @@ ligmg_status ligmg_get_stream(ligmg_handle h, void **stream);
 /* Kernels launched by this library in this process so far. */
 ligmg_status ligmg_launch_count(int64_t *count);
 
+/* Differentiation through the solve (no reference counterpart).
+ * ligmg_forward solves L x = b like ligmg_solve and keeps x on the device.
+ * ligmg_backward takes g = dloss/dx (host, length n), solves the adjoint
+ * system lambda = L^+ g with the same hierarchy (L is symmetric), and writes
+ *   dw[e] = -(x_i - x_j)(lambda_i - lambda_j)  for every stored off-diagonal
+ *           entry e = (i, j) of the input CSR (the derivative with respect to
+ *           the weight of edge {i, j}; both (i, j) and (j, i) carry it),
+ *           0 on diagonal entries;                                (length nnz)
+ *   db    = lambda with its mean removed                          (length n)
+ * from the kept forward solution (no second forward solve).  Either output
+ * may be null.  `info` (optional) describes the adjoint solve. */
+ligmg_status ligmg_forward(ligmg_handle h, const double *b, double *x,
+                           ligmg_info *info);
+ligmg_status ligmg_backward(ligmg_handle h, const double *g, double *dw,
+                            double *db, ligmg_info *info);
+
 /* y = A x with the level's FP64 matrix, device pointers, allocating nothing.
  * This entry point has no counterpart in the reference.  It exists for
  * callers that cannot allocate device memory at the point of the call: code

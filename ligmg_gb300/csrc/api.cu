@@ -103,6 +103,19 @@ __global__ void k_invdiag(const i64 *rp, const i32 *ci, const double *v, i64 n, 
   invd[i] = 1.0 / v[lo];
 }
 
+// dloss/dw_ij = -(x_i - x_j)(lambda_i - lambda_j) for each stored off-diagonal
+// entry; one warp per row
+__global__ void k_edge_grad(const i64 *rp, const i32 *ci, i64 n, const double *x,
+                            const double *lam, double *dw) {
+  i64 i = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= n) return;
+  double xi = x[i], li = lam[i];
+  for (i64 e = rp[i] + (threadIdx.x & 31); e < rp[i + 1]; e += 32) {
+    i32 j = ci[e];
+    dw[e] = (j == i) ? 0.0 : -(xi - x[j]) * (li - lam[j]);
+  }
+}
+
 __global__ void k_mul_diag(i64 n, const double *d, const double *x, double *y) {
   i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) y[i] = d[i] * x[i];
@@ -335,6 +348,8 @@ struct PrecGraph {
 
 struct ligmg_handle_s {
   std::map<std::tuple<int, int, int>, lg::PrecGraph> pgraphs;
+  lg::DBuf<double> fwd_x;  // forward solution kept for ligmg_backward
+  bool has_fwd = false;
   lg::Profiler prof;
   ligmg_options opts;
   int device = 0;
@@ -1041,6 +1056,11 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
     ;  // single coarse level: the pseudo-inverse is the preconditioner
   OuterWork &w = outer_work(H, k, nb, n0);
   LG_CUDA(cudaMemcpyAsync(w.Bfull.p, dB, sizeof(double) * n0 * k, cudaMemcpyDeviceToDevice, s));
+  // remove the constant from b first (the reference expects a mean-free b
+  // from its caller, main.cpp:138-139; R 1 is not constant)
+  col_reduce<double>(n0, k, Red::Sum, w.Bfull.p, nullptr, w.slot(S_SUM), w.scratch.p,
+                     w.scratch_len, s);
+  sub_mean<double>(n0, k, w.Bfull.p, w.slot(S_SUM), s);
   if (do_once) {
     EpiArgs a;
     a.y = w.B.p;
@@ -1063,9 +1083,7 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
   }
   LG_CUDA(cudaMemcpyAsync(dX, w.Xfull.p, sizeof(double) * n0 * k, cudaMemcpyDeviceToDevice, s));
   // true residual ||b - L x|| / ||b|| with b's constant projected out
-  double *sum = w.slot(S_SUM), *d1 = w.slot(S_ZQ), *d2 = w.slot(S_BETA);
-  col_reduce<double>(n0, k, Red::Sum, w.Bfull.p, nullptr, sum, w.scratch.p, w.scratch_len, s);
-  sub_mean<double>(n0, k, w.Bfull.p, sum, s);
+  double *d1 = w.slot(S_ZQ), *d2 = w.slot(S_BETA);
   EpiArgs a;
   a.y = w.Res.p;
   a.b = w.Bfull.p;
@@ -1267,6 +1285,55 @@ ligmg_status ligmg_solve_from(ligmg_handle h, const double *b, double *x, int32_
 ligmg_status ligmg_solve_batched(ligmg_handle h, const double *B, int32_t k, double *X,
                                  ligmg_info *info) {
   return solve_host(h, B, k, X, 0, info);
+}
+
+ligmg_status ligmg_forward(ligmg_handle h, const double *b, double *x, ligmg_info *info) {
+  if (!h || !b || !x) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    if (h->opts.precision == LIGMG_PREC_FP32) ensure_fp32(*h);
+    i64 n = h->h[0]->A.n;
+    DBuf<double> dB(n, h->s);
+    if (h->fwd_x.n != n) h->fwd_x.alloc(n, h->s);
+    dB.upload(b, n);
+    ligmg_status st = solve_device(*h, 1, 0, dB.p, h->fwd_x.p, info);
+    h->fwd_x.download(x, n);
+    LG_CUDA(cudaStreamSynchronize(h->s));
+    h->has_fwd = true;
+    return st;
+  });
+}
+
+ligmg_status ligmg_backward(ligmg_handle h, const double *g, double *dw, double *db,
+                            ligmg_info *info) {
+  if (!h || !g) return LIGMG_ERR_INVALID_ARGUMENT;
+  if (!h->has_fwd) return LIGMG_ERR_INVALID_ARGUMENT;  // no kept forward solution
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    const Level &L0 = *h->h[0];
+    i64 n = L0.A.n;
+    DBuf<double> dG(n, h->s), lam(n, h->s);
+    dG.upload(g, n);
+    // adjoint solve: L is symmetric, so lambda = L^+ g uses the same hierarchy
+    ligmg_status st = solve_device(*h, 1, 0, dG.p, lam.p, info);
+    // db = lambda with its mean removed (x depends on b only through its
+    // mean-free part)
+    OuterWork &w = *h->ow[1];
+    col_reduce<double>(n, 1, Red::Sum, lam.p, nullptr, w.slot(S_SUM), w.scratch.p,
+                       w.scratch_len, h->s);
+    sub_mean<double>(n, 1, lam.p, w.slot(S_SUM), h->s);
+    if (dw) {
+      DBuf<double> ddw(L0.A.nnz, h->s);
+      k_edge_grad<<<grid_for(n * 32, 256), 256, 0, h->s>>>(L0.A.rp.p, L0.A.ci.p, n,
+                                                           h->fwd_x.p, lam.p, ddw.p);
+      LG_LAUNCH();
+      ddw.download(dw, L0.A.nnz);
+      LG_CUDA(cudaStreamSynchronize(h->s));
+    }
+    if (db) lam.download(db, n);
+    LG_CUDA(cudaStreamSynchronize(h->s));
+    return st;
+  });
 }
 
 ligmg_status ligmg_hierarchy_levels(ligmg_handle h, int32_t *num_levels) {

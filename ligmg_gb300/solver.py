@@ -189,6 +189,29 @@ class Solver:
         check(lib().ligmg_spmv(self._h, level, _p(x), _p(y)), "ligmg_spmv")
         return y
 
+    # ---- differentiation -----------------------------------------------------
+    def forward(self, b) -> ConvergenceInfo:
+        """Solve L x = b and keep x for backward() (ligmg_forward)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.empty_like(b)
+        info, hist, ci, ct = self._info(1)
+        st = check(lib().ligmg_forward(self._h, _p(b), _p(x), C.byref(info)), "ligmg_forward")
+        return ConvergenceInfo(hist[: info.history_len].copy(), info.iters, info.solve_seconds,
+                               info.work, x, info.true_rel_residual, st == 0, ci, ct,
+                               info.cycle_complexity)
+
+    def backward(self, g):
+        """Adjoint of the kept forward solve (ligmg_backward): returns (dw, db)
+        with dw per stored CSR entry of the input matrix (the edge-weight
+        derivative on off-diagonal entries, 0 on the diagonal) and db = dloss/db."""
+        g = np.ascontiguousarray(g, dtype=np.float64)
+        dw = np.empty(len(self._ci))
+        db = np.empty(self.n)
+        info, hist, ci, ct = self._info(1)
+        check(lib().ligmg_backward(self._h, _p(g), _p(dw), _p(db), C.byref(info)),
+              "ligmg_backward")
+        return dw, db
+
     # ---- measurement ---------------------------------------------------------
     def profile(self, enable=True):
         check(lib().ligmg_profile_enable(self._h, 1 if enable else 0))

@@ -1201,6 +1201,10 @@ int orc_solve(orc_handle H, const double *b, double *x, int from, ligmg_info *in
   auto t0 = std::chrono::steady_clock::now();
   i64 n = h[from].A.n;
   std::vector<double> bv(b, b + n), rhs;
+  // the constant is removed from b before anything else: the reference leaves
+  // this to its caller (main.cpp:138-139), and R 1 is not constant, so
+  // projecting only the reduced right-hand side would change the answer
+  remove_mean(bv);
   bool do_once = H->opts.top_elim && h[from].type == LT::Elim;  // :322
   size_t base = from;
   if (do_once) {
@@ -1223,8 +1227,7 @@ int orc_solve(orc_handle H, const double *b, double *x, int from, ligmg_info *in
   std::copy(sol.begin(), sol.end(), x);
   if (info) {
     std::vector<double> r;
-    std::vector<double> bp = bv;
-    remove_mean(bp);
+    const std::vector<double> &bp = bv;
     residual(h[from].A, sol, bp, r);
     double bn = std::sqrt(dot(bp, bp));
     info->iters = iters;
