@@ -509,8 +509,22 @@ struct Engine {
     i64 n = L.A.n;
     MatView<T> A = viewA<T>(L, k, s);
     const T *invd = invdT<T>(L);
-    if (o().smoother_type == LIGMG_SMOOTHER_JACOBI)
-      throw Error(LIGMG_ERR_UNSUPPORTED, "jacobi smoother in the solve phase");
+    if (o().smoother_type == LIGMG_SMOOTHER_JACOBI) {
+      // create_smoother (smoothing.hpp:206-211): one weighted-Jacobi sweep
+      // (omega = 2/3) per smoother call, whatever the iteration count
+      const double omega = 2.0 / 3.0;
+      if (x_zero) {
+        cheb_init_zero<T>(n, k, b, invd, 1.0 / omega, x, s);
+        return;
+      }
+      EpiArgs a;
+      a.b = b; a.invd = invd; a.xin = x; a.y = w.xt.p; a.c1 = omega;
+      timed(H, (int)l, LIGMG_KERNEL_RESID, k, sizeof(T) == 8,
+            core_bytes(n, L.A.nnz, n, k, sizeof(T)) + (3.0 * n * k + n) * sizeof(T),
+            [&] { spmm<T>(A, x, k, Epi::Jacobi, a, s); });
+      LG_CUDA(cudaMemcpyAsync(x, w.xt.p, sizeof(T) * n * k, cudaMemcpyDeviceToDevice, s));
+      return;
+    }
     if (iters <= 0) return;
     const T *r_cur;
     const T *x_cur;
@@ -1226,9 +1240,9 @@ ligmg_status ligmg_create(int64_t n, const int64_t *rowptr, const int32_t *col,
     if (o.kcycle_iters < 1 || o.num_tvs < 0 || o.max_levels < 1 || o.iters < 0 ||
         (o.precision != LIGMG_PREC_FP64 && o.precision != LIGMG_PREC_FP32))
       return LIGMG_ERR_INVALID_ARGUMENT;
-    if (o.smoother_type != LIGMG_SMOOTHER_CHEBYSHEV || o.outer_ksp_type > LIGMG_KSP_FCG ||
+    if (o.smoother_type > LIGMG_SMOOTHER_CHEBYSHEV || o.outer_ksp_type > LIGMG_KSP_FCG ||
         o.kcycle_ksp_type != LIGMG_KSP_FCG || o.max_agg_size > 0 || o.rejection_ratio >= 0 ||
-        o.elim_iters > 1 || (o.aff_scaling != LIGMG_AFF_MAX && o.aff_scaling != LIGMG_AFF_NONE))
+        o.elim_iters > 1 || o.aff_scaling < LIGMG_AFF_NONE || o.aff_scaling > LIGMG_AFF_MAX)
       return LIGMG_ERR_UNSUPPORTED;
     H->device = o.device;
     LG_CUDA(cudaSetDevice(H->device));

@@ -359,11 +359,61 @@ __global__ void k_aff_values(const i64 *rp, const i32 *ci, const double *v, i64 
 
 __device__ __forceinline__ double dmax_ref(double a, double b) { return (a < b) ? b : a; }
 
+// Sequential per-row sums for the sum-based scalings (aggregation.hpp:352-367):
+// mode 0: row sums of a(i,.) (entry order = ascending column);
+// mode 1: column sums of a(.,i) = sums of the transposed values over row i;
+// mode 2: column sums of the row-scaled matrix, a(j,i) / rowsum[j].
+__global__ void k_aff_sums(const i64 *rp, const i32 *ci, i64 n, const double *aij,
+                           const double *aji, const double *rowsum, int mode, double *out) {
+  i64 i = warp_row();
+  if (i >= n) return;
+  unsigned lane = lane_id();
+  double acc = 0.0;
+  for (i64 base = rp[i]; base < rp[i + 1]; base += 32) {
+    i64 k = base + lane;
+    double v = 0.0;
+    bool in = k < rp[i + 1];
+    if (in) {
+      if (mode == 0) v = aij[k];
+      else if (mode == 1) v = aji[k];
+      else v = __ddiv_rn(aji[k], rowsum[ci[k]]);
+    }
+    unsigned m = __ballot_sync(0xffffffffu, in);
+    for (int q = 0; q < 32; q++) {
+      double t = __shfl_sync(0xffffffffu, v, q);
+      if (m & (1u << q)) acc = __dadd_rn(acc, t);
+    }
+  }
+  if (lane == 0) out[i] = acc;
+}
+
+struct AffScale {
+  int mode;
+  const double *row_max, *col_max;  // MAX
+  const double *rsum, *csum;        // ROW/SYM: rsum; COLUMN: csum; ROWCOLUMN: rsum + csum
+};
+
+// scaled value at (i, j) given the raw values a1 = a(i, j) and a2 = a(j, i)
+__device__ __forceinline__ double aff_scaled(const AffScale &S, i64 i, i32 j, double a1,
+                                             double a2) {
+  switch (S.mode) {
+    case LIGMG_AFF_MAX: return __ddiv_rn(a1, dmax_ref(S.row_max[i], S.col_max[j]));
+    case LIGMG_AFF_ROW: return __ddiv_rn(a1, S.rsum[i]);
+    case LIGMG_AFF_COLUMN: return __ddiv_rn(a1, S.csum[j]);
+    case LIGMG_AFF_ROWCOLUMN: return __ddiv_rn(__ddiv_rn(a1, S.rsum[i]), S.csum[j]);
+    case LIGMG_AFF_SYM: {  // (Aff^T + Aff) / 2 after row scaling (:361-367)
+      double r1 = __ddiv_rn(a1, S.rsum[i]), r2 = __ddiv_rn(a2, S.rsum[j]);
+      return __ddiv_rn(__dadd_rn(r2, r1), 2.0);
+    }
+    default: return a1;
+  }
+}
+
 // Max scaling + prune (:368-401), kept counts per row, and column sums
 // (:863-864) accumulated sequentially in ascending row order.
 __global__ void k_aff_scale(const i64 *rp, const i32 *ci, i64 n, const double *aij,
-                            const double *aji, const double *row_max, const double *col_max,
-                            int scaling, double thresh, i64 *kcnt, double *colsum) {
+                            const double *aji, AffScale S, double thresh, i64 *kcnt,
+                            double *colsum) {
   i64 i = warp_row();
   if (i >= n) return;
   unsigned lane = lane_id();
@@ -376,13 +426,8 @@ __global__ void k_aff_scale(const i64 *rp, const i32 *ci, i64 n, const double *a
     bool keep1 = false, keep2 = false;
     if (in) {
       i32 j = ci[k];
-      if (scaling == LIGMG_AFF_MAX) {
-        s1 = __ddiv_rn(aij[k], dmax_ref(row_max[i], col_max[j]));
-        s2 = __ddiv_rn(aji[k], dmax_ref(row_max[j], col_max[i]));
-      } else {
-        s1 = aij[k];
-        s2 = aji[k];
-      }
+      s1 = aff_scaled(S, i, j, aij[k], aji[k]);  // entry (i, j)
+      s2 = aff_scaled(S, j, (i32)i, aji[k], aij[k]);  // transposed entry (j, i)
       keep1 = !(s1 < thresh);
       keep2 = !(s2 < thresh);
     }
@@ -400,8 +445,8 @@ __global__ void k_aff_scale(const i64 *rp, const i32 *ci, i64 n, const double *a
 }
 
 __global__ void k_aff_fill(const i64 *rp, const i32 *ci, i64 n, const double *aij,
-                           const double *row_max, const double *col_max, int scaling,
-                           double thresh, const i64 *arp, i32 *aci, double *av) {
+                           const double *aji, AffScale S, double thresh, const i64 *arp,
+                           i32 *aci, double *av) {
   i64 i = warp_row();
   if (i >= n) return;
   unsigned lane = lane_id();
@@ -413,8 +458,7 @@ __global__ void k_aff_fill(const i64 *rp, const i32 *ci, i64 n, const double *ai
     i32 j = 0;
     if (k < rp[i + 1]) {
       j = ci[k];
-      s1 = (scaling == LIGMG_AFF_MAX) ? __ddiv_rn(aij[k], dmax_ref(row_max[i], col_max[j]))
-                                      : aij[k];
+      s1 = aff_scaled(S, i, j, aij[k], aji[k]);
       keep = !(s1 < thresh);
     }
     unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -792,8 +836,6 @@ void gpu_aggregation(const DCsr<double> &A, const AggParams &p, const double *tv
   int ntv = p.num_tvs;
   bool need_tvs = p.strength_metric == LIGMG_STRENGTH_AFFINITY ||
                   p.strength_metric == LIGMG_STRENGTH_ALGEBRAIC_DISTANCE;
-  if (p.aff_scaling != LIGMG_AFF_MAX && p.aff_scaling != LIGMG_AFF_NONE)
-    throw Error(LIGMG_ERR_UNSUPPORTED, "aff_scaling other than max/none");
   if (need_tvs && (ntv < 1 || ntv > 32)) throw Error(LIGMG_ERR_UNSUPPORTED, "num_tvs");
   DBuf<i64> dpos(n, s);
   k_diag_pos<<<grid_for(n, 256), 256, 0, s>>>(A.rp.p, A.ci.p, n, dpos.p);
@@ -823,12 +865,28 @@ void gpu_aggregation(const DCsr<double> &A, const AggParams &p, const double *tv
       A.rp.p, A.ci.p, A.v.p, n, ntv, out.tvs.p, sq.p, p.strength_metric, aij.p, aji.p, rmax.p,
       cmax.p);
   LG_LAUNCH();
+  AffScale S{p.aff_scaling, rmax.p, cmax.p, nullptr, nullptr};
+  DBuf<double> rsum, csum;
+  int sm = p.aff_scaling;
+  if (sm == LIGMG_AFF_ROW || sm == LIGMG_AFF_ROWCOLUMN || sm == LIGMG_AFF_SYM) {
+    rsum.alloc(n, s);
+    k_aff_sums<<<grid_for(n * 32, kBlock), kBlock, 0, s>>>(A.rp.p, A.ci.p, n, aij.p, aji.p,
+                                                           nullptr, 0, rsum.p);
+    LG_LAUNCH();
+    S.rsum = rsum.p;
+  }
+  if (sm == LIGMG_AFF_COLUMN || sm == LIGMG_AFF_ROWCOLUMN) {
+    csum.alloc(n, s);
+    k_aff_sums<<<grid_for(n * 32, kBlock), kBlock, 0, s>>>(
+        A.rp.p, A.ci.p, n, aij.p, aji.p, rsum.p, sm == LIGMG_AFF_ROWCOLUMN ? 2 : 1, csum.p);
+    LG_LAUNCH();
+    S.csum = csum.p;
+  }
   DBuf<i64> kcnt(n + 1, s);
   kcnt.zero();
   out.colsum.alloc(n, s);
-  k_aff_scale<<<grid_for(n * 32, kBlock), kBlock, 0, s>>>(A.rp.p, A.ci.p, n, aij.p, aji.p, rmax.p,
-                                                           cmax.p, p.aff_scaling, p.thresh,
-                                                           kcnt.p, out.colsum.p);
+  k_aff_scale<<<grid_for(n * 32, kBlock), kBlock, 0, s>>>(A.rp.p, A.ci.p, n, aij.p, aji.p, S,
+                                                           p.thresh, kcnt.p, out.colsum.p);
   LG_LAUNCH();
   DCsr<double> &F = out.aff;
   F.n = F.m = n;
@@ -838,9 +896,8 @@ void gpu_aggregation(const DCsr<double> &A, const AggParams &p, const double *tv
   F.nnz = read_scalar(atot.p, s);
   F.ci.alloc(F.nnz, s);
   F.v.alloc(F.nnz, s);
-  k_aff_fill<<<grid_for(n * 32, kBlock), kBlock, 0, s>>>(A.rp.p, A.ci.p, n, aij.p, rmax.p, cmax.p,
-                                                          p.aff_scaling, p.thresh, F.rp.p, F.ci.p,
-                                                          F.v.p);
+  k_aff_fill<<<grid_for(n * 32, kBlock), kBlock, 0, s>>>(A.rp.p, A.ci.p, n, aij.p, aji.p, S,
+                                                          p.thresh, F.rp.p, F.ci.p, F.v.p);
   LG_LAUNCH();
   aij.release();
   aji.release();

@@ -175,13 +175,21 @@ __device__ __forceinline__ void epilogue(const EpiArgs &a, i64 r, int c0, T (&ac
     if (a.rout) vstore<T, VW>((T *)a.rout + off, rr);
     if (a.dout) vstore<T, VW>((T *)a.dout + off, d);
     vstore<T, VW>((T *)a.xout + off, x);
-  } else {  // ElimInterp
+  } else if constexpr (E == Epi::ElimInterp) {
     T b[VW];
     vload<T, VW>((const T *)a.b + off, b);
     const T qd = ((const T *)a.q)[r];
 #pragma unroll
     for (int q = 0; q < VW; q++) b[q] = acc[q] + qd * b[q];
     vstore<T, VW>((T *)a.y + off, b);
+  } else {  // Jacobi: for a Laplacian, sum over negative entries = (A x)_i - a_ii x_i
+    T b[VW], x[VW];
+    vload<T, VW>((const T *)a.b + off, b);
+    vload<T, VW>((const T *)a.xin + off, x);
+    const T wi = (T)a.c1 * ((const T *)a.invd)[r];
+#pragma unroll
+    for (int q = 0; q < VW; q++) x[q] = x[q] + wi * (b[q] - acc[q]);
+    vstore<T, VW>((T *)a.y + off, x);
   }
 }
 
@@ -337,6 +345,7 @@ void spmm(const MatView<T> &A, const T *X, int k, Epi epi, const EpiArgs &a, cud
     case Epi::ChebA: return dispatch_k<T, Epi::ChebA>(A, X, k, a, s);
     case Epi::ChebB: return dispatch_k<T, Epi::ChebB>(A, X, k, a, s);
     case Epi::ElimInterp: return dispatch_k<T, Epi::ElimInterp>(A, X, k, a, s);
+    case Epi::Jacobi: return dispatch_k<T, Epi::Jacobi>(A, X, k, a, s);
   }
 }
 template void spmm<float>(const MatView<float> &, const float *, int, Epi, const EpiArgs &,

@@ -49,6 +49,7 @@ enum class Epi {
   ChebA,       // r = b - A x; d = invd r / theta; xo = x + d
   ChebB,       // r' = r - A d; d' = c1 d + c2 invd r'; xo = xi + d'
   ElimInterp,  // y = A x + q .* b   (A = P, x = xc)
+  Jacobi,      // y = xi + w invd (b - A x)   (weighted Jacobi sweep, w = c1)
 };
 
 struct EpiArgs {

@@ -523,7 +523,8 @@ Csr affinity_matrix(const Csr &A, const ligmg_options &o, GlibcRand &rng,
   }
   // scaling (:348-398)
   std::vector<double> sums(n);
-  if (o.aff_scaling == LIGMG_AFF_ROW || o.aff_scaling == LIGMG_AFF_ROWCOLUMN) {
+  if (o.aff_scaling == LIGMG_AFF_ROW || o.aff_scaling == LIGMG_AFF_ROWCOLUMN ||
+      o.aff_scaling == LIGMG_AFF_SYM) {
     for (i64 r = 0; r < n; r++) {
       double s = 0.0;
       for (i64 e = Aff.rp[r]; e < Aff.rp[r + 1]; e++) s += Aff.v[e];
@@ -538,6 +539,17 @@ Csr affinity_matrix(const Csr &A, const ligmg_options &o, GlibcRand &rng,
       for (i64 e = Aff.rp[r]; e < Aff.rp[r + 1]; e++) sums[Aff.ci[e]] += Aff.v[e];
     for (i64 r = 0; r < n; r++)
       for (i64 e = Aff.rp[r]; e < Aff.rp[r + 1]; e++) Aff.v[e] = Aff.v[e] / sums[Aff.ci[e]];
+  }
+  if (o.aff_scaling == LIGMG_AFF_SYM) {  // Aff = (Aff^T + Aff) / 2 (:361-367)
+    std::vector<double> sym(Aff.v.size());
+    for (i64 r = 0; r < n; r++)
+      for (i64 e = Aff.rp[r]; e < Aff.rp[r + 1]; e++) {
+        i64 c = Aff.ci[e];
+        auto b = Aff.ci.begin() + Aff.rp[c], en = Aff.ci.begin() + Aff.rp[c + 1];
+        i64 t = std::lower_bound(b, en, (i32)r) - Aff.ci.begin();  // symmetric pattern
+        sym[e] = (Aff.v[t] + Aff.v[e]) / 2;
+      }
+    Aff.v = sym;
   }
   if (o.aff_scaling == LIGMG_AFF_MAX) {
     std::vector<double> row_max(n, 0.0), col_max(n, 0.0);

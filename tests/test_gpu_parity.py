@@ -64,6 +64,19 @@ def test_setup_bit_exact(name):
             assert abs(S.level_lmax(l) - R.level_lmax(l)) <= 1e-12 * R.level_lmax(l)
 
 
+@pytest.mark.parametrize("opt", [dict(aff_scaling="row"), dict(aff_scaling="column"),
+                                 dict(aff_scaling="rowcolumn"), dict(aff_scaling="sym"),
+                                 dict(aff_scaling="none"), dict(strength_metric="none"),
+                                 dict(strength_metric="algebraic-distance")])
+def test_setup_options_bit_exact(opt):
+    L = GRAPHS["rmat12"]()
+    S, R = Solver(L, **opt), O.OracleSolver(L, **opt)
+    assert S.num_levels == R.num_levels
+    for l in range(R.num_levels - 1):
+        assert (S.level_ids(l) == R.level_ids(l)).all(), (opt, l)
+        assert (S.level_matrix(l)[2].view(np.int64) == R.level_matrix(l)[2].view(np.int64)).all()
+
+
 @pytest.mark.parametrize("kcycle", [0, 1])
 @pytest.mark.parametrize("name", ["grid48_logn", "my_matrix", "rmat12", "grid3d_12"])
 def test_cycle_fp64_matches_oracle(name, kcycle):
@@ -76,6 +89,19 @@ def test_cycle_fp64_matches_oracle(name, kcycle):
         b = _proj(rng.standard_normal(n))
         xg, xr = S.cycle(level, b), R.cycle(level, b)
         assert _relerr(xg, xr) <= 1e-12, (level, _relerr(xg, xr))
+
+
+@pytest.mark.parametrize("kcycle", [0, 1])
+def test_jacobi_smoother_matches_oracle(kcycle):
+    L = GRAPHS["grid48_logn"]()
+    kw = dict(smoother_type="jacobi", kcycle=kcycle, outer_ksp_type="fcg")
+    S, R = Solver(L, **kw), O.OracleSolver(L, **kw)
+    b = _proj(np.random.default_rng(2).standard_normal(L.n))
+    assert _relerr(S.cycle(0, b), R.cycle(0, b)) <= 1e-12
+    info = S.solve(G.rhs(L.n, seed=3))
+    xr, ir = R.solve(G.rhs(L.n, seed=3))
+    assert info.converged and abs(info.iters() - ir["iters"]) <= 1
+    assert _relerr(info.solution, xr) <= 1e-6
 
 
 @pytest.mark.parametrize("name", ["grid48_logn", "rmat12"])
