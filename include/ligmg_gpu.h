@@ -225,6 +225,25 @@ ligmg_status ligmg_get_stream(ligmg_handle h, void **stream);
 /* Kernels launched by this library in this process so far. */
 ligmg_status ligmg_launch_count(int64_t *count);
 
+/* A batch of independent graph Laplacians solved together (no reference
+ * counterpart; the reference solves one graph per Solver).  The graphs are
+ * given as one block-diagonal CSR matrix: graph g owns rows and columns
+ * [vertex_offsets[g], vertex_offsets[g+1]) and no entry may leave its block.
+ * One hierarchy is built for the union (no aggregate or elimination ever
+ * crosses graphs); every graph keeps its own Krylov scalars, its own
+ * null-space constant and its own convergence test, which runs on the GPU,
+ * so ligmg_batch_solve replays the whole solve of all graphs from one
+ * captured CUDA graph.  Requires outer_ksp_type = FCG.  b and x are the
+ * concatenated right-hand sides and solutions (length vertex_offsets[G]);
+ * iters and true_rel_residual (optional, length G) report per graph. */
+ligmg_status ligmg_batch_create(int32_t num_graphs, const int64_t *vertex_offsets,
+                                const int64_t *rowptr, const int32_t *col,
+                                const double *val, const ligmg_options *opts,
+                                ligmg_handle *out);
+ligmg_status ligmg_batch_solve(ligmg_handle h, const double *b, double *x,
+                               int32_t *iters, double *true_rel_residual,
+                               ligmg_info *info);
+
 /* Differentiation through the solve (no reference counterpart).
  * ligmg_forward solves L x = b like ligmg_solve and keeps x on the device.
  * ligmg_backward takes g = dloss/dx (host, length n), solves the adjoint

@@ -72,6 +72,8 @@ def lib(path=None):
     L.ligmg_launch_count.argtypes = [P(C.c_int64)]
     L.ligmg_spmv_device_noalloc.argtypes = [vp, C.c_int32, vp, vp]
     L.ligmg_forward.argtypes = [vp, vp, vp, P(Info)]
+    L.ligmg_batch_create.argtypes = [C.c_int32, vp, vp, vp, vp, P(Options), P(vp)]
+    L.ligmg_batch_solve.argtypes = [vp, vp, vp, vp, vp, P(Info)]
     L.ligmg_backward.argtypes = [vp, vp, vp, vp, P(Info)]
     for name in header_functions():
         if name not in ("ligmg_default_options", "ligmg_status_string"):

@@ -100,7 +100,8 @@ __global__ void k_invdiag(const i64 *rp, const i32 *ci, const double *v, i64 n, 
     i64 mid = (lo + hi) >> 1;
     if (ci[mid] < i) lo = mid + 1; else hi = mid;
   }
-  invd[i] = 1.0 / v[lo];
+  double d = v[lo];
+  invd[i] = d > 0 ? 1.0 / d : 0.0;  // a one-vertex component of a batch has d = 0
 }
 
 // dloss/dw_ij = -(x_i - x_j)(lambda_i - lambda_j) for each stored off-diagonal
@@ -114,6 +115,39 @@ __global__ void k_edge_grad(const i64 *rp, const i32 *ci, i64 n, const double *x
     i32 j = ci[e];
     dw[e] = (j == i) ? 0.0 : -(xi - x[j]) * (li - lam[j]);
   }
+}
+
+// segment offsets of the next level: the first new id inside each segment
+__global__ void k_gather_offsets(const i32 *scan, const i64 *seg_in, i64 nseg, i64 nc,
+                                 i64 *seg_out) {
+  i64 sg = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (sg > nseg) return;
+  seg_out[sg] = (sg == nseg) ? nc : (i64)scan[seg_in[sg]];
+}
+
+__global__ void k_fill_rowseg(const i64 *segptr, i64 nseg, i64 n, i32 *rowseg) {
+  i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  i64 lo = 0, hi = nseg - 1;  // largest sg with segptr[sg] <= r
+  while (lo < hi) {
+    i64 mid = (lo + hi + 1) >> 1;
+    if (segptr[mid] <= r) lo = mid; else hi = mid - 1;
+  }
+  rowseg[r] = (i32)lo;
+}
+
+// every row's columns must stay inside its segment (block-diagonal batch)
+__global__ void k_check_blockdiag(const i64 *rp, const i32 *ci, i64 n, const i32 *rowseg,
+                                  const i64 *segptr, int *bad) {
+  i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  i32 sg = rowseg[r];
+  i64 lo = segptr[sg], hi = segptr[sg + 1];
+  for (i64 e = rp[r]; e < rp[r + 1]; e++)
+    if (ci[e] < lo || ci[e] >= hi) {
+      *bad = 1;
+      return;
+    }
 }
 
 __global__ void k_mul_diag(i64 n, const double *d, const double *x, double *y) {
@@ -147,6 +181,18 @@ struct Level {
   // Chebyshev coefficients
   double theta = 1, delta = 1;
   std::vector<double> c1, c2;
+
+  // batch mode: rows of segment (graph) s are [seg_host[s], seg_host[s+1])
+  std::vector<i64> seg_host;
+  DBuf<i64> segptr;
+  DBuf<i32> rowseg;
+  SegInfo seginfo() const {
+    SegInfo S;
+    S.nseg = seg_host.empty() ? 0 : (i64)seg_host.size() - 1;
+    S.ptr = segptr.p;
+    S.rowseg = rowseg.p;
+    return S;
+  }
 
   bool is_exact() const { return type == LIGMG_LEVEL_ELIM; }
   i64 work(const ligmg_options &o) const {
@@ -251,8 +297,10 @@ struct LevelWork {
   DBuf<T> in, out, r, d0, d1, xt;           // cycle buffers
   DBuf<T> fz, fp0, fp1, fq0, fq1;           // K-cycle FCG buffers (fr = in, fx = out)
   DBuf<double> sc, scratch, fscratch;
-  i64 scratch_len = 0;
+  DBuf<double> segsc;  // batch mode: S_NSLOT x nseg scalars
+  i64 scratch_len = 0, nseg = 0;
   double *slot(int s, int k) { return sc.p + (i64)s * k * 2; }
+  double *sslot(int s) { return segsc.p + (i64)s * nseg; }
 };
 
 template <typename T>
@@ -261,7 +309,15 @@ struct Work {
   std::vector<LevelWork<T>> lw;
 };
 
+// batch-mode outer scalars (one per graph)
+struct SegOuter {
+  DBuf<double> sc, rn2, rn0sq;
+  DBuf<int> frozen, iters;
+  DBuf<float2> Pdf;
+};
+
 struct OuterWork {
+  SegOuter so;
   int k = 0;
   i64 n = 0;
   DBuf<double> X, R, Z, P0, P1, Q0, Q1, B, Bfull, Xfull, Res, sc, scratch, fscratch;
@@ -281,6 +337,7 @@ struct ProfRec {
 struct Profiler {
   bool on = false;
   bool capturing = false;
+  bool suspended = false;  // no records while capturing a whole batch solve
   std::vector<ProfRec> capture_tmpl;
   std::vector<cudaEvent_t> pool;
   std::vector<ProfRec> pending;
@@ -348,6 +405,10 @@ struct PrecGraph {
 
 struct ligmg_handle_s {
   std::map<std::tuple<int, int, int>, lg::PrecGraph> pgraphs;
+  // batch mode: vertex offsets of the graphs in the block-diagonal input
+  std::vector<lg::i64> seg0;
+  cudaGraphExec_t batch_first = nullptr, batch_more = nullptr;  // whole-solve graphs
+  size_t batch_base = 0;
   lg::DBuf<double> fwd_x;  // forward solution kept for ligmg_backward
   bool has_fwd = false;
   lg::Profiler prof;
@@ -366,6 +427,8 @@ struct ligmg_handle_s {
     if (s) cudaStreamSynchronize(s);
     for (auto &g : pgraphs) g.second.reset();
     pgraphs.clear();
+    if (batch_first) cudaGraphExecDestroy(batch_first);
+    if (batch_more) cudaGraphExecDestroy(batch_more);
     w32.clear();
     w64.clear();
     ow.clear();
@@ -386,7 +449,7 @@ using Handle = ligmg_handle_s;
 
 template <typename F>
 void timed(Handle &H, int level, int kind, int k, int fp64, double bytes, F &&f) {
-  if (!H.prof.on) {
+  if (!H.prof.on || H.prof.suspended) {
     f();
     return;
   }
@@ -488,6 +551,11 @@ Work<T> &work_for(Handle &H, int k) {
     w.scratch.alloc(w.scratch_len, s);
     w.fscratch.alloc(fused_scratch_len(n, k), s);
     w.fscratch.zero();  // reduction ticket starts at zero
+    w.nseg = L.seginfo().nseg;
+    if (w.nseg > 0) {
+      w.segsc.alloc((i64)S_NSLOT * w.nseg, s);
+      w.segsc.zero();
+    }
   }
   return W;
 }
@@ -638,19 +706,34 @@ struct Engine {
     LG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * n * k, s));
     T *r = b;
     T *p = w.fp0.p, *pp = w.fp1.p, *q = w.fq0.p, *qp = w.fq1.p;
+    const SegInfo S = L.seginfo();
+    const bool seg = S.nseg > 0;
     FcgScalars sc{w.slot(S_SUM, k), w.slot(S_BETA, k), w.slot(S_ETA0, k), w.slot(S_ETA1, k),
                   w.slot(S_ALPHA, k), nullptr};
+    if (seg)  // one set of Krylov scalars per graph of the batch
+      sc = FcgScalars{w.sslot(S_SUM), w.sslot(S_BETA), w.sslot(S_ETA0), w.sslot(S_ETA1),
+                      w.sslot(S_ALPHA), nullptr};
     for (int it = 0; it < iters; it++) {
       cycle(l, r, w.fz.p);
-      fcg_beta<T>(n, k, w.fz.p, it > 0 ? qp : nullptr, sc, w.fscratch.p, s);
-      fcg_dir<T>(n, k, p, w.fz.p, it > 0 ? pp : nullptr, sc, s);
+      if (seg) {
+        seg_fcg_beta<T>(S, w.fz.p, it > 0 ? qp : nullptr, sc, s);
+        seg_fcg_dir<T>(S, n, p, w.fz.p, it > 0 ? pp : nullptr, sc, s);
+      } else {
+        fcg_beta<T>(n, k, w.fz.p, it > 0 ? qp : nullptr, sc, w.fscratch.p, s);
+        fcg_dir<T>(n, k, p, w.fz.p, it > 0 ? pp : nullptr, sc, s);
+      }
       EpiArgs a;
       a.y = q;
       timed(H, (int)l, LIGMG_KERNEL_SPMV, k, sizeof(T) == 8,
             core_bytes(n, L.A.nnz, n, k, sizeof(T)) + 1.0 * n * k * sizeof(T),
             [&] { spmm<T>(A, p, k, Epi::Store, a, s); });
-      fcg_alpha<T>(n, k, p, q, r, sc, w.fscratch.p, s);
-      fcg_update<T>(n, k, x, r, p, q, sc.alpha, it + 1 < iters, s);
+      if (seg) {
+        seg_fcg_alpha<T>(S, p, q, r, sc, s);
+        seg_fcg_update<T>(S, n, x, r, p, q, sc.alpha, it + 1 < iters, s);
+      } else {
+        fcg_alpha<T>(n, k, p, q, r, sc, w.fscratch.p, s);
+        fcg_update<T>(n, k, x, r, p, q, sc.alpha, it + 1 < iters, s);
+      }
       std::swap(p, pp);
       std::swap(q, qp);
       std::swap(sc.eta, sc.eta_prev);
@@ -763,6 +846,37 @@ void make_hierarchy(Handle &H, i64 n, const i64 *rowptr, const i32 *col, const d
   ligmg_status st = gpu_validate(cur, s);
   if (st != LIGMG_OK) throw Error(st, "input validation");
   H.nnz0 = nnz;
+  // batch mode: segment offsets of the current matrix, carried level to level
+  const i64 nseg = H.seg0.empty() ? 0 : (i64)H.seg0.size() - 1;
+  std::vector<i64> cur_seg = H.seg0;
+  auto attach = [&](Level &L) {
+    if (!nseg) return;
+    L.seg_host = cur_seg;
+    L.segptr.alloc(nseg + 1, s);
+    L.segptr.upload(cur_seg.data(), nseg + 1);
+    L.rowseg.alloc(L.A.n, s);
+    k_fill_rowseg<<<grid_for(L.A.n, 256), 256, 0, s>>>(L.segptr.p, nseg, L.A.n, L.rowseg.p);
+    LG_LAUNCH();
+    LG_CUDA(cudaStreamSynchronize(s));
+  };
+  auto next_offsets = [&](const Level &L, const i32 *scan, i64 nc) {
+    if (!nseg) return;
+    DBuf<i64> out(nseg + 1, s);
+    k_gather_offsets<<<grid_for(nseg + 1, 128), 128, 0, s>>>(scan, L.segptr.p, nseg, nc, out.p);
+    LG_LAUNCH();
+    cur_seg = out.to_host();
+  };
+  if (nseg) {  // the input must be block-diagonal along the given offsets
+    DBuf<i64> sp(nseg + 1, s);
+    DBuf<i32> rs(n, s);
+    DBuf<int> bad(1, s);
+    bad.zero();
+    sp.upload(cur_seg.data(), nseg + 1);
+    k_fill_rowseg<<<grid_for(n, 256), 256, 0, s>>>(sp.p, nseg, n, rs.p);
+    k_check_blockdiag<<<grid_for(n, 256), 256, 0, s>>>(cur.rp.p, cur.ci.p, n, rs.p, sp.p, bad.p);
+    LG_LAUNCH();
+    if (read_scalar(bad.p, s)) throw Error(LIGMG_ERR_INVALID_ARGUMENT, "batch not block-diagonal");
+  }
   GlibcRand rng(o.seed);
   for (i64 i = 0; i < o.rng_skip; i++) rng.next();
   AggParams ap;
@@ -789,6 +903,8 @@ void make_hierarchy(Handle &H, i64 n, const i64 *rowptr, const i32 *col, const d
         E->A = std::move(cur);
         E->nc = E->elim.nc;
         finish_level(H, *E);
+        attach(*E);
+        next_offsets(*E, E->elim.pos.p, E->nc);
         h.push_back(std::move(E));
         cur = std::move(next);
       }
@@ -816,6 +932,8 @@ void make_hierarchy(Handle &H, i64 n, const i64 *rowptr, const i32 *col, const d
     gpu_galerkin_agg(cur, G->agg.agg.p, G->nc, next, s);
     G->A = std::move(cur);
     finish_level(H, *G);
+    attach(*G);
+    next_offsets(*G, G->agg.rank.p, G->nc);
     estimate_lmax(H, *G);
     setup_smoother_params(o, *G);
     h.push_back(std::move(G));
@@ -824,7 +942,9 @@ void make_hierarchy(Handle &H, i64 n, const i64 *rowptr, const i32 *col, const d
   auto C = std::make_unique<Level>();
   C->type = LIGMG_LEVEL_COARSE;
   C->A = std::move(cur);
-  st = gpu_coarse_pinv(C->A, C->pinv, s);
+  attach(*C);
+  st = gpu_coarse_pinv(C->A, C->pinv, s, nseg ? C->rowseg.p : nullptr,
+                       nseg ? C->segptr.p : nullptr);
   if (st != LIGMG_OK) throw Error(st, "coarse pseudo-inverse");
   finish_level(H, *C);
   h.push_back(std::move(C));
@@ -884,6 +1004,12 @@ void apply_prec_body(Handle &H, int k, size_t base, const double *r, double *z, 
     convert<double, float>(n * k, r, w.in.p, H.s);
     E.cycle(base, w.in.p, w.out.p);
     convert<float, double>(n * k, w.out.p, z, H.s);
+  }
+  const SegInfo S = L.seginfo();
+  if (S.nseg > 0) {  // one constant per graph of the batch
+    seg_sum<double>(S, z, sum, H.s);
+    seg_sub_mean<double>(S, n, z, sum, H.s);
+    return;
   }
   col_reduce<double>(n, k, Red::Sum, z, nullptr, sum, scratch, scratch_len, H.s);
   sub_mean<double>(n, k, z, sum, H.s);
@@ -1055,6 +1181,128 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
   return res;
 }
 
+// Batch mode outer FCG: every graph has its own Krylov scalars and its own
+// convergence test, evaluated on the device, so a whole solve needs no host
+// round trip.  kGraphIters iterations are captured into one CUDA graph (the
+// first from x0 = 0, later blocks continue); a batch that converges within
+// the first block is solved by one graph launch.
+constexpr int kGraphIters = 16;  // even: the continuation block repeats the buffer parity
+
+template <typename T>
+void seg_outer_iteration(Handle &H, size_t base, OuterWork &w, SegOuter &so, int it,
+                         bool dfprod) {
+  cudaStream_t s = H.s;
+  Level &L = *H.h[base];
+  i64 n = L.A.n, ns = L.seginfo().nseg;
+  SegInfo S = L.seginfo();
+  auto slot = [&](int q) { return so.sc.p + (i64)q * ns; };
+  bool odd = it & 1;
+  double *P = odd ? w.P1.p : w.P0.p, *PP = odd ? w.P0.p : w.P1.p;
+  double *Q = odd ? w.Q1.p : w.Q0.p, *QP = odd ? w.Q0.p : w.Q1.p;
+  double *eta = odd ? slot(S_ETA1) : slot(S_ETA0), *eta_prev = odd ? slot(S_ETA0) : slot(S_ETA1);
+  apply_prec_body<T>(H, 1, base, w.R.p, w.Z.p, slot(S_SUM), w.scratch.p, w.scratch_len);
+  FcgScalars sc{slot(S_ZQ), slot(S_BETA), eta, eta_prev, slot(S_ALPHA), so.frozen.p};
+  seg_fcg_beta<double>(S, w.Z.p, it > 0 ? QP : nullptr, sc, s);
+  seg_fcg_dir<double>(S, n, P, w.Z.p, it > 0 ? PP : nullptr, sc, s, dfprod ? so.Pdf.p : nullptr);
+  MatView<double> A = viewA<double>(L, 1, s);
+  EpiArgs a;
+  a.y = Q;
+  if (dfprod) spmm_df(A, L.Adf.p, so.Pdf.p, 1, Q, s);
+  else spmm<double>(A, P, 1, Epi::Store, a, s);
+  seg_fcg_alpha<double>(S, P, Q, w.R.p, sc, s);
+  seg_fcg_update<double>(S, n, w.X.p, w.R.p, P, Q, slot(S_ALPHA), true, s);
+  seg_dot<double>(S, w.R.p, w.R.p, so.rn2.p, s);
+  seg_converge(ns, so.rn2.p, so.rn0sq.p, H.opts.tol, it, so.frozen.p, so.iters.p, s);
+}
+
+template <typename T>
+SolveResult outer_solve_seg(Handle &H, size_t base, OuterWork &w) {
+  cudaStream_t s = H.s;
+  Level &L = *H.h[base];
+  i64 n = L.A.n;
+  const SegInfo S = L.seginfo();
+  i64 ns = S.nseg;
+  bool dfprod = sizeof(T) == 4;
+  if (dfprod && L.Adf.n != L.A.nnz) {
+    L.Adf.alloc(L.A.nnz, s);
+    split_df(L.A.nnz, L.A.v.p, L.Adf.p, s);
+  }
+  SegOuter &so = w.so;
+  if (so.frozen.n != ns || so.Pdf.n != n) {
+    so.sc.alloc((i64)S_NSLOT * ns, s);
+    so.sc.zero();
+    so.rn2.alloc(ns, s);
+    so.rn0sq.alloc(ns, s);
+    so.frozen.alloc(ns, s);
+    so.iters.alloc(ns, s);
+    so.Pdf.alloc(n, s);
+  }
+  // x0 = 0, r0 = b (b's constant per graph already removed by the caller)
+  LG_CUDA(cudaMemsetAsync(w.X.p, 0, sizeof(double) * n, s));
+  LG_CUDA(cudaMemcpyAsync(w.R.p, w.B.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  LG_CUDA(cudaMemsetAsync(so.frozen.p, 0, sizeof(int) * ns, s));
+  seg_dot<double>(S, w.R.p, w.R.p, so.rn0sq.p, s);
+  seg_converge(ns, so.rn0sq.p, so.rn0sq.p, 0.0, -1, so.frozen.p, so.iters.p, s);  // b = 0
+  // direct run of one cycle: creates every lazily built plan and buffer
+  apply_prec_body<T>(H, 1, base, w.R.p, w.Z.p, so.sc.p, w.scratch.p, w.scratch_len);
+  auto capture = [&](int it0) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t e = nullptr;
+    LG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    H.prof.suspended = true;
+    try {
+      for (int it = it0; it < it0 + kGraphIters; it++)
+        seg_outer_iteration<T>(H, base, w, so, it, dfprod);
+    } catch (...) {
+      H.prof.suspended = false;
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    H.prof.suspended = false;
+    LG_CUDA(cudaStreamEndCapture(s, &g));
+    cudaError_t err = cudaGraphInstantiate(&e, g, 0);
+    cudaGraphDestroy(g);
+    LG_CUDA(err);
+    return e;
+  };
+  if (!H.batch_first || H.batch_base != base) {
+    if (H.batch_first) cudaGraphExecDestroy(H.batch_first);
+    if (H.batch_more) cudaGraphExecDestroy(H.batch_more);
+    H.batch_first = capture(0);
+    H.batch_more = capture(kGraphIters);
+    H.batch_base = base;
+  }
+  SolveResult res;
+  std::vector<int> fz(ns), its(ns);
+  int done = 0;
+  for (int launch = 0; done < H.opts.iters; launch++) {
+    LG_CUDA(cudaGraphLaunch(launch == 0 ? H.batch_first : H.batch_more, s));
+    done += kGraphIters;
+    LG_CUDA(cudaMemcpyAsync(fz.data(), so.frozen.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, s));
+    LG_CUDA(cudaStreamSynchronize(s));
+    bool all = true;
+    for (int v : fz) all = all && v;
+    if (all) break;
+  }
+  std::vector<double> r2(ns), r0(ns);
+  LG_CUDA(cudaMemcpyAsync(its.data(), so.iters.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, s));
+  LG_CUDA(cudaMemcpyAsync(r2.data(), so.rn2.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
+  LG_CUDA(cudaMemcpyAsync(r0.data(), so.rn0sq.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
+  LG_CUDA(cudaStreamSynchronize(s));
+  res.converged = true;
+  res.col_iters = its;
+  res.rel.assign(ns, 0.0);
+  for (i64 g = 0; g < ns; g++) {
+    if (!std::isfinite(r2[g])) throw Error(LIGMG_ERR_BREAKDOWN, "non-finite residual");
+    res.converged = res.converged && fz[g];
+    res.iters = std::max(res.iters, its[g]);
+    res.rel[g] = r0[g] > 0 ? std::sqrt(r2[g] / r0[g]) : 0.0;
+  }
+  res.hist0 = {std::sqrt(r0[0]), std::sqrt(r2[0])};
+  return res;
+}
+
 // full solve: B (n0 x k) in w.Bfull -> w.Xfull; fills info
 ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *dX,
                           ligmg_info *info) {
@@ -1069,12 +1317,22 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
   if (H.h[base]->type == LIGMG_LEVEL_COARSE && H.h.size() == 1)
     ;  // single coarse level: the pseudo-inverse is the preconditioner
   OuterWork &w = outer_work(H, k, nb, n0);
+  const SegInfo SF = F.seginfo();
+  const bool seg = SF.nseg > 0;
+  if (seg && k != 1) throw Error(LIGMG_ERR_UNSUPPORTED, "batch mode solves one RHS per graph");
+  DBuf<double> segbuf;
+  if (seg) segbuf.alloc(2 * SF.nseg, s);
   LG_CUDA(cudaMemcpyAsync(w.Bfull.p, dB, sizeof(double) * n0 * k, cudaMemcpyDeviceToDevice, s));
   // remove the constant from b first (the reference expects a mean-free b
   // from its caller, main.cpp:138-139; R 1 is not constant)
-  col_reduce<double>(n0, k, Red::Sum, w.Bfull.p, nullptr, w.slot(S_SUM), w.scratch.p,
-                     w.scratch_len, s);
-  sub_mean<double>(n0, k, w.Bfull.p, w.slot(S_SUM), s);
+  if (seg) {
+    seg_sum<double>(SF, w.Bfull.p, segbuf.p, s);
+    seg_sub_mean<double>(SF, n0, w.Bfull.p, segbuf.p, s);
+  } else {
+    col_reduce<double>(n0, k, Red::Sum, w.Bfull.p, nullptr, w.slot(S_SUM), w.scratch.p,
+                       w.scratch_len, s);
+    sub_mean<double>(n0, k, w.Bfull.p, w.slot(S_SUM), s);
+  }
   if (do_once) {
     EpiArgs a;
     a.y = w.B.p;
@@ -1084,8 +1342,13 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
   } else {
     LG_CUDA(cudaMemcpyAsync(w.B.p, w.Bfull.p, sizeof(double) * n0 * k, cudaMemcpyDeviceToDevice, s));
   }
-  SolveResult res = (H.opts.precision == LIGMG_PREC_FP32) ? outer_solve<float>(H, base, w, k)
-                                                          : outer_solve<double>(H, base, w, k);
+  SolveResult res;
+  if (seg)
+    res = (H.opts.precision == LIGMG_PREC_FP32) ? outer_solve_seg<float>(H, base, w)
+                                                : outer_solve_seg<double>(H, base, w);
+  else
+    res = (H.opts.precision == LIGMG_PREC_FP32) ? outer_solve<float>(H, base, w, k)
+                                                : outer_solve<double>(H, base, w, k);
   if (do_once) {  // x = P x + Q b (:349-354)
     EpiArgs c;
     c.y = w.Xfull.p; c.b = w.Bfull.p; c.q = F.elim.Q.p;
@@ -1103,17 +1366,26 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
   a.b = w.Bfull.p;
   timed(H, from, LIGMG_KERNEL_RESID, k, 1, core_bytes(n0, F.A.nnz, n0, k, 8) + 16.0 * n0 * k,
         [&] { spmm<double>(viewA<double>(F, k, s), w.Xfull.p, k, Epi::Resid, a, s); });
-  col_reduce<double>(n0, k, Red::Dot, w.Res.p, w.Res.p, d1, w.scratch.p, w.scratch_len, s);
-  col_reduce<double>(n0, k, Red::Dot, w.Bfull.p, w.Bfull.p, d2, w.scratch.p, w.scratch_len, s);
-  std::vector<double> h1(k), h2(k);
-  LG_CUDA(cudaMemcpyAsync(h1.data(), d1, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
-  LG_CUDA(cudaMemcpyAsync(h2.data(), d2, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  int kc = seg ? (int)SF.nseg : k;  // reported columns: RHS columns or graphs
+  std::vector<double> h1(kc), h2(kc);
+  if (seg) {
+    seg_dot<double>(SF, w.Res.p, w.Res.p, segbuf.p, s);
+    seg_dot<double>(SF, w.Bfull.p, w.Bfull.p, segbuf.p + SF.nseg, s);
+    LG_CUDA(cudaMemcpyAsync(h1.data(), segbuf.p, sizeof(double) * kc, cudaMemcpyDeviceToHost, s));
+    LG_CUDA(cudaMemcpyAsync(h2.data(), segbuf.p + SF.nseg, sizeof(double) * kc,
+                            cudaMemcpyDeviceToHost, s));
+  } else {
+    col_reduce<double>(n0, k, Red::Dot, w.Res.p, w.Res.p, d1, w.scratch.p, w.scratch_len, s);
+    col_reduce<double>(n0, k, Red::Dot, w.Bfull.p, w.Bfull.p, d2, w.scratch.p, w.scratch_len, s);
+    LG_CUDA(cudaMemcpyAsync(h1.data(), d1, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+    LG_CUDA(cudaMemcpyAsync(h2.data(), d2, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  }
   LG_CUDA(cudaStreamSynchronize(s));
   double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   H.prof.collect();
   if (info) {
     double worst_true = 0, worst_rel = 0;
-    for (int c = 0; c < k; c++) {
+    for (int c = 0; c < kc; c++) {
       double tr = h2[c] > 0 ? std::sqrt(h1[c]) / std::sqrt(h2[c]) : 0.0;
       worst_true = std::max(worst_true, tr);
       worst_rel = std::max(worst_rel, res.rel[c]);
@@ -1345,6 +1617,57 @@ ligmg_status ligmg_backward(ligmg_handle h, const double *g, double *dw, double 
       LG_CUDA(cudaStreamSynchronize(h->s));
     }
     if (db) lam.download(db, n);
+    LG_CUDA(cudaStreamSynchronize(h->s));
+    return st;
+  });
+}
+
+ligmg_status ligmg_batch_create(int32_t num_graphs, const int64_t *vertex_offsets,
+                                const int64_t *rowptr, const int32_t *col, const double *val,
+                                const ligmg_options *opts, ligmg_handle *out) {
+  if (!out) return LIGMG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (num_graphs < 1 || !vertex_offsets || !rowptr || !col || !val)
+    return LIGMG_ERR_INVALID_ARGUMENT;
+  i64 n = vertex_offsets[num_graphs];
+  if (vertex_offsets[0] != 0 || n <= 0 || n >= INT32_MAX || rowptr[0] != 0)
+    return LIGMG_ERR_INVALID_ARGUMENT;
+  for (int32_t g = 0; g < num_graphs; g++)
+    if (vertex_offsets[g + 1] <= vertex_offsets[g]) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    std::unique_ptr<Handle> H(new Handle());
+    if (opts) H->opts = *opts; else ligmg_default_options(&H->opts);
+    const ligmg_options &o = H->opts;
+    if (o.outer_ksp_type != LIGMG_KSP_FCG || o.smoother_type > LIGMG_SMOOTHER_CHEBYSHEV ||
+        o.max_agg_size > 0 || o.rejection_ratio >= 0 || o.elim_iters > 1 ||
+        o.kcycle_ksp_type != LIGMG_KSP_FCG ||
+        (o.precision != LIGMG_PREC_FP64 && o.precision != LIGMG_PREC_FP32))
+      return LIGMG_ERR_UNSUPPORTED;
+    H->seg0.assign(vertex_offsets, vertex_offsets + num_graphs + 1);
+    H->device = o.device;
+    LG_CUDA(cudaSetDevice(H->device));
+    LG_CUDA(cudaStreamCreateWithFlags(&H->s, cudaStreamNonBlocking));
+    make_hierarchy(*H, n, rowptr, col, val);
+    *out = H.release();
+    return LIGMG_OK;
+  });
+}
+
+ligmg_status ligmg_batch_solve(ligmg_handle h, const double *b, double *x, int32_t *iters,
+                               double *true_rel_residual, ligmg_info *info) {
+  if (!h || !b || !x || h->seg0.empty()) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    if (h->opts.precision == LIGMG_PREC_FP32) ensure_fp32(*h);
+    i64 n = h->h[0]->A.n;
+    ligmg_info local{};
+    ligmg_info *inf = info ? info : &local;
+    inf->col_iters = iters;
+    inf->col_true_rel_residual = true_rel_residual;
+    DBuf<double> dB(n, h->s), dX(n, h->s);
+    dB.upload(b, n);
+    ligmg_status st = solve_device(*h, 1, 0, dB.p, dX.p, inf);
+    dX.download(x, n);
     LG_CUDA(cudaStreamSynchronize(h->s));
     return st;
   });

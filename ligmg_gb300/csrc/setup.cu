@@ -627,13 +627,21 @@ __global__ void k_u32_to_i32(const u32 *a, i64 n, i32 *b) {
 }
 
 // ---- coarse pseudo-inverse: Gauss-Jordan on M = A + 11'/n (SPD) -----------
+// value of the constant projector 11'/n_s at (r, k): 1/n_s within a segment
+__device__ __forceinline__ double proj_entry(i64 r, i64 k, i64 n, const i32 *rowseg,
+                                             const i64 *segptr) {
+  if (!rowseg) return 1.0 / (double)n;
+  i32 a = rowseg[r];
+  if (a != rowseg[k]) return 0.0;
+  return 1.0 / (double)(segptr[a + 1] - segptr[a]);
+}
+
 __global__ void k_dense_init(const i64 *rp, const i32 *ci, const double *v, i64 n, double *M,
-                             double *I) {
+                             double *I, const i32 *rowseg, const i64 *segptr) {
   i64 r = warp_row();
   if (r >= n) return;
-  double c = 1.0 / (double)n;
   for (i64 k = lane_id(); k < n; k += 32) {
-    M[r * n + k] = c;
+    M[r * n + k] = proj_entry(r, k, n, rowseg, segptr);
     I[r * n + k] = (k == r) ? 1.0 : 0.0;
   }
   __syncwarp();
@@ -674,9 +682,9 @@ __global__ void k_gj_factors(const double *M, i64 n, i64 p, double *fac) {
   if (r < n) fac[r] = M[r * n + p];
 }
 
-__global__ void k_sub_const(double *I, i64 nn, double c) {
-  i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < nn) I[k] -= c;
+__global__ void k_sub_proj(double *I, i64 n, const i32 *rowseg, const i64 *segptr) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n * n) I[t] -= proj_entry(t / n, t % n, n, rowseg, segptr);
 }
 
 }  // namespace
@@ -723,19 +731,21 @@ void gpu_elimination(const DCsr<double> &A, int elim_degree, double elim_factor,
                      ElimResult &out, cudaStream_t s) {
   i64 n = A.n;
   DBuf<uint8_t> cand(n, s);
-  DBuf<i32> keep(n, s), pos(n, s), tot(1, s);
+  DBuf<i32> keep(n, s), tot(1, s);
+  out.pos.alloc(n, s);
+  i32 *posp = out.pos.p;
   DBuf<i64> dpos(n, s);
   k_elim_cand<<<grid_for(n * 32, kBlock), kBlock, 0, s>>>(A.rp.p, A.v.p, n, elim_degree, cand.p);
   k_elim_select<<<grid_for(n, 256), 256, 0, s>>>(A.rp.p, A.ci.p, A.v.p, n, cand.p, keep.p);
   LG_LAUNCH();
-  exclusive_scan<i32>(keep.p, pos.p, n, s, tot.p);
+  exclusive_scan<i32>(keep.p, posp, n, s, tot.p);
   i64 num_no_elim = read_scalar(tot.p, s);
   out.accepted = !((double)num_no_elim > (double)n * elim_factor);  // :226
   if (!out.accepted) return;
   i64 nc = num_no_elim;
   out.nc = nc;
   out.new_id.alloc(n, s);
-  k_new_ids<<<grid_for(n, 256), 256, 0, s>>>(keep.p, pos.p, n, out.new_id.p);
+  k_new_ids<<<grid_for(n, 256), 256, 0, s>>>(keep.p, posp, n, out.new_id.p);
   k_diag_pos<<<grid_for(n, 256), 256, 0, s>>>(A.rp.p, A.ci.p, n, dpos.p);
   DBuf<i64> pcnt(n + 1, s);
   pcnt.zero();
@@ -945,7 +955,9 @@ void gpu_aggregation(const DCsr<double> &A, const AggParams &p, const double *tv
     if (p.max_agg_size > 0) throw Error(LIGMG_ERR_UNSUPPORTED, "max_agg_size > 0");
   }
   // aggregate ids: rank of the root among roots (remove_zero_rows)
-  DBuf<i32> is_root(n, s), rank(n, s), ntot(1, s);
+  DBuf<i32> is_root(n, s), ntot(1, s);
+  out.rank.alloc(n, s);
+  DBuf<i32> &rank = out.rank;
   is_root.zero();
   k_root_flags<<<grid_for(n, 256), 256, 0, s>>>(n, out.ind.p, is_root.p);
   LG_LAUNCH();
@@ -969,7 +981,8 @@ void gpu_aggregation(const DCsr<double> &A, const AggParams &p, const double *tv
   exclusive_scan<i64>(mcnt.p, out.mrp.p, out.nc + 1, s);
 }
 
-ligmg_status gpu_coarse_pinv(const DCsr<double> &A, DBuf<double> &out, cudaStream_t s) {
+ligmg_status gpu_coarse_pinv(const DCsr<double> &A, DBuf<double> &out, cudaStream_t s,
+                             const i32 *rowseg, const i64 *segptr) {
   i64 n = A.n;
   // dense n x n factor; the coarsening loop stops near nnz <= min_size, so a
   // coarse level this large means min_size was set far outside its range
@@ -978,7 +991,8 @@ ligmg_status gpu_coarse_pinv(const DCsr<double> &A, DBuf<double> &out, cudaStrea
   out.alloc(n * n, s);
   DBuf<int> bad(1, s);
   bad.zero();
-  k_dense_init<<<grid_for(n * 32, kBlock), kBlock, 0, s>>>(A.rp.p, A.ci.p, A.v.p, n, M.p, out.p);
+  k_dense_init<<<grid_for(n * 32, kBlock), kBlock, 0, s>>>(A.rp.p, A.ci.p, A.v.p, n, M.p, out.p,
+                                                            rowseg, segptr);
   LG_LAUNCH();
   unsigned gx = (unsigned)std::min<i64>(cdiv(n, 256), 64);
   for (i64 p = 0; p < n; p++) {
@@ -989,7 +1003,7 @@ ligmg_status gpu_coarse_pinv(const DCsr<double> &A, DBuf<double> &out, cudaStrea
     k_gj_eliminate<<<g, 256, 0, s>>>(M.p, out.p, n, p, fac.p);
   }
   LG_LAUNCH();
-  k_sub_const<<<grid_for(n * n, 256), 256, 0, s>>>(out.p, n * n, 1.0 / (double)n);
+  k_sub_proj<<<grid_for(n * n, 256), 256, 0, s>>>(out.p, n, rowseg, segptr);
   LG_LAUNCH();
   if (read_scalar(bad.p, s)) return LIGMG_ERR_DISCONNECTED;
   return LIGMG_OK;

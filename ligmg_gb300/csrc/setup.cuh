@@ -13,6 +13,7 @@ struct ElimResult {
   DCsr<double> P;     // n x nc
   DCsr<double> R;     // nc x n  (P^T, rows ascending in fine index)
   DBuf<double> Q;     // n, 1/A_jj on eliminated vertices, 0 elsewhere
+  DBuf<i32> pos;      // n, exclusive scan of the kept flags (new id of kept rows)
 };
 void gpu_elimination(const DCsr<double> &A, int elim_degree, double elim_factor,
                      ElimResult &out, cudaStream_t s);
@@ -26,6 +27,7 @@ struct AggResult {
   DBuf<i32> members;    // n fine vertices grouped by aggregate, ascending
   DBuf<double> colsum, votes, tvs;
   DBuf<i32> ind, st;    // final AggState
+  DBuf<i32> rank;       // n, number of aggregate roots with a smaller index
 };
 struct AggParams {
   int num_tvs, tvs_smooth, agg_iters, strength_metric, aff_scaling;
@@ -53,6 +55,9 @@ ligmg_status gpu_validate(const DCsr<double> &A, cudaStream_t s);
 
 // Dense pseudo-inverse of a connected Laplacian (coarse level):
 // out = (A + 11'/n)^-1 - 11'/n, row-major n x n.
-ligmg_status gpu_coarse_pinv(const DCsr<double> &A, DBuf<double> &out, cudaStream_t s);
+// With rowseg/segptr (batch of graphs stored block-diagonally) the constant
+// of every segment is handled separately.
+ligmg_status gpu_coarse_pinv(const DCsr<double> &A, DBuf<double> &out, cudaStream_t s,
+                             const i32 *rowseg = nullptr, const i64 *segptr = nullptr);
 
 }  // namespace lg

@@ -781,6 +781,166 @@ int fused_blocks(i64 n, int k) {
 
 }  // namespace
 
+// ---- segment-mode kernels ---------------------------------------------------
+namespace {
+// OP 0: sum x; 1: x.y; 2: beta step (sum z, z.qp, sum qp); 3: alpha (p.q, p.r)
+template <typename T, int OP>
+__global__ void __launch_bounds__(256)
+    k_seg_red(SegInfo S, const T *x, const T *y, const T *w, FcgScalars sc, double *out) {
+  constexpr int NV = (OP == 2) ? 3 : (OP == 3 ? 2 : 1);
+  __shared__ double sh[NV][256];
+  const i64 sg = blockIdx.x;
+  const i64 r0 = S.ptr[sg], r1 = S.ptr[sg + 1];
+  double a[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) a[v] = 0;
+  for (i64 r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    double xv = (double)x[r];
+    if constexpr (OP == 0) {
+      a[0] += xv;
+    } else if constexpr (OP == 1) {
+      a[0] += xv * (double)y[r];
+    } else if constexpr (OP == 2) {
+      a[0] += xv;
+      if (y) {
+        double yv = (double)y[r];
+        a[1] += xv * yv;
+        a[2] += yv;
+      }
+    } else {
+      a[0] += xv * (double)y[r];
+      a[1] += xv * (double)w[r];
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NV; v++) sh[v][threadIdx.x] = a[v];
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st)
+#pragma unroll
+      for (int v = 0; v < NV; v++) sh[v][threadIdx.x] += sh[v][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x) return;
+  if constexpr (OP == 0 || OP == 1) {
+    out[sg] = sh[0][0];
+  } else if constexpr (OP == 2) {
+    double mu = sh[0][0] / (double)(r1 - r0);
+    sc.mu[sg] = mu;
+    double e = sc.eta_prev[sg];
+    sc.beta[sg] = (y && e != 0.0) ? (sh[1][0] - mu * sh[2][0]) / e : 0.0;
+  } else {
+    double eta = sh[0][0];
+    sc.eta[sg] = eta;
+    bool fz = sc.frozen && sc.frozen[sg];
+    sc.alpha[sg] = (fz || eta == 0.0) ? 0.0 : sh[1][0] / eta;
+  }
+}
+
+template <typename T>
+__global__ void k_seg_sub_mean(SegInfo S, i64 n, T *x, const double *sums) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  i32 sg = S.rowseg[t];
+  double mu = sums[sg] / (double)(S.ptr[sg + 1] - S.ptr[sg]);
+  x[t] = (T)((double)x[t] - mu);
+}
+
+template <typename T>
+__global__ void k_seg_fcg_dir(SegInfo S, i64 n, T *p, const T *z, const T *pp, FcgScalars sc,
+                              float2 *pdf) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  i32 sg = S.rowseg[t];
+  T v = z[t] - (T)sc.mu[sg];
+  if (pp) v = v - (T)sc.beta[sg] * pp[t];
+  p[t] = v;
+  if (pdf) {
+    float h = (float)v;
+    pdf[t] = make_float2(h, (float)((double)v - (double)h));
+  }
+}
+
+template <typename T>
+__global__ void k_seg_fcg_update(SegInfo S, i64 n, T *x, T *r, const T *p, const T *q,
+                                 const double *alpha, int upd) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  T a = (T)alpha[S.rowseg[t]];
+  x[t] = x[t] + a * p[t];
+  if (upd) r[t] = r[t] - a * q[t];
+}
+
+__global__ void k_seg_converge(i64 nseg, const double *rn2, const double *rn0sq, double tol2,
+                               int it, int *frozen, int *iters) {
+  i64 sg = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (sg >= nseg || frozen[sg]) return;
+  iters[sg] = it + 1;
+  if (rn2[sg] <= tol2 * rn0sq[sg]) frozen[sg] = 1;  // a NaN norm never freezes
+}
+}  // namespace
+
+template <typename T>
+void seg_fcg_beta(const SegInfo &S, const T *z, const T *qp, FcgScalars sc, cudaStream_t s) {
+  k_seg_red<T, 2><<<(unsigned)S.nseg, 256, 0, s>>>(S, z, qp, nullptr, sc, nullptr);
+  LG_LAUNCH();
+}
+template <typename T>
+void seg_fcg_alpha(const SegInfo &S, const T *p, const T *q, const T *r, FcgScalars sc,
+                   cudaStream_t s) {
+  k_seg_red<T, 3><<<(unsigned)S.nseg, 256, 0, s>>>(S, p, q, r, sc, nullptr);
+  LG_LAUNCH();
+}
+template <typename T>
+void seg_dot(const SegInfo &S, const T *x, const T *y, double *out, cudaStream_t s) {
+  FcgScalars none{};
+  k_seg_red<T, 1><<<(unsigned)S.nseg, 256, 0, s>>>(S, x, y, nullptr, none, out);
+  LG_LAUNCH();
+}
+template <typename T>
+void seg_sum(const SegInfo &S, const T *x, double *out, cudaStream_t s) {
+  FcgScalars none{};
+  k_seg_red<T, 0><<<(unsigned)S.nseg, 256, 0, s>>>(S, x, nullptr, nullptr, none, out);
+  LG_LAUNCH();
+}
+template <typename T>
+void seg_sub_mean(const SegInfo &S, i64 n, T *x, const double *sums, cudaStream_t s) {
+  k_seg_sub_mean<T><<<grid_for(n, 256), 256, 0, s>>>(S, n, x, sums);
+  LG_LAUNCH();
+}
+template <typename T>
+void seg_fcg_dir(const SegInfo &S, i64 n, T *p, const T *z, const T *pp, FcgScalars sc,
+                 cudaStream_t s, float2 *pdf) {
+  k_seg_fcg_dir<T><<<grid_for(n, 256), 256, 0, s>>>(S, n, p, z, pp, sc, pdf);
+  LG_LAUNCH();
+}
+template <typename T>
+void seg_fcg_update(const SegInfo &S, i64 n, T *x, T *r, const T *p, const T *q,
+                    const double *alpha, bool update_r, cudaStream_t s) {
+  k_seg_fcg_update<T><<<grid_for(n, 256), 256, 0, s>>>(S, n, x, r, p, q, alpha, update_r ? 1 : 0);
+  LG_LAUNCH();
+}
+void seg_converge(i64 nseg, const double *rn2, const double *rn0sq, double tol, int it,
+                  int *frozen, int *iters, cudaStream_t s) {
+  k_seg_converge<<<grid_for(nseg, 128), 128, 0, s>>>(nseg, rn2, rn0sq, tol * tol, it, frozen,
+                                                      iters);
+  LG_LAUNCH();
+}
+#define LG_SEG_INST(T)                                                                      \
+  template void seg_fcg_beta<T>(const SegInfo &, const T *, const T *, FcgScalars,          \
+                                cudaStream_t);                                              \
+  template void seg_fcg_alpha<T>(const SegInfo &, const T *, const T *, const T *,          \
+                                 FcgScalars, cudaStream_t);                                 \
+  template void seg_dot<T>(const SegInfo &, const T *, const T *, double *, cudaStream_t);  \
+  template void seg_sum<T>(const SegInfo &, const T *, double *, cudaStream_t);             \
+  template void seg_sub_mean<T>(const SegInfo &, i64, T *, const double *, cudaStream_t);   \
+  template void seg_fcg_dir<T>(const SegInfo &, i64, T *, const T *, const T *, FcgScalars, \
+                               cudaStream_t, float2 *);                                     \
+  template void seg_fcg_update<T>(const SegInfo &, i64, T *, T *, const T *, const T *,     \
+                                  const double *, bool, cudaStream_t);
+LG_SEG_INST(float)
+LG_SEG_INST(double)
+
 i64 fused_scratch_len(i64 n, int k) { return 2 + (i64)fused_blocks(n, k) * 3 * k; }
 
 template <typename T>

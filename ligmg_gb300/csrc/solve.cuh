@@ -149,6 +149,38 @@ void fcg_alpha(i64 n, int k, const T *p, const T *q, const T *r, FcgScalars sc,
 template <typename T>
 void col_dot1(i64 n, int k, const T *x, const T *y, double *out, double *scratch, cudaStream_t s);
 
+// ---- segment mode (a batch of graphs stored as one block-diagonal matrix) --
+// Rows of segment s are [ptr[s], ptr[s+1]); every level keeps segments
+// contiguous.  Krylov scalars are per segment (one right-hand side column).
+struct SegInfo {
+  i64 nseg = 0;
+  const i64 *ptr = nullptr;    // nseg + 1 row offsets
+  const i32 *rowseg = nullptr; // segment id of every row
+};
+// One block per segment; the block also computes the step's scalars.
+template <typename T>
+void seg_fcg_beta(const SegInfo &S, const T *z, const T *qp, FcgScalars sc, cudaStream_t s);
+template <typename T>
+void seg_fcg_alpha(const SegInfo &S, const T *p, const T *q, const T *r, FcgScalars sc,
+                   cudaStream_t s);
+template <typename T>
+void seg_dot(const SegInfo &S, const T *x, const T *y, double *out, cudaStream_t s);
+template <typename T>
+void seg_sum(const SegInfo &S, const T *x, double *out, cudaStream_t s);
+// elementwise with per-row scalar lookup scalar[rowseg[i]]
+template <typename T>
+void seg_sub_mean(const SegInfo &S, i64 n, T *x, const double *sums, cudaStream_t s);
+template <typename T>
+void seg_fcg_dir(const SegInfo &S, i64 n, T *p, const T *z, const T *pp, FcgScalars sc,
+                 cudaStream_t s, float2 *pdf = nullptr);
+template <typename T>
+void seg_fcg_update(const SegInfo &S, i64 n, T *x, T *r, const T *p, const T *q,
+                    const double *alpha, bool update_r, cudaStream_t s);
+// device-side convergence: frozen[s] |= rn2[s] <= tol^2 rn0sq[s]; iters[s] set
+// to `it` + 1 for segments still active after this iteration
+void seg_converge(i64 nseg, const double *rn2, const double *rn0sq, double tol, int it,
+                  int *frozen, int *iters, cudaStream_t s);
+
 // scalar kernels on device (k columns)
 void scal_div(int k, const double *num, const double *den, double *out, const int *frozen,
               cudaStream_t s);  // out = frozen ? 0 : num/den (0 when den == 0)

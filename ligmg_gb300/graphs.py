@@ -153,6 +153,32 @@ def read_mtx(path, adjacency=False) -> Laplacian:
                      A.data.astype(np.float64), str(path))
 
 
+def union(graphs):
+    """Block-diagonal union of Laplacians: (vertex_offsets, Laplacian)."""
+    offs = np.zeros(len(graphs) + 1, dtype=np.int64)
+    for g, L in enumerate(graphs):
+        offs[g + 1] = offs[g] + L.n
+    rp = [np.zeros(1, dtype=np.int64)]
+    base = 0
+    for g, L in enumerate(graphs):
+        rp.append(L.rowptr[1:] + base)
+        base += L.nnz
+    col = np.concatenate([L.col.astype(np.int64) + offs[g] for g, L in enumerate(graphs)])
+    val = np.concatenate([L.val for L in graphs])
+    U = Laplacian(int(offs[-1]), np.concatenate(rp), col.astype(np.int32), val,
+                  f"union{len(graphs)}")
+    return offs, U
+
+
+def rgg_batch(count=256, nmin=10_000, nmax=200_000, seed=0):
+    """The uneven batch workload: `count` random geometric graphs with vertex
+    counts log-uniform in [nmin, nmax], mean degree ~12, weights
+    clip(1/dist, 0.1, 10), largest component each."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(nmin), np.log(nmax), count)).astype(np.int64)
+    return [rgg(int(n), seed=seed + 1 + g) for g, n in enumerate(sizes)]
+
+
 def rhs(n, k=1, seed=0) -> np.ndarray:
     """Zero-mean N(0,1) right-hand side(s); k > 1 gives an n x k row-major block."""
     rng = np.random.default_rng(seed + 12345)

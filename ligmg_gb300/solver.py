@@ -252,3 +252,61 @@ class Solver:
         f.write("graph,solver,iters,rel_error,cycle_complexity,wda,setup_time,solve_time,nnz,nodes\n")
         f.write(f"{graph},ligmg,{info.iters()},{info.rel_residual()},{info.cycle_complexity()},"
                 f"{info.wda()},{setup_time},{info.time()},{nnz},1\n")
+
+
+class BatchSolver:
+    """A batch of independent graph Laplacians solved together
+    (ligmg_batch_create / ligmg_batch_solve): one block-diagonal hierarchy,
+    per-graph Krylov scalars and convergence, the whole solve replayed from
+    one captured CUDA graph."""
+
+    def __init__(self, graphs, options: _abi.Options = None, **kw):
+        from .graphs import union
+        kw.setdefault("outer_ksp_type", "fcg")
+        self.graphs = list(graphs)
+        self.offsets, self.union = union(self.graphs)
+        U = self.union
+        self.options = options if options is not None else _abi.default_options(**kw)
+        h = C.c_void_p()
+        self._keep = (self.offsets, U.rowptr, U.col, U.val)
+        check(lib().ligmg_batch_create(len(self.graphs), _p(self.offsets), _p(U.rowptr),
+                                       _p(U.col), _p(U.val), C.byref(self.options),
+                                       C.byref(h)), "ligmg_batch_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ligmg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_levels(self):
+        x = C.c_int32()
+        check(lib().ligmg_hierarchy_levels(self._h, C.byref(x)))
+        return x.value
+
+    def solve(self, bs):
+        """bs: one right-hand side per graph (list) or the concatenated vector.
+        Returns (list of solutions, ConvergenceInfo with per-graph arrays)."""
+        G = len(self.graphs)
+        b = np.ascontiguousarray(np.concatenate(bs) if isinstance(bs, (list, tuple)) else bs,
+                                 dtype=np.float64)
+        x = np.empty_like(b)
+        iters = np.zeros(G, np.int32)
+        tr = np.zeros(G)
+        info = _abi.Info()
+        hist = np.zeros(8)
+        info.residual_history = hist.ctypes.data_as(C.POINTER(C.c_double))
+        info.history_capacity = 8
+        st = check(lib().ligmg_batch_solve(self._h, _p(b), _p(x), _p(iters), _p(tr),
+                                           C.byref(info)), "ligmg_batch_solve")
+        xs = [x[self.offsets[g]:self.offsets[g + 1]].copy() for g in range(G)]
+        return xs, ConvergenceInfo(hist[: info.history_len].copy(), info.iters,
+                                   info.solve_seconds, info.work, x, info.true_rel_residual,
+                                   st == 0, iters, tr, info.cycle_complexity)
