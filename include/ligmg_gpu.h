@@ -184,6 +184,37 @@ ligmg_status ligmg_level_matrix(ligmg_handle h, int32_t level, int64_t *rowptr,
 /* Level ids (length n): aggregate id per vertex for an aggregation level,
  * coarse id (or -1 when eliminated) for an elimination level. */
 ligmg_status ligmg_level_ids(ligmg_handle h, int32_t level, int32_t *ids);
+/* Prolongation of a level (n x nc CSR; P(i, agg[i]) = 1 for aggregation,
+ * elimination.hpp:288-334 for elimination) and, for elimination levels, the
+ * Q diagonal (length n; null to skip).  Two-call protocol: call with null
+ * arrays to get *nnz.  Used by dump_hierarchy (ligmg.hpp:47-52). */
+ligmg_status ligmg_level_prolongation(ligmg_handle h, int32_t level,
+                                      int64_t *nnz, int64_t *rowptr,
+                                      int32_t *col, double *val, double *q);
+
+/* Build a handle from an existing hierarchy instead of running the setup:
+ * the reverse of dump_hierarchy (ligmg.hpp:47-52, multigrid.hpp:295-313).
+ * Every level gives its input matrix; aggregation levels give aggregate ids,
+ * elimination levels give P (n x nc) and the Q diagonal; the last level is
+ * the coarse level.  The handle estimates the Chebyshev bounds and forms the
+ * coarse pseudo-inverse itself.  Arrays are host arrays, copied. */
+typedef struct ligmg_level_desc {
+  int32_t type;            /* LIGMG_LEVEL_* */
+  int64_t n, nnz;          /* level matrix (CSR, same rules as ligmg_create) */
+  const int64_t *rowptr;
+  const int32_t *col;
+  const double *val;
+  int64_t nc;              /* size of the next level */
+  const int32_t *ids;      /* aggregation: aggregate id per vertex */
+  int64_t pnnz;            /* elimination: P (n x nc CSR) and Q diagonal */
+  const int64_t *prow;
+  const int32_t *pcol;
+  const double *pval;
+  const double *q;
+} ligmg_level_desc;
+ligmg_status ligmg_import_hierarchy(int32_t num_levels, const ligmg_level_desc *levels,
+                                    const ligmg_options *opts, ligmg_handle *out);
+
 /* Largest eigenvalue estimate of D^-1 A used by the level's Chebyshev smoother. */
 ligmg_status ligmg_level_lmax(ligmg_handle h, int32_t level, double *lmax);
 

@@ -168,3 +168,21 @@ class KernelStat(C.Structure):
         ("seconds", C.c_double),
         ("bytes", C.c_double),
     ]
+
+
+class LevelDesc(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32),
+        ("n", C.c_int64),
+        ("nnz", C.c_int64),
+        ("rowptr", C.c_void_p),
+        ("col", C.c_void_p),
+        ("val", C.c_void_p),
+        ("nc", C.c_int64),
+        ("ids", C.c_void_p),
+        ("pnnz", C.c_int64),
+        ("prow", C.c_void_p),
+        ("pcol", C.c_void_p),
+        ("pval", C.c_void_p),
+        ("q", C.c_void_p),
+    ]

@@ -8,7 +8,7 @@ import os
 import re
 
 from . import build as _build
-from ._abi import Info, KernelStat, Options
+from ._abi import Info, KernelStat, LevelDesc, Options
 
 HEADER = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "include", "ligmg_gpu.h")
 
@@ -72,6 +72,8 @@ def lib(path=None):
     L.ligmg_launch_count.argtypes = [P(C.c_int64)]
     L.ligmg_spmv_device_noalloc.argtypes = [vp, C.c_int32, vp, vp]
     L.ligmg_forward.argtypes = [vp, vp, vp, P(Info)]
+    L.ligmg_level_prolongation.argtypes = [vp, C.c_int32, P(C.c_int64), vp, vp, vp, vp]
+    L.ligmg_import_hierarchy.argtypes = [C.c_int32, P(LevelDesc), P(Options), P(vp)]
     L.ligmg_batch_create.argtypes = [C.c_int32, vp, vp, vp, vp, P(Options), P(vp)]
     L.ligmg_batch_solve.argtypes = [vp, vp, vp, vp, vp, P(Info)]
     L.ligmg_backward.argtypes = [vp, vp, vp, vp, P(Info)]

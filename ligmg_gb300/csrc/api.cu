@@ -1673,6 +1673,121 @@ ligmg_status ligmg_batch_solve(ligmg_handle h, const double *b, double *x, int32
   });
 }
 
+ligmg_status ligmg_level_prolongation(ligmg_handle h, int32_t level, int64_t *nnz,
+                                      int64_t *rowptr, int32_t *col, double *val, double *q) {
+  if (!h || !nnz || level < 0 || level >= (int)h->h.size()) return LIGMG_ERR_INVALID_ARGUMENT;
+  const Level &L = *h->h[level];
+  if (L.type == LIGMG_LEVEL_COARSE) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    i64 n = L.A.n;
+    if (L.type == LIGMG_LEVEL_AGG) {
+      *nnz = n;
+      if (rowptr)
+        for (i64 i = 0; i <= n; i++) rowptr[i] = i;
+      if (col) L.agg.agg.download(col, n);
+      if (val)
+        for (i64 i = 0; i < n; i++) val[i] = 1.0;
+      if (q)
+        for (i64 i = 0; i < n; i++) q[i] = 0.0;
+    } else {
+      *nnz = L.elim.P.nnz;
+      if (rowptr) L.elim.P.rp.download(rowptr, n + 1);
+      if (col) L.elim.P.ci.download(col, L.elim.P.nnz);
+      if (val) L.elim.P.v.download(val, L.elim.P.nnz);
+      if (q) L.elim.Q.download(q, n);
+    }
+    LG_CUDA(cudaStreamSynchronize(h->s));
+    return LIGMG_OK;
+  });
+}
+
+ligmg_status ligmg_import_hierarchy(int32_t num_levels, const ligmg_level_desc *levels,
+                                    const ligmg_options *opts, ligmg_handle *out) {
+  if (!out) return LIGMG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (num_levels < 1 || !levels) return LIGMG_ERR_INVALID_ARGUMENT;
+  for (int32_t l = 0; l < num_levels; l++) {
+    const ligmg_level_desc &d = levels[l];
+    bool last = l == num_levels - 1;
+    if (d.n <= 0 || !d.rowptr || !d.col || !d.val || d.rowptr[d.n] != d.nnz)
+      return LIGMG_ERR_INVALID_ARGUMENT;
+    if (last != (d.type == LIGMG_LEVEL_COARSE)) return LIGMG_ERR_INVALID_ARGUMENT;
+    if (d.type == LIGMG_LEVEL_AGG && (!d.ids || d.nc <= 0)) return LIGMG_ERR_INVALID_ARGUMENT;
+    if (d.type == LIGMG_LEVEL_ELIM && (!d.prow || !d.pcol || !d.pval || !d.q || d.nc <= 0))
+      return LIGMG_ERR_INVALID_ARGUMENT;
+    if (!last && levels[l + 1].n != d.nc) return LIGMG_ERR_INVALID_ARGUMENT;
+  }
+  return guard([&]() -> ligmg_status {
+    std::unique_ptr<Handle> H(new Handle());
+    if (opts) H->opts = *opts; else ligmg_default_options(&H->opts);
+    H->device = H->opts.device;
+    LG_CUDA(cudaSetDevice(H->device));
+    LG_CUDA(cudaStreamCreateWithFlags(&H->s, cudaStreamNonBlocking));
+    cudaStream_t s = H->s;
+    auto t0 = std::chrono::steady_clock::now();
+    H->nnz0 = levels[0].nnz;
+    for (int32_t l = 0; l < num_levels; l++) {
+      const ligmg_level_desc &d = levels[l];
+      auto L = std::make_unique<Level>();
+      L->type = d.type;
+      L->A.n = L->A.m = d.n;
+      L->A.nnz = d.nnz;
+      L->A.rp.alloc(d.n + 1, s);
+      L->A.ci.alloc(d.nnz, s);
+      L->A.v.alloc(d.nnz, s);
+      L->A.rp.upload(d.rowptr, d.n + 1);
+      L->A.ci.upload(d.col, d.nnz);
+      L->A.v.upload(d.val, d.nnz);
+      if (l == 0) {
+        ligmg_status st = gpu_validate(L->A, s);
+        if (st != LIGMG_OK) return st;
+      }
+      L->nc = d.type == LIGMG_LEVEL_COARSE ? 0 : d.nc;
+      if (d.type == LIGMG_LEVEL_AGG) {
+        L->agg.nc = d.nc;
+        L->agg.agg.alloc(d.n, s);
+        L->agg.agg.upload(d.ids, d.n);
+        gpu_members(L->agg.agg.p, d.n, d.nc, L->agg.mrp, L->agg.members, s);
+      } else if (d.type == LIGMG_LEVEL_ELIM) {
+        ElimResult &E = L->elim;
+        E.accepted = true;
+        E.nc = d.nc;
+        E.P.n = d.n;
+        E.P.m = d.nc;
+        E.P.nnz = d.pnnz;
+        E.P.rp.alloc(d.n + 1, s);
+        E.P.ci.alloc(d.pnnz, s);
+        E.P.v.alloc(d.pnnz, s);
+        E.P.rp.upload(d.prow, d.n + 1);
+        E.P.ci.upload(d.pcol, d.pnnz);
+        E.P.v.upload(d.pval, d.pnnz);
+        E.Q.alloc(d.n, s);
+        E.Q.upload(d.q, d.n);
+        gpu_transpose(E.P, E.R, s);
+        std::vector<i32> nid(d.n, -1);  // coarse id of kept vertices (P entry 1 on a kept row)
+        for (i64 i = 0; i < d.n; i++)
+          if (d.q[i] == 0.0 && d.prow[i + 1] - d.prow[i] == 1) nid[i] = d.pcol[d.prow[i]];
+        E.new_id.alloc(d.n, s);
+        E.new_id.upload(nid.data(), d.n);
+      } else {
+        ligmg_status st = gpu_coarse_pinv(L->A, L->pinv, s);
+        if (st != LIGMG_OK) return st;
+      }
+      finish_level(*H, *L);
+      if (d.type == LIGMG_LEVEL_AGG) {
+        estimate_lmax(*H, *L);
+        setup_smoother_params(H->opts, *L);
+      }
+      LG_CUDA(cudaStreamSynchronize(s));
+      H->h.push_back(std::move(L));
+    }
+    H->setup_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    *out = H.release();
+    return LIGMG_OK;
+  });
+}
+
 ligmg_status ligmg_hierarchy_levels(ligmg_handle h, int32_t *num_levels) {
   if (!h || !num_levels) return LIGMG_ERR_INVALID_ARGUMENT;
   *num_levels = (int32_t)h->h.size();

@@ -966,19 +966,24 @@ void gpu_aggregation(const DCsr<double> &A, const AggParams &p, const double *tv
   out.agg.alloc(n, s);
   k_agg_ids<<<grid_for(n, 256), 256, 0, s>>>(n, out.ind.p, rank.p, out.agg.p);
   LG_LAUNCH();
+  gpu_members(out.agg.p, n, out.nc, out.mrp, out.members, s);
+}
+
+void gpu_members(const i32 *agg, i64 n, i64 nc, DBuf<i64> &mrp, DBuf<i32> &members,
+                 cudaStream_t s) {
   // members grouped by aggregate (R as CSR), ascending fine index
   DBuf<u64> mkeys(n, s);
   DBuf<u32> mvals(n, s);
-  DBuf<i64> mcnt(out.nc + 1, s);
+  DBuf<i64> mcnt(nc + 1, s);
   mcnt.zero();
-  k_agg_keys<<<grid_for(n, 256), 256, 0, s>>>(n, out.agg.p, mkeys.p, mvals.p, mcnt.p);
+  k_agg_keys<<<grid_for(n, 256), 256, 0, s>>>(n, agg, mkeys.p, mvals.p, mcnt.p);
   LG_LAUNCH();
-  radix_sort_pairs(mkeys.p, mvals.p, n, bits_for(out.nc - 1), s);
-  out.members.alloc(n, s);
-  k_u32_to_i32<<<grid_for(n, 256), 256, 0, s>>>(mvals.p, n, out.members.p);
+  radix_sort_pairs(mkeys.p, mvals.p, n, bits_for(nc - 1), s);
+  members.alloc(n, s);
+  k_u32_to_i32<<<grid_for(n, 256), 256, 0, s>>>(mvals.p, n, members.p);
   LG_LAUNCH();
-  out.mrp.alloc(out.nc + 1, s);
-  exclusive_scan<i64>(mcnt.p, out.mrp.p, out.nc + 1, s);
+  mrp.alloc(nc + 1, s);
+  exclusive_scan<i64>(mcnt.p, mrp.p, nc + 1, s);
 }
 
 ligmg_status gpu_coarse_pinv(const DCsr<double> &A, DBuf<double> &out, cudaStream_t s,

@@ -47,6 +47,11 @@ void gpu_galerkin(const DCsr<double> &A, const DCsr<double> &P, DCsr<double> &C,
 void gpu_galerkin_agg(const DCsr<double> &A, const i32 *agg, i64 nc, DCsr<double> &C,
                       cudaStream_t s);
 
+// Member CSR of an aggregation (R): fine vertices grouped by aggregate id,
+// ascending inside each aggregate.
+void gpu_members(const i32 *agg, i64 n, i64 nc, DBuf<i64> &mrp, DBuf<i32> &members,
+                 cudaStream_t s);
+
 // CSR transpose with rows of the result ascending (stable).
 void gpu_transpose(const DCsr<double> &A, DCsr<double> &T, cudaStream_t s);
 

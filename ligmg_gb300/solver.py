@@ -189,6 +189,76 @@ class Solver:
         check(lib().ligmg_spmv(self._h, level, _p(x), _p(y)), "ligmg_spmv")
         return y
 
+    # ---- hierarchy export / import --------------------------------------------
+    def level_prolongation(self, level):
+        inf = self.level_info(level)
+        nnz = C.c_int64()
+        check(lib().ligmg_level_prolongation(self._h, level, C.byref(nnz), None, None, None,
+                                             None))
+        rp = np.empty(inf["n"] + 1, np.int64)
+        ci = np.empty(nnz.value, np.int32)
+        v = np.empty(nnz.value, np.float64)
+        q = np.empty(inf["n"], np.float64)
+        check(lib().ligmg_level_prolongation(self._h, level, C.byref(nnz), _p(rp), _p(ci),
+                                             _p(v), _p(q)))
+        return rp, ci, v, q
+
+    def export_levels(self):
+        from .petsc_io import Level
+        out = []
+        for l in range(self.num_levels):
+            inf = self.level_info(l)
+            rp, ci, v = self.level_matrix(l)
+            lv = Level(inf["type"], inf["n"], rp, ci, v, inf["nc"])
+            if inf["type"] == "agg":
+                lv.ids = self.level_ids(l)
+            elif inf["type"] == "elim":
+                lv.prow, lv.pcol, lv.pval, lv.q = self.level_prolongation(l)
+            out.append(lv)
+        return out
+
+    def dump_hierarchy(self, directory):
+        """dump_hierarchy (ligmg.hpp:47-52): PETSc binary files per level."""
+        from .petsc_io import dump
+        dump(self.export_levels(), directory)
+
+    @classmethod
+    def import_hierarchy(cls, levels, options: _abi.Options = None, **kw):
+        """Handle over an existing hierarchy (list of petsc_io.Level, e.g. from
+        petsc_io.load(dir) or an exported hierarchy), without running setup."""
+        self = cls.__new__(cls)
+        self.options = options if options is not None else _abi.default_options(**kw)
+        types = {"elim": 0, "agg": 1, "coarse": 2}
+        descs = (_abi.LevelDesc * len(levels))()
+        keep = []
+        for d, lv in zip(descs, levels):
+            arrs = [np.ascontiguousarray(lv.rowptr, np.int64), np.ascontiguousarray(lv.col, np.int32),
+                    np.ascontiguousarray(lv.val, np.float64)]
+            keep.append(arrs)
+            d.type = types[lv.type]
+            d.n = lv.n
+            d.nnz = int(arrs[0][-1])
+            d.rowptr, d.col, d.val = (a.ctypes.data for a in arrs)
+            d.nc = lv.nc
+            if lv.type == "agg":
+                ids = np.ascontiguousarray(lv.ids, np.int32)
+                keep.append(ids)
+                d.ids = ids.ctypes.data
+            elif lv.type == "elim":
+                pa = [np.ascontiguousarray(lv.prow, np.int64), np.ascontiguousarray(lv.pcol, np.int32),
+                      np.ascontiguousarray(lv.pval, np.float64), np.ascontiguousarray(lv.q, np.float64)]
+                keep.append(pa)
+                d.prow, d.pcol, d.pval, d.q = (a.ctypes.data for a in pa)
+                d.pnnz = int(pa[0][-1])
+        h = C.c_void_p()
+        check(lib().ligmg_import_hierarchy(len(levels), descs, C.byref(self.options),
+                                           C.byref(h)), "ligmg_import_hierarchy")
+        self._h = h
+        L0 = levels[0]
+        self.n = L0.n
+        self._rp, self._ci, self._v = keep[0]
+        return self
+
     # ---- differentiation -----------------------------------------------------
     def forward(self, b) -> ConvergenceInfo:
         """Solve L x = b and keep x for backward() (ligmg_forward)."""

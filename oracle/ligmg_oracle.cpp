@@ -1160,6 +1160,21 @@ int orc_level_lmax(orc_handle h, int level, double *lmax) {
   return LIGMG_OK;
 }
 
+int orc_level_prolongation(orc_handle h, int level, int64_t *nnz, int64_t *rowptr,
+                           int32_t *col, double *val, double *q) {
+  if (level < 0 || level >= (int)h->h.size() || h->h[level].type == LT::Coarse) return LIGMG_ERR_INVALID_ARGUMENT;
+  const Level &L = h->h[level];
+  *nnz = L.P.nnz();
+  if (rowptr) std::copy(L.P.rp.begin(), L.P.rp.end(), rowptr);
+  if (col) std::copy(L.P.ci.begin(), L.P.ci.end(), col);
+  if (val) std::copy(L.P.v.begin(), L.P.v.end(), val);
+  if (q) {
+    if (L.type == LT::Elim) std::copy(L.Q.begin(), L.Q.end(), q);
+    else std::fill(q, q + L.A.n, 0.0);
+  }
+  return LIGMG_OK;
+}
+
 int orc_level_aff_nnz(orc_handle h, int level, int64_t *nnz) {
   if (level < 0 || level >= (int)h->h.size() || h->h[level].type != LT::Agg)
     return LIGMG_ERR_INVALID_ARGUMENT;

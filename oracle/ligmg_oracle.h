@@ -36,6 +36,10 @@ int orc_level_matrix(orc_handle h, int level, int64_t *rowptr, int32_t *col,
                      double *val);
 int orc_level_ids(orc_handle h, int level, int32_t *ids);
 int orc_level_lmax(orc_handle h, int level, double *lmax);
+/* prolongation (n x nc CSR) and Q diagonal of a non-coarse level; two-call
+ * protocol (null arrays: only *nnz) */
+int orc_level_prolongation(orc_handle h, int level, int64_t *nnz, int64_t *rowptr,
+                           int32_t *col, double *val, double *q);
 /* affinity matrix of an aggregation level: rowptr n+1, then col/val */
 int orc_level_aff_nnz(orc_handle h, int level, int64_t *nnz);
 int orc_level_aff(orc_handle h, int level, int64_t *rowptr, int32_t *col,

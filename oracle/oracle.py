@@ -39,6 +39,7 @@ def lib():
         L.orc_level_matrix.argtypes = [vp, C.c_int, vp, vp, vp]
         L.orc_level_ids.argtypes = [vp, C.c_int, vp]
         L.orc_level_lmax.argtypes = [vp, C.c_int, P(C.c_double)]
+        L.orc_level_prolongation.argtypes = [vp, C.c_int, P(C.c_int64), vp, vp, vp, vp]
         L.orc_level_aff_nnz.argtypes = [vp, C.c_int, P(C.c_int64)]
         L.orc_level_aff.argtypes = [vp, C.c_int, vp, vp, vp]
         L.orc_level_debug.argtypes = [vp, C.c_int, C.c_int, vp]
@@ -149,6 +150,32 @@ class OracleSolver:
         x = C.c_double()
         lib().orc_level_lmax(self.h, l, C.byref(x))
         return x.value
+
+    def level_prolongation(self, l):
+        inf = self.level_info(l)
+        nnz = C.c_int64()
+        lib().orc_level_prolongation(self.h, l, C.byref(nnz), None, None, None, None)
+        rp = np.empty(inf["n"] + 1, np.int64)
+        ci = np.empty(nnz.value, np.int32)
+        cv = np.empty(nnz.value, np.float64)
+        q = np.empty(inf["n"], np.float64)
+        lib().orc_level_prolongation(self.h, l, C.byref(nnz), _p(rp), _p(ci), _p(cv), _p(q))
+        return rp, ci, cv, q
+
+    def export_levels(self):
+        """Level descriptions (ligmg_gb300.petsc_io.Level) of this hierarchy."""
+        from ligmg_gb300.petsc_io import Level
+        out = []
+        for l in range(self.num_levels):
+            inf = self.level_info(l)
+            rp, ci, cv = self.level_matrix(l)
+            lv = Level(inf["type"], inf["n"], rp, ci, cv, inf["nc"])
+            if inf["type"] == "agg":
+                lv.ids = self.level_ids(l)
+            elif inf["type"] == "elim":
+                lv.prow, lv.pcol, lv.pval, lv.q = self.level_prolongation(l)
+            out.append(lv)
+        return out
 
     def level_aff(self, l):
         inf = self.level_info(l)

@@ -231,3 +231,35 @@ def test_unsupported_k_rejected():
     S = Solver(L)
     with pytest.raises(LigmgError):
         S.solve_batched(np.zeros((L.n, 3)))
+
+
+@pytest.mark.parametrize("name", ["my_matrix", "rmat12"])
+def test_cycle_on_imported_oracle_hierarchy(name, tmp_path):
+    """The spec check on an exported hierarchy: import the oracle's
+    hierarchy (written to PETSc binary and read back) and compare one FP64
+    cycle and a full solve with the oracle's."""
+    from ligmg_gb300 import petsc_io
+    L = GRAPHS[name]()
+    kw = dict(kcycle=1, outer_ksp_type="fcg")
+    R = O.OracleSolver(L, **kw)
+    petsc_io.dump(R.export_levels(), tmp_path)
+    S = Solver.import_hierarchy(petsc_io.load(tmp_path), **kw)
+    assert S.num_levels == R.num_levels
+    for l in range(R.num_levels - 1):
+        assert abs(S.level_lmax(l) - R.level_lmax(l)) <= 1e-12 * max(R.level_lmax(l), 1)
+    b = _proj(np.random.default_rng(5).standard_normal(L.n))
+    assert _relerr(S.cycle(0, b), R.cycle(0, b)) <= 1e-12
+    info = S.solve(G.rhs(L.n, seed=6))
+    xr, _ = R.solve(G.rhs(L.n, seed=6))
+    assert info.converged and _relerr(info.solution, xr) <= 1e-6
+
+
+def test_gpu_dump_import_round_trip(tmp_path):
+    L = GRAPHS["rmat12"]()
+    S = Solver(L, kcycle=1, outer_ksp_type="fcg")
+    S.dump_hierarchy(str(tmp_path))
+    from ligmg_gb300 import petsc_io
+    T = Solver.import_hierarchy(petsc_io.load(tmp_path), kcycle=1, outer_ksp_type="fcg")
+    b = G.rhs(L.n, seed=8)
+    a, c = S.solve(b), T.solve(b)
+    assert a.iters() == c.iters() and np.array_equal(a.solution, c.solution)
