@@ -256,6 +256,13 @@ ligmg_status ligmg_get_stream(ligmg_handle h, void **stream);
 /* Kernels launched by this library in this process so far. */
 ligmg_status ligmg_launch_count(int64_t *count);
 
+/* Jacobi-preconditioned CG on the input matrix (the reference's own
+ * comparison solver, --test-cg: src/main.cpp:168-180 with the InvDiagSR
+ * preconditioner z = D^-1 r, smoothing.hpp:56-76), FP64, rtol opts.tol,
+ * at most opts.iters iterations, constant projected out of b and of z. */
+ligmg_status ligmg_solve_pcg_jacobi(ligmg_handle h, const double *b, double *x,
+                                    ligmg_info *info);
+
 /* A batch of independent graph Laplacians solved together (no reference
  * counterpart; the reference solves one graph per Solver).  The graphs are
  * given as one block-diagonal CSR matrix: graph g owns rows and columns

@@ -891,6 +891,8 @@ void make_hierarchy(Handle &H, i64 n, const i64 *rowptr, const i32 *col, const d
   ap.agg_iter_factor = o.agg_iter_factor;
   ap.votes_to_seed = (double)o.votes_to_seed;
   ap.max_agg_size = (double)o.max_agg_size;
+  ap.rejection_ratio = o.rejection_ratio;
+  ap.rejection_to_seed = o.rejection_to_seed != 0;
   auto &h = H.h;
   while ((int)h.size() < o.max_levels && (h.empty() || h.back()->A.nnz > o.min_size)) {
     if (o.always_elim && o.elim_iters >= 1) {
@@ -1513,8 +1515,7 @@ ligmg_status ligmg_create(int64_t n, const int64_t *rowptr, const int32_t *col,
         (o.precision != LIGMG_PREC_FP64 && o.precision != LIGMG_PREC_FP32))
       return LIGMG_ERR_INVALID_ARGUMENT;
     if (o.smoother_type > LIGMG_SMOOTHER_CHEBYSHEV || o.outer_ksp_type > LIGMG_KSP_FCG ||
-        o.kcycle_ksp_type != LIGMG_KSP_FCG || o.max_agg_size > 0 || o.rejection_ratio >= 0 ||
-        o.elim_iters > 1 || o.aff_scaling < LIGMG_AFF_NONE || o.aff_scaling > LIGMG_AFF_MAX)
+        o.kcycle_ksp_type != LIGMG_KSP_FCG || o.elim_iters > 1 || o.aff_scaling < LIGMG_AFF_NONE || o.aff_scaling > LIGMG_AFF_MAX)
       return LIGMG_ERR_UNSUPPORTED;
     H->device = o.device;
     LG_CUDA(cudaSetDevice(H->device));
@@ -1622,6 +1623,87 @@ ligmg_status ligmg_backward(ligmg_handle h, const double *g, double *dw, double 
   });
 }
 
+ligmg_status ligmg_solve_pcg_jacobi(ligmg_handle h, const double *b, double *x,
+                                    ligmg_info *info) {
+  if (!h || !b || !x) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(h->device));
+    auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = h->s;
+    const Level &L = *h->h[0];
+    i64 n = L.A.n;
+    MatView<double> A = viewA<double>(L, 1, s);
+    DBuf<double> X(n, s), R(n, s), Z(n, s), P(n, s), Q(n, s), sc(8, s), red(fused_scratch_len(n, 1), s);
+    red.zero();
+    R.upload(b, n);
+    i64 slen = col_reduce_scratch(n, 1);
+    DBuf<double> scratch(slen, s);
+    col_reduce<double>(n, 1, Red::Sum, R.p, nullptr, sc.p, scratch.p, slen, s);
+    sub_mean<double>(n, 1, R.p, sc.p, s);
+    X.zero();
+    auto prec = [&]() {  // z = D^-1 r, constant removed (null space on the Mat)
+      k_mul_diag<<<grid_for(n, 256), 256, 0, s>>>(n, L.invd.p, R.p, Z.p);
+      LG_LAUNCH();
+      col_reduce<double>(n, 1, Red::Sum, Z.p, nullptr, sc.p, scratch.p, slen, s);
+      sub_mean<double>(n, 1, Z.p, sc.p, s);
+    };
+    double *rz = sc.p + 1, *rz_old = sc.p + 2, *beta = sc.p + 3, *pq = sc.p + 4,
+           *alpha = sc.p + 5, *rn2 = sc.p + 6;
+    col_dot1<double>(n, 1, R.p, R.p, rn2, red.p, s);
+    double rn0 = std::sqrt(read_scalar(rn2, s));
+    std::vector<double> hist{rn0};
+    int it = 0;
+    bool conv = rn0 == 0;
+    if (!conv) {
+      prec();
+      col_dot1<double>(n, 1, Z.p, R.p, rz, red.p, s);
+      LG_CUDA(cudaMemcpyAsync(P.p, Z.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    }
+    for (; !conv && it < h->opts.iters; it++) {
+      EpiArgs a;
+      a.y = Q.p;
+      spmm<double>(A, P.p, 1, Epi::Store, a, s);
+      col_dot1<double>(n, 1, P.p, Q.p, pq, red.p, s);
+      scal_div(1, rz, pq, alpha, nullptr, s);
+      fcg_update<double>(n, 1, X.p, R.p, P.p, Q.p, alpha, true, s);
+      col_dot1<double>(n, 1, R.p, R.p, rn2, red.p, s);
+      double rn = std::sqrt(read_scalar(rn2, s));
+      hist.push_back(rn);
+      if (!std::isfinite(rn)) throw Error(LIGMG_ERR_BREAKDOWN, "non-finite residual");
+      if (rn <= std::max(h->opts.tol * rn0, 1e-60)) {
+        conv = true;
+        it++;
+        break;
+      }
+      prec();
+      LG_CUDA(cudaMemcpyAsync(rz_old, rz, sizeof(double), cudaMemcpyDeviceToDevice, s));
+      col_dot1<double>(n, 1, Z.p, R.p, rz, red.p, s);
+      scal_div(1, rz, rz_old, beta, nullptr, s);
+      cg_direction<double>(n, 1, P.p, Z.p, beta, s);
+    }
+    X.download(x, n);
+    LG_CUDA(cudaStreamSynchronize(s));
+    if (info) {
+      info->iters = it;
+      info->converged = conv;
+      info->rel_residual = rn0 > 0 ? hist.back() / rn0 : 0.0;
+      info->true_rel_residual = info->rel_residual;
+      info->cycle_complexity = (double)n / (double)L.A.nnz;  // main.cpp:177
+      info->work = it * (1 + info->cycle_complexity);
+      info->solve_seconds =
+          std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      info->setup_seconds = 0;
+      info->history_len = 0;
+      if (info->residual_history && info->history_capacity > 0) {
+        int m = std::min((int)hist.size(), info->history_capacity);
+        std::copy(hist.begin(), hist.begin() + m, info->residual_history);
+        info->history_len = m;
+      }
+    }
+    return conv ? LIGMG_OK : LIGMG_NOT_CONVERGED;
+  });
+}
+
 ligmg_status ligmg_batch_create(int32_t num_graphs, const int64_t *vertex_offsets,
                                 const int64_t *rowptr, const int32_t *col, const double *val,
                                 const ligmg_options *opts, ligmg_handle *out) {
@@ -1639,8 +1721,7 @@ ligmg_status ligmg_batch_create(int32_t num_graphs, const int64_t *vertex_offset
     if (opts) H->opts = *opts; else ligmg_default_options(&H->opts);
     const ligmg_options &o = H->opts;
     if (o.outer_ksp_type != LIGMG_KSP_FCG || o.smoother_type > LIGMG_SMOOTHER_CHEBYSHEV ||
-        o.max_agg_size > 0 || o.rejection_ratio >= 0 || o.elim_iters > 1 ||
-        o.kcycle_ksp_type != LIGMG_KSP_FCG ||
+        o.elim_iters > 1 || o.kcycle_ksp_type != LIGMG_KSP_FCG ||
         (o.precision != LIGMG_PREC_FP64 && o.precision != LIGMG_PREC_FP32))
       return LIGMG_ERR_UNSUPPORTED;
     H->seg0.assign(vertex_offsets, vertex_offsets + num_graphs + 1);

@@ -589,6 +589,90 @@ __global__ void k_mark(i64 n, int first_iter, int nn, double max_agg_size, doubl
   }
 }
 
+// ---- reject_aggregates (aggregation.hpp:630-685) --------------------------
+__device__ __forceinline__ bool st_decided(int x) {
+  return x == ST_Decided || x == ST_DecidedRoot || x == ST_Seed || x == ST_SeedNeighbor;
+}
+__global__ void k_rej_count(i64 n, const i32 *st, const i32 *ind, i64 *size, i64 *mcnt,
+                            uint8_t *member) {
+  i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int s = st[i];
+  if (st_decided(s) && ind[i] >= 0) atomicAdd((unsigned long long *)&size[ind[i]], 1ull);
+  bool m = (s == ST_Decided || s == ST_SeedNeighbor) && ind[i] >= 0;
+  member[i] = m ? 1 : 0;
+  if (m) atomicAdd((unsigned long long *)&mcnt[ind[i]], 1ull);
+}
+__global__ void k_rej_keys(const i32 *list, i64 m, const i32 *ind, u64 *keys, u32 *vals) {
+  i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  keys[k] = (u64)(u32)ind[list[k]];
+  vals[k] = (u32)list[k];
+}
+// members sorted by (root, index); reset the first csz^2/(size-1) of every
+// root whose aggregate is larger than max_size; flag that root
+__global__ void k_rej_apply(i64 m, const u64 *keys, const u32 *vals, const i64 *mstart,
+                            const i64 *mcnt, const i64 *size, i64 max_size, i32 *st, i32 *ind,
+                            uint8_t *rootflag) {
+  i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  i64 root = (i64)keys[k];
+  i64 sz = size[root];
+  if (sz <= max_size) return;
+  i64 csz = mcnt[root];
+  i64 local = csz * csz / (sz - 1);
+  if (k - mstart[root] < local) {
+    st[vals[k]] = ST_Undecided;
+    ind[vals[k]] = -1;
+  }
+  rootflag[root] = 1;
+}
+__global__ void k_rej_roots(i64 n, const uint8_t *rootflag, i32 *st) {
+  i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && rootflag[i]) st[i] = ST_DecidedRoot;
+}
+
+// ---- conductance_rejection with ext_int_ratio (aggregation.hpp:563-628,752-778)
+__global__ void k_ext_int_ratio(const i64 *rp, const i32 *ci, const double *v, i64 n,
+                                const i32 *st, const i32 *ind, double *ratio) {
+  i64 i = warp_row();
+  if (i >= n) return;
+  unsigned lane = lane_id();
+  double ext = 0.0, inn = 0.0;
+  bool me = st_decided(st[i]);
+  if (me) {
+    for (i64 base = rp[i]; base < rp[i + 1]; base += 32) {
+      i64 k = base + lane;
+      int kind = 0;  // 0: skip, 1: internal, 2: external
+      double a = 0;
+      if (k < rp[i + 1]) {
+        i32 j = ci[k];
+        if (j != i) {
+          a = v[k];
+          kind = (st_decided(st[j]) && ind[j] == ind[i]) ? 1 : 2;
+        }
+      }
+      for (int q = 0; q < 32; q++) {
+        int kq = __shfl_sync(0xffffffffu, kind, q);
+        double aq = __shfl_sync(0xffffffffu, a, q);
+        if (kq == 1) inn = __dsub_rn(inn, aq);
+        else if (kq == 2) ext = __dsub_rn(ext, aq);
+      }
+    }
+  }
+  if (lane == 0) ratio[i] = __ddiv_rn(ext, inn);
+}
+__global__ void k_conductance(i64 n, const double *ratio, double thr, int to_seed, i32 *st,
+                              i32 *ind) {
+  i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int s = st[i];
+  if (ratio[i] > thr && (s == ST_Decided || s == ST_SeedNeighbor)) {
+    st[i] = to_seed ? ST_Seed : ST_Undecided;
+    ind[i] = (i32)i;
+  }
+}
+
 __global__ void k_init_states(i64 n, i32 *st, i32 *ind) {
   i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
@@ -952,7 +1036,40 @@ void gpu_aggregation(const DCsr<double> &A, const AggParams &p, const double *tv
                                              out.votes.p, out.colsum.p, va_st.p, va_ind.p,
                                              out.st.p, out.ind.p);
     LG_LAUNCH();
-    if (p.max_agg_size > 0) throw Error(LIGMG_ERR_UNSUPPORTED, "max_agg_size > 0");
+    if (p.max_agg_size > 0) {  // reject_aggregates
+      DBuf<i64> size(n, s), mcnt(n + 1, s), mstart(n + 1, s);
+      DBuf<uint8_t> member(n, s), rootflag(n, s);
+      size.zero();
+      mcnt.zero();
+      rootflag.zero();
+      k_rej_count<<<grid_for(n, 256), 256, 0, s>>>(n, out.st.p, out.ind.p, size.p, mcnt.p,
+                                                   member.p);
+      LG_LAUNCH();
+      DBuf<i32> list(n, s);
+      i64 m = compact_indices(member.p, n, list.p, s);
+      if (m > 0) {
+        exclusive_scan<i64>(mcnt.p, mstart.p, n + 1, s);
+        DBuf<u64> keys(m, s);
+        DBuf<u32> vals(m, s);
+        k_rej_keys<<<grid_for(m, 256), 256, 0, s>>>(list.p, m, out.ind.p, keys.p, vals.p);
+        LG_LAUNCH();
+        radix_sort_pairs(keys.p, vals.p, m, key_bits, s);
+        k_rej_apply<<<grid_for(m, 256), 256, 0, s>>>(m, keys.p, vals.p, mstart.p, mcnt.p, size.p,
+                                                     (i64)p.max_agg_size, out.st.p, out.ind.p,
+                                                     rootflag.p);
+        k_rej_roots<<<grid_for(n, 256), 256, 0, s>>>(n, rootflag.p, out.st.p);
+        LG_LAUNCH();
+      }
+    }
+    if (iter >= p.agg_iters / 2 && p.rejection_ratio >= 0) {  // conductance_rejection
+      DBuf<double> ratio(n, s);
+      k_ext_int_ratio<<<grid_for(n * 32, kBlock), kBlock, 0, s>>>(A.rp.p, A.ci.p, A.v.p, n,
+                                                                  out.st.p, out.ind.p, ratio.p);
+      k_conductance<<<grid_for(n, 256), 256, 0, s>>>(n, ratio.p, p.rejection_ratio,
+                                                     p.rejection_to_seed ? 1 : 0, out.st.p,
+                                                     out.ind.p);
+      LG_LAUNCH();
+    }
   }
   // aggregate ids: rank of the root among roots (remove_zero_rows)
   DBuf<i32> is_root(n, s), ntot(1, s);

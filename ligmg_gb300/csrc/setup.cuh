@@ -33,6 +33,8 @@ struct AggParams {
   int num_tvs, tvs_smooth, agg_iters, strength_metric, aff_scaling;
   bool neighbor_of_neighbor;
   double thresh, agg_init_factor, agg_iter_factor, votes_to_seed, max_agg_size;
+  double rejection_ratio;
+  bool rejection_to_seed;
 };
 // tvs_host: num_tvs x n test vectors already drawn and mean-projected on the
 // host (row t = test vector t).

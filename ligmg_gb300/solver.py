@@ -165,6 +165,18 @@ class Solver:
                                info.work, x, info.true_rel_residual, st == 0, ci, ct,
                                info.cycle_complexity)
 
+    def solve_pcg_jacobi(self, b) -> ConvergenceInfo:
+        """Jacobi-preconditioned CG on the input matrix (the reference's
+        --test-cg comparison, src/main.cpp:168-180)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.empty_like(b)
+        info, hist, ci, ct = self._info(1, history=self.options.iters + 2)
+        st = check(lib().ligmg_solve_pcg_jacobi(self._h, _p(b), _p(x), C.byref(info)),
+                   "ligmg_solve_pcg_jacobi")
+        return ConvergenceInfo(hist[: info.history_len].copy(), info.iters, info.solve_seconds,
+                               info.work, x, info.true_rel_residual, st == 0, ci, ct,
+                               info.cycle_complexity)
+
     def solve_batched(self, B) -> ConvergenceInfo:
         """k right-hand sides as an n x k row-major block (k in 1,2,4,...,64)."""
         B = np.ascontiguousarray(B, dtype=np.float64)

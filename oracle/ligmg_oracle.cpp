@@ -664,6 +664,32 @@ void aggregation(const Csr &A, const ligmg_options &o, GlibcRand &rng, Level &L)
         }
       }
     }
+    // conductance_rejection (:752-778) with ext_int_ratio (:563-628), from the
+    // second half of the iterations; the ratio reads the states before any
+    // vertex is rejected
+    if (iter >= o.agg_iters / 2 && o.rejection_ratio >= 0) {
+      auto decided = [](int32_t x) {
+        return x == Decided || x == DecidedRoot || x == Seed || x == SeedNeighbor;
+      };
+      std::vector<double> ratio(n);
+      for (i64 i = 0; i < n; i++) {
+        double ext = 0, inn = 0;
+        if (decided(st[i])) {
+          for (i64 e = A.rp[i]; e < A.rp[i + 1]; e++) {
+            i64 j = A.ci[e];
+            if (j == i) continue;
+            if (decided(st[j]) && ind[j] == ind[i]) inn -= A.v[e];
+            else ext -= A.v[e];
+          }
+        }
+        ratio[i] = ext / inn;
+      }
+      for (i64 i = 0; i < n; i++)
+        if (ratio[i] > o.rejection_ratio && (st[i] == Decided || st[i] == SeedNeighbor)) {
+          st[i] = o.rejection_to_seed ? Seed : Undecided;
+          ind[i] = i;
+        }
+    }
   }
   L.dbg_colsum = col_sum;
   L.dbg_votes = votes;

@@ -67,7 +67,10 @@ def test_setup_bit_exact(name):
 @pytest.mark.parametrize("opt", [dict(aff_scaling="row"), dict(aff_scaling="column"),
                                  dict(aff_scaling="rowcolumn"), dict(aff_scaling="sym"),
                                  dict(aff_scaling="none"), dict(strength_metric="none"),
-                                 dict(strength_metric="algebraic-distance")])
+                                 dict(strength_metric="algebraic-distance"),
+                                 dict(max_agg_size=6), dict(rejection_ratio=1.5),
+                                 dict(rejection_ratio=1.0, rejection_to_seed=1),
+                                 dict(neighbor_of_neighbor=1)])
 def test_setup_options_bit_exact(opt):
     L = GRAPHS["rmat12"]()
     S, R = Solver(L, **opt), O.OracleSolver(L, **opt)
@@ -263,3 +266,15 @@ def test_gpu_dump_import_round_trip(tmp_path):
     b = G.rhs(L.n, seed=8)
     a, c = S.solve(b), T.solve(b)
     assert a.iters() == c.iters() and np.array_equal(a.solution, c.solution)
+
+
+def test_pcg_jacobi_baseline():
+    L = GRAPHS["grid48_logn"]()
+    S = Solver(L, iters=5000)
+    b = G.rhs(L.n, seed=12)
+    info = S.solve_pcg_jacobi(b)
+    assert info.converged
+    r = b - L.to_scipy() @ info.solution
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 2e-8
+    mg = S.solve(b)
+    assert mg.iters() < info.iters()  # multigrid needs far fewer iterations
