@@ -71,6 +71,12 @@ def parse():
     ap.add_argument("--scale", type=int, default=SCALE)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--workload", default="rmat20", choices=["rmat20", "grid3d-ksweep", "rgg-batch"],
+                    help="rmat20: the headline line (default); grid3d-ksweep: 128^3 7-point grid, "
+                         "lognormal weights, k in 1,8,32,64; rgg-batch: 256 uneven random "
+                         "geometric graphs solved in one launch")
+    ap.add_argument("--grid", type=int, default=128)
+    ap.add_argument("--graphs", type=int, default=256)
     return ap.parse_args()
 
 
@@ -380,10 +386,102 @@ def run_ours(args):
     print(json.dumps(out), flush=True)
 
 
+def _timed_solves(S, stream, Bd, k, steps, warmup):
+    import torch
+    n = Bd[0].shape[0]
+    Xd = torch.empty((n, k), dtype=torch.float64, device=Bd[0].device)
+    for w in range(warmup):
+        S.solve_batched_device(Bd[w % len(Bd)].data_ptr(), k, Xd.data_ptr())
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    infos = [S.solve_batched_device(Bd[t % len(Bd)].data_ptr(), k, Xd.data_ptr())
+             for t in range(steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), infos
+
+
+def run_grid3d(args):
+    """configs[2]: k right-hand sides as an n x k block, k in {1, 8, 32, 64}."""
+    import torch
+    from ligmg_gb300 import Solver
+    from ligmg_gb300 import build as Bld
+    from ligmg_gb300 import graphs as G
+    Bld.build()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    L = G.grid3d(args.grid, weights="lognormal", seed=1)
+    log(f"grid3d n={L.n} nnz={L.nnz}")
+    S = Solver(L, **solver_kw("fp32"))
+    S.set_stream(stream.cuda_stream)
+    per_k = {}
+    for k in (1, 8, 32, 64):
+        Bd = [torch.from_numpy(G.rhs(L.n, k=k, seed=7 + i)).to(dev).reshape(L.n, k).contiguous()
+              for i in range(2)]
+        ms, infos = _timed_solves(S, stream, Bd, k, args.steps, args.warmup)
+        per_k[k] = {"ms_per_rhs": ms / (args.steps * k), "iters": [i.iters() for i in infos],
+                    "max_true_rel_residual": max(float(np.max(i.col_true_rel_residual)) for i in infos)}
+        log(f"k={k} {per_k[k]['ms_per_rhs']:.3f} ms/RHS")
+        del Bd
+    S64 = Solver(L, **solver_kw("fp64"))
+    S64.set_stream(stream.cuda_stream)
+    b1 = [torch.from_numpy(G.rhs(L.n, seed=3)).to(dev).reshape(L.n, 1).contiguous()]
+    ms64, inf64 = _timed_solves(S64, stream, b1, 1, 3, 1)
+    out = {"metric": METRIC, "value": per_k[32]["ms_per_rhs"], "unit": "ms/RHS", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_k[32]["ms_per_rhs"] * 32,
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+           "dtype": "fp32 cycle / fp64 outer", "data": "synthetic",
+           "config": {"workload": f"grid3d {args.grid}^3 7-point, lognormal(0,1) weights, n={L.n} "
+                                  f"nnz={L.nnz}; FP32 hierarchy, K-cycle, FCG rtol 1e-8",
+                      "per_k": per_k, "fp64_single_ms_per_rhs": ms64 / 3}}
+    print(json.dumps(out), flush=True)
+
+
+def run_rgg_batch(args):
+    """configs[3]: 256 random geometric graphs (n log-uniform in [1e4, 2e5])
+    solved together from one captured CUDA graph."""
+    from ligmg_gb300 import BatchSolver, Solver
+    from ligmg_gb300 import build as Bld
+    from ligmg_gb300 import graphs as G
+    Bld.build()
+    t0 = time.perf_counter()
+    gs = G.rgg_batch(args.graphs, seed=0)
+    log(f"{len(gs)} graphs, {sum(g.n for g in gs)} vertices, {sum(g.nnz for g in gs)} nnz "
+        f"generated in {time.perf_counter() - t0:.1f}s")
+    t0 = time.perf_counter()
+    B = BatchSolver(gs, precision="fp32", kcycle=1)
+    setup = time.perf_counter() - t0
+    bs = [G.rhs(g.n, seed=100 + i) for i, g in enumerate(gs)]
+    for _ in range(args.warmup):
+        B.solve(bs)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        xs, info = B.solve(bs)
+    secs = (time.perf_counter() - t0) / args.steps
+    out = {"metric": METRIC, "value": 1e3 * secs / len(gs), "unit": "ms/RHS", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs,
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+           "dtype": "fp32 cycle / fp64 outer", "data": "synthetic",
+           "config": {"workload": f"{len(gs)} random geometric graphs, n log-uniform in "
+                                  f"[1e4, 2e5], mean degree ~12, w = clip(1/d, .1, 10), LCC; "
+                                  f"one RHS each; host-timed ligmg_batch_solve incl. H2D/D2H",
+                      "vertices": int(sum(g.n for g in gs)), "nnz": int(sum(g.nnz for g in gs)),
+                      "setup_s": setup, "max_iters": int(np.max(info.col_iters)),
+                      "converged": bool(info.converged),
+                      "max_true_rel_residual": float(np.max(info.col_true_rel_residual)),
+                      "levels": B.num_levels}}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "grid3d-ksweep":
+        run_grid3d(args)
+    elif args.workload == "rgg-batch":
+        run_rgg_batch(args)
     else:
         run_ours(args)
 
