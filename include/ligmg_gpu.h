@@ -238,6 +238,12 @@ ligmg_status ligmg_spmv(ligmg_handle h, int32_t level, const double *x,
 #define LIGMG_KERNEL_CHEB_B 3      /* later Chebyshev steps */
 #define LIGMG_KERNEL_ELIM_INTERP 4 /* x = P xc + Q b */
 #define LIGMG_KERNEL_ELIM_RESTRICT 5 /* bc = R b */
+#define LIGMG_KERNEL_AGG_RESTRICT 6  /* bc = R r, R the 0/1 member matrix */
+#define LIGMG_KERNEL_AGG_PROLONG 7   /* x += P xc */
+#define LIGMG_KERNEL_COARSE 8        /* x = pinv b (dense coarse level) */
+#define LIGMG_KERNEL_KRYLOV 9        /* K-cycle inner FCG reductions and updates */
+#define LIGMG_KERNEL_VECTOR 10       /* smoother start, copies, scaling, conversions */
+#define LIGMG_KERNEL_OUTER 11        /* outer Krylov reductions, updates, projection */
 typedef struct ligmg_kernel_stat {
   int32_t level;
   int32_t kind;      /* LIGMG_KERNEL_* */
@@ -253,7 +259,8 @@ ligmg_status ligmg_profile_enable(ligmg_handle h, int32_t enable);
  * caller's events on that stream bracket the handle's kernels. */
 ligmg_status ligmg_set_stream(ligmg_handle h, void *stream);
 ligmg_status ligmg_get_stream(ligmg_handle h, void **stream);
-/* Kernels launched by this library in this process so far. */
+/* Kernels launched by this library in this process so far (kernels run
+ * from the library's CUDA graphs are counted on every replay). */
 ligmg_status ligmg_launch_count(int64_t *count);
 
 /* Jacobi-preconditioned CG on the input matrix (the reference's own

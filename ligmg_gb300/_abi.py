@@ -155,7 +155,8 @@ def default_options(**overrides) -> Options:
 
 
 KERNEL_KINDS = {0: "spmv", 1: "resid", 2: "cheb_a", 3: "cheb_b", 4: "elim_interp",
-                5: "elim_restrict"}
+                5: "elim_restrict", 6: "agg_restrict", 7: "agg_prolong", 8: "coarse",
+                9: "krylov", 10: "vector", 11: "outer"}
 
 
 class KernelStat(C.Structure):

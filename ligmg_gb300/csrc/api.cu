@@ -171,6 +171,10 @@ struct Level {
   bool has32 = false;
   DBuf<float> Av32, invd32, Pv32, Rv32, Q32, pinv32;
   DBuf<float2> Adf;  // (hi, lo) float pairs of A's FP64 values (outer product)
+  // aggregation levels: unit values of the member matrix R (nc x n, rows
+  // agg.mrp / agg.members), so restriction runs through the hub-split SpMM
+  DBuf<double> ones64;
+  DBuf<float> ones32;
   // hub-row plans: hubA64 (FP64, k = 1) is built at setup; the others are
   // built on first use per (precision, k) from the cached host row pointers
   HubPlan<double> hubA64;
@@ -231,8 +235,8 @@ const HubPlan<T> &plan_for(const Level &L, bool isR, int k, cudaStream_t s) {
   HubPlan<T> &p = plans<T>(L, isR)[k];
   if (!p.built) {
     const std::vector<i64> &rp = isR ? L.rrp_host : L.rp_host;
-    i64 n = isR ? L.elim.R.n : L.A.n;
-    p.build(rp.data(), n, entries_per_step(sizeof(T), k), k, s);
+    i64 n = (i64)rp.size() - 1;
+    p.build(rp.data(), n, split_unit(sizeof(T), k), k, s);
   }
   return p;
 }
@@ -244,6 +248,10 @@ const T *valsA(const Level &L) {
 }
 template <typename T>
 const T *valsR(const Level &L) {
+  if (L.type == LIGMG_LEVEL_AGG) {
+    if constexpr (sizeof(T) == 8) return (const T *)L.ones64.p;
+    else return (const T *)L.ones32.p;
+  }
   if constexpr (sizeof(T) == 8) return (const T *)L.elim.R.v.p;
   else return (const T *)L.Rv32.p;
 }
@@ -258,7 +266,12 @@ MatView<T> viewA(const Level &L, int k, cudaStream_t s) {
 template <typename T>
 MatView<T> viewR(const Level &L, int k, cudaStream_t s) {
   MatView<T> m;
-  m.n = L.elim.R.n; m.rp = L.elim.R.rp.p; m.ci = L.elim.R.ci.p; m.v = valsR<T>(L);
+  if (L.type == LIGMG_LEVEL_AGG) {
+    m.n = L.nc; m.rp = L.agg.mrp.p; m.ci = L.agg.members.p;
+  } else {
+    m.n = L.elim.R.n; m.rp = L.elim.R.rp.p; m.ci = L.elim.R.ci.p;
+  }
+  m.v = valsR<T>(L);
   m.lanes_per_row = L.lanesR;
   plan_for<T>(L, true, k, s).fill(m);
   return m;
@@ -389,6 +402,7 @@ struct PrecGraph {
   const double *r = nullptr;
   double *z = nullptr;
   bool prof = false;
+  int64_t kernels = 0;  // library kernels recorded in the graph
   std::vector<ProfRec> tmpl;
   void reset() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -408,6 +422,7 @@ struct ligmg_handle_s {
   // batch mode: vertex offsets of the graphs in the block-diagonal input
   std::vector<lg::i64> seg0;
   cudaGraphExec_t batch_first = nullptr, batch_more = nullptr;  // whole-solve graphs
+  int64_t batch_first_kernels = 0, batch_more_kernels = 0;
   size_t batch_base = 0;
   lg::DBuf<double> fwd_x;  // forward solution kept for ligmg_backward
   bool has_fwd = false;
@@ -424,7 +439,14 @@ struct ligmg_handle_s {
   std::map<int, std::unique_ptr<lg::Work<double>>> w64;
   std::map<int, std::unique_ptr<lg::OuterWork>> ow;
   ~ligmg_handle_s() {
+    // Buffers keep the stream they were allocated on, which may be a stream
+    // that is destroyed below or a caller's stream that no longer exists.
+    // After the handle's streams are idle, every buffer is therefore freed
+    // with a synchronous cudaFree, and all of them (fwd_x included) before
+    // any stream is destroyed.
     if (s) cudaStreamSynchronize(s);
+    for (auto o : old_streams) cudaStreamSynchronize(o);
+    lg::SyncFreeScope sync_free;
     for (auto &g : pgraphs) g.second.reset();
     pgraphs.clear();
     if (batch_first) cudaGraphExecDestroy(batch_first);
@@ -433,11 +455,8 @@ struct ligmg_handle_s {
     w64.clear();
     ow.clear();
     h.clear();
-    if (s) cudaStreamSynchronize(s);
-    for (auto o : old_streams) {
-      cudaStreamSynchronize(o);
-      cudaStreamDestroy(o);
-    }
+    fwd_x.release();
+    for (auto o : old_streams) cudaStreamDestroy(o);
     if (s && own_stream) cudaStreamDestroy(s);
   }
 };
@@ -582,7 +601,8 @@ struct Engine {
       // (omega = 2/3) per smoother call, whatever the iteration count
       const double omega = 2.0 / 3.0;
       if (x_zero) {
-        cheb_init_zero<T>(n, k, b, invd, 1.0 / omega, x, s);
+        timed(H, (int)l, LIGMG_KERNEL_VECTOR, k, sizeof(T) == 8, (2.0 * n * k + n) * sizeof(T),
+              [&] { cheb_init_zero<T>(n, k, b, invd, 1.0 / omega, x, s); });
         return;
       }
       EpiArgs a;
@@ -590,7 +610,9 @@ struct Engine {
       timed(H, (int)l, LIGMG_KERNEL_RESID, k, sizeof(T) == 8,
             core_bytes(n, L.A.nnz, n, k, sizeof(T)) + (3.0 * n * k + n) * sizeof(T),
             [&] { spmm<T>(A, x, k, Epi::Jacobi, a, s); });
-      LG_CUDA(cudaMemcpyAsync(x, w.xt.p, sizeof(T) * n * k, cudaMemcpyDeviceToDevice, s));
+      timed(H, (int)l, LIGMG_KERNEL_VECTOR, k, sizeof(T) == 8, 2.0 * n * k * sizeof(T), [&] {
+        LG_CUDA(cudaMemcpyAsync(x, w.xt.p, sizeof(T) * n * k, cudaMemcpyDeviceToDevice, s));
+      });
       return;
     }
     if (iters <= 0) return;
@@ -599,11 +621,10 @@ struct Engine {
     T *d_cur;
     T *d_other = w.d1.p;
     if (x_zero) {
-      if (iters == 1) {
-        cheb_init_zero<T>(n, k, b, invd, L.theta, x, s);
-        return;
-      }
-      cheb_init_zero<T>(n, k, b, invd, L.theta, w.d0.p, s);
+      T *d0 = iters == 1 ? x : w.d0.p;
+      timed(H, (int)l, LIGMG_KERNEL_VECTOR, k, sizeof(T) == 8, (2.0 * n * k + n) * sizeof(T),
+            [&] { cheb_init_zero<T>(n, k, b, invd, L.theta, d0, s); });
+      if (iters == 1) return;
       d_cur = w.d0.p;
       x_cur = w.d0.p;  // x1 = d0
       r_cur = b;       // r0 = b
@@ -618,7 +639,9 @@ struct Engine {
       x_cur = w.xt.p;
       r_cur = w.r.p;
       if (iters == 1) {
-        LG_CUDA(cudaMemcpyAsync(x, w.xt.p, sizeof(T) * n * k, cudaMemcpyDeviceToDevice, s));
+        timed(H, (int)l, LIGMG_KERNEL_VECTOR, k, sizeof(T) == 8, 2.0 * n * k * sizeof(T), [&] {
+          LG_CUDA(cudaMemcpyAsync(x, w.xt.p, sizeof(T) * n * k, cudaMemcpyDeviceToDevice, s));
+        });
         return;
       }
     }
@@ -651,7 +674,9 @@ struct Engine {
     Level &L = *H.h[l];
     i64 n = L.A.n;
     if (L.type == LIGMG_LEVEL_COARSE) {
-      coarse_apply<T>(n, k, pinvT<T>(L), b, x, s);
+      timed(H, (int)l, LIGMG_KERNEL_COARSE, k, sizeof(T) == 8,
+            ((double)n * n + 2.0 * n * k) * sizeof(T),
+            [&] { coarse_apply<T>(n, k, pinvT<T>(L), b, x, s); });
       return;
     }
     LevelWork<T> &nw = W.lw[l + 1];
@@ -678,11 +703,19 @@ struct Engine {
     timed(H, (int)l, LIGMG_KERNEL_RESID, k, sizeof(T) == 8,
           core_bytes(n, L.A.nnz, n, k, sizeof(T)) + 2.0 * n * k * sizeof(T),
           [&] { spmm<T>(viewA<T>(L, k, s), x, k, Epi::Resid, a, s); });
-    restrict_agg<T>(L.nc, k, L.agg.mrp.p, L.agg.members.p, w.r.p, nw.in.p, s);
+    EpiArgs rs;
+    rs.y = nw.in.p;
+    timed(H, (int)l, LIGMG_KERNEL_AGG_RESTRICT, k, sizeof(T) == 8,
+          8.0 * (L.nc + 1) + 4.0 * n + ((double)n + L.nc) * k * sizeof(T),
+          [&] { spmm<T>(viewR<T>(L, k, s), w.r.p, k, Epi::Store, rs, s); });
     recurse(l, nw.in.p, nw.out.p);
-    prolong_agg<T>(n, k, L.agg.agg.p, nw.out.p, x, s);
+    timed(H, (int)l, LIGMG_KERNEL_AGG_PROLONG, k, sizeof(T) == 8,
+          4.0 * n + (2.0 * n + L.nc) * k * sizeof(T),
+          [&] { prolong_agg<T>(n, k, L.agg.agg.p, nw.out.p, x, s); });
     smooth(l, x, b, o().post_smooth, false);
-    if (o().constant_correction) scale_vec<T>(n, k, x, 4.0 / 3.0, s);
+    if (o().constant_correction)
+      timed(H, (int)l, LIGMG_KERNEL_VECTOR, k, sizeof(T) == 8, 2.0 * n * k * sizeof(T),
+            [&] { scale_vec<T>(n, k, x, 4.0 / 3.0, s); });
   }
 
   void recurse(size_t l, T *bc, T *xc) {
@@ -703,7 +736,8 @@ struct Engine {
     LevelWork<T> &w = W.lw[l];
     i64 n = L.A.n;
     MatView<T> A = viewA<T>(L, k, s);
-    LG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * n * k, s));
+    timed(H, (int)l, LIGMG_KERNEL_VECTOR, k, sizeof(T) == 8, 1.0 * n * k * sizeof(T),
+          [&] { LG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * n * k, s)); });
     T *r = b;
     T *p = w.fp0.p, *pp = w.fp1.p, *q = w.fq0.p, *qp = w.fq1.p;
     const SegInfo S = L.seginfo();
@@ -715,25 +749,31 @@ struct Engine {
                       w.sslot(S_ALPHA), nullptr};
     for (int it = 0; it < iters; it++) {
       cycle(l, r, w.fz.p);
-      if (seg) {
-        seg_fcg_beta<T>(S, w.fz.p, it > 0 ? qp : nullptr, sc, s);
-        seg_fcg_dir<T>(S, n, p, w.fz.p, it > 0 ? pp : nullptr, sc, s);
-      } else {
-        fcg_beta<T>(n, k, w.fz.p, it > 0 ? qp : nullptr, sc, w.fscratch.p, s);
-        fcg_dir<T>(n, k, p, w.fz.p, it > 0 ? pp : nullptr, sc, s);
-      }
+      const double nk = (double)n * k * sizeof(T);
+      timed(H, (int)l, LIGMG_KERNEL_KRYLOV, k, sizeof(T) == 8, (it > 0 ? 5.0 : 3.0) * nk, [&] {
+        if (seg) {
+          seg_fcg_beta<T>(S, w.fz.p, it > 0 ? qp : nullptr, sc, s);
+          seg_fcg_dir<T>(S, n, p, w.fz.p, it > 0 ? pp : nullptr, sc, s);
+        } else {
+          fcg_beta<T>(n, k, w.fz.p, it > 0 ? qp : nullptr, sc, w.fscratch.p, s);
+          fcg_dir<T>(n, k, p, w.fz.p, it > 0 ? pp : nullptr, sc, s);
+        }
+      });
       EpiArgs a;
       a.y = q;
       timed(H, (int)l, LIGMG_KERNEL_SPMV, k, sizeof(T) == 8,
             core_bytes(n, L.A.nnz, n, k, sizeof(T)) + 1.0 * n * k * sizeof(T),
             [&] { spmm<T>(A, p, k, Epi::Store, a, s); });
-      if (seg) {
-        seg_fcg_alpha<T>(S, p, q, r, sc, s);
-        seg_fcg_update<T>(S, n, x, r, p, q, sc.alpha, it + 1 < iters, s);
-      } else {
-        fcg_alpha<T>(n, k, p, q, r, sc, w.fscratch.p, s);
-        fcg_update<T>(n, k, x, r, p, q, sc.alpha, it + 1 < iters, s);
-      }
+      timed(H, (int)l, LIGMG_KERNEL_KRYLOV, k, sizeof(T) == 8, (it + 1 < iters ? 9.0 : 6.0) * nk,
+            [&] {
+              if (seg) {
+                seg_fcg_alpha<T>(S, p, q, r, sc, s);
+                seg_fcg_update<T>(S, n, x, r, p, q, sc.alpha, it + 1 < iters, s);
+              } else {
+                fcg_alpha<T>(n, k, p, q, r, sc, w.fscratch.p, s);
+                fcg_update<T>(n, k, x, r, p, q, sc.alpha, it + 1 < iters, s);
+              }
+            });
       std::swap(p, pp);
       std::swap(q, qp);
       std::swap(sc.eta, sc.eta_prev);
@@ -821,11 +861,19 @@ void finish_level(Handle &H, Level &L) {
   LG_LAUNCH();
   L.lanesA = lanes_for(L.A.nnz, L.A.n);
   L.rp_host = L.A.rp.to_host();
-  L.hubA64.build(L.rp_host.data(), L.A.n, entries_per_step(8, 1), 1, s);
+  L.hubA64.build(L.rp_host.data(), L.A.n, split_unit(8, 1), 1, s);
   if (L.type == LIGMG_LEVEL_ELIM) {
     L.rrp_host = L.elim.R.rp.to_host();
     L.lanesR = lanes_for(L.elim.R.nnz, L.elim.R.n);
     L.lanesP = lanes_for(L.elim.P.nnz, L.elim.P.n);
+  }
+  if (L.type == LIGMG_LEVEL_AGG) {
+    L.rrp_host = L.agg.mrp.to_host();
+    L.lanesR = lanes_for(L.A.n, L.nc);
+    L.ones64.alloc(L.A.n, s);
+    L.ones32.alloc(L.A.n, s);
+    fill_value<double>(L.A.n, L.ones64.p, 1.0, s);
+    fill_value<float>(L.A.n, L.ones32.p, 1.0f, s);
   }
 }
 
@@ -1003,18 +1051,22 @@ void apply_prec_body(Handle &H, int k, size_t base, const double *r, double *z, 
     E.cycle(base, r, z);
   } else {
     LevelWork<T> &w = W.lw[base];
-    convert<double, float>(n * k, r, w.in.p, H.s);
+    timed(H, (int)base, LIGMG_KERNEL_VECTOR, k, 0, 12.0 * n * k,
+          [&] { convert<double, float>(n * k, r, w.in.p, H.s); });
     E.cycle(base, w.in.p, w.out.p);
-    convert<float, double>(n * k, w.out.p, z, H.s);
+    timed(H, (int)base, LIGMG_KERNEL_VECTOR, k, 0, 12.0 * n * k,
+          [&] { convert<float, double>(n * k, w.out.p, z, H.s); });
   }
   const SegInfo S = L.seginfo();
-  if (S.nseg > 0) {  // one constant per graph of the batch
-    seg_sum<double>(S, z, sum, H.s);
-    seg_sub_mean<double>(S, n, z, sum, H.s);
-    return;
-  }
-  col_reduce<double>(n, k, Red::Sum, z, nullptr, sum, scratch, scratch_len, H.s);
-  sub_mean<double>(n, k, z, sum, H.s);
+  timed(H, (int)base, LIGMG_KERNEL_OUTER, k, 1, 24.0 * n * k, [&] {
+    if (S.nseg > 0) {  // one constant per graph of the batch
+      seg_sum<double>(S, z, sum, H.s);
+      seg_sub_mean<double>(S, n, z, sum, H.s);
+      return;
+    }
+    col_reduce<double>(n, k, Red::Sum, z, nullptr, sum, scratch, scratch_len, H.s);
+    sub_mean<double>(n, k, z, sum, H.s);
+  });
 }
 
 // The K-cycle issues thousands of small kernels per application; after one
@@ -1031,6 +1083,7 @@ void apply_prec(Handle &H, int k, size_t base, const double *r, double *z, doubl
   PrecGraph &g = H.pgraphs[std::make_tuple(k, (int)sizeof(T), (int)base)];
   if (g.exec && g.r == r && g.z == z && g.prof == H.prof.on) {
     LG_CUDA(cudaGraphLaunch(g.exec, H.s));
+    add_launches(g.kernels);
     if (H.prof.on)
       for (const ProfRec &t : g.tmpl) H.prof.pending.push_back(t);
     return;
@@ -1040,6 +1093,7 @@ void apply_prec(Handle &H, int k, size_t base, const double *r, double *z, doubl
   cudaGraph_t graph = nullptr;
   H.prof.capture_tmpl.clear();
   H.prof.capturing = H.prof.on;
+  const int64_t c0 = launches_now();
   LG_CUDA(cudaStreamBeginCapture(H.s, cudaStreamCaptureModeThreadLocal));
   try {
     body();
@@ -1047,9 +1101,12 @@ void apply_prec(Handle &H, int k, size_t base, const double *r, double *z, doubl
     cudaStreamEndCapture(H.s, &graph);
     if (graph) cudaGraphDestroy(graph);
     H.prof.capturing = false;
+    add_launches(c0 - launches_now());
     throw;
   }
   H.prof.capturing = false;
+  g.kernels = launches_now() - c0;
+  add_launches(-g.kernels);
   LG_CUDA(cudaStreamEndCapture(H.s, &graph));
   cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
   cudaGraphDestroy(graph);
@@ -1137,8 +1194,11 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
     } else {  // FCG (Notay), one stored direction; fused scalar reductions
       precondition();
       FcgScalars sc{tmp, beta, eta, eta_prev, alpha, w.frozen.p};
-      fcg_beta<double>(n, k, w.Z.p, it > 0 ? QP : nullptr, sc, w.fscratch.p, s);
-      fcg_dir<double>(n, k, P, w.Z.p, it > 0 ? PP : nullptr, sc, s, dfprod ? w.Pdf.p : nullptr);
+      const double nk = 8.0 * n * k;
+      timed(H, (int)base, LIGMG_KERNEL_OUTER, k, 1, (it > 0 ? 5.0 : 3.0) * nk, [&] {
+        fcg_beta<double>(n, k, w.Z.p, it > 0 ? QP : nullptr, sc, w.fscratch.p, s);
+        fcg_dir<double>(n, k, P, w.Z.p, it > 0 ? PP : nullptr, sc, s, dfprod ? w.Pdf.p : nullptr);
+      });
       EpiArgs a;
       a.y = Q;
       timed(H, (int)base, LIGMG_KERNEL_SPMV, k, 1, core_bytes(n, L.A.nnz, n, k, 8) + 8.0 * n * k,
@@ -1146,13 +1206,16 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
               if (dfprod) spmm_df(A, L.Adf.p, w.Pdf.p, k, Q, s);
               else spmm<double>(A, P, k, Epi::Store, a, s);
             });
-      fcg_alpha<double>(n, k, P, Q, w.R.p, sc, w.fscratch.p, s);
-      fcg_update<double>(n, k, w.X.p, w.R.p, P, Q, alpha, true, s);
+      timed(H, (int)base, LIGMG_KERNEL_OUTER, k, 1, 9.0 * nk, [&] {
+        fcg_alpha<double>(n, k, P, Q, w.R.p, sc, w.fscratch.p, s);
+        fcg_update<double>(n, k, w.X.p, w.R.p, P, Q, alpha, true, s);
+      });
       std::swap(P, PP);
       std::swap(Q, QP);
       std::swap(eta, eta_prev);
     }
-    col_dot1<double>(n, k, w.R.p, w.R.p, rn2, w.fscratch.p, s);
+    timed(H, (int)base, LIGMG_KERNEL_OUTER, k, 1, 8.0 * n * k,
+          [&] { col_dot1<double>(n, k, w.R.p, w.R.p, rn2, w.fscratch.p, s); });
     LG_CUDA(cudaMemcpyAsync(h_rn2.data(), rn2, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
     LG_CUDA(cudaStreamSynchronize(s));
     if (H.prof.on) H.prof.collect();  // graph replays re-record the same events
@@ -1247,9 +1310,10 @@ SolveResult outer_solve_seg(Handle &H, size_t base, OuterWork &w) {
   seg_converge(ns, so.rn0sq.p, so.rn0sq.p, 0.0, -1, so.frozen.p, so.iters.p, s);  // b = 0
   // direct run of one cycle: creates every lazily built plan and buffer
   apply_prec_body<T>(H, 1, base, w.R.p, w.Z.p, so.sc.p, w.scratch.p, w.scratch_len);
-  auto capture = [&](int it0) {
+  auto capture = [&](int it0, int64_t &kernels) {
     cudaGraph_t g = nullptr;
     cudaGraphExec_t e = nullptr;
+    const int64_t c0 = launches_now();
     LG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     H.prof.suspended = true;
     try {
@@ -1259,9 +1323,12 @@ SolveResult outer_solve_seg(Handle &H, size_t base, OuterWork &w) {
       H.prof.suspended = false;
       cudaStreamEndCapture(s, &g);
       if (g) cudaGraphDestroy(g);
+      add_launches(c0 - launches_now());
       throw;
     }
     H.prof.suspended = false;
+    kernels = launches_now() - c0;
+    add_launches(-kernels);
     LG_CUDA(cudaStreamEndCapture(s, &g));
     cudaError_t err = cudaGraphInstantiate(&e, g, 0);
     cudaGraphDestroy(g);
@@ -1271,8 +1338,8 @@ SolveResult outer_solve_seg(Handle &H, size_t base, OuterWork &w) {
   if (!H.batch_first || H.batch_base != base) {
     if (H.batch_first) cudaGraphExecDestroy(H.batch_first);
     if (H.batch_more) cudaGraphExecDestroy(H.batch_more);
-    H.batch_first = capture(0);
-    H.batch_more = capture(kGraphIters);
+    H.batch_first = capture(0, H.batch_first_kernels);
+    H.batch_more = capture(kGraphIters, H.batch_more_kernels);
     H.batch_base = base;
   }
   SolveResult res;
@@ -1280,6 +1347,7 @@ SolveResult outer_solve_seg(Handle &H, size_t base, OuterWork &w) {
   int done = 0;
   for (int launch = 0; done < H.opts.iters; launch++) {
     LG_CUDA(cudaGraphLaunch(launch == 0 ? H.batch_first : H.batch_more, s));
+    add_launches(launch == 0 ? H.batch_first_kernels : H.batch_more_kernels);
     done += kGraphIters;
     LG_CUDA(cudaMemcpyAsync(fz.data(), so.frozen.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, s));
     LG_CUDA(cudaStreamSynchronize(s));

@@ -30,14 +30,27 @@ inline void cuda_check(cudaError_t e, const char *what) {
     throw Error(LIGMG_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
   throw Error(LIGMG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
-// kernels launched by the library (every launch site calls LG_LAUNCH once)
+// kernels launched by the library (every launch site calls LG_LAUNCH once;
+// a launch recorded into a CUDA graph is taken back out at capture and
+// counted again on every replay of the graph)
 extern int64_t g_launches;
+inline int64_t launches_now() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+inline void add_launches(int64_t d) { __atomic_fetch_add(&g_launches, d, __ATOMIC_RELAXED); }
 #define LG_CUDA(x) ::lg::cuda_check((x), #x)
 #define LG_LAUNCH()                                             \
   do {                                                          \
     __atomic_fetch_add(&::lg::g_launches, 1, __ATOMIC_RELAXED); \
     ::lg::cuda_check(cudaGetLastError(), "kernel launch");      \
   } while (0)
+
+// While set (by SyncFreeScope, in this thread), DBuf::release frees with a
+// synchronous cudaFree instead of a free ordered on the buffer's stream.
+extern thread_local bool g_free_sync;
+struct SyncFreeScope {
+  bool prev;
+  SyncFreeScope() : prev(g_free_sync) { g_free_sync = true; }
+  ~SyncFreeScope() { g_free_sync = prev; }
+};
 
 constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
 
@@ -77,7 +90,10 @@ struct DBuf {
     if (count > 0) LG_CUDA(cudaMallocAsync((void **)&p, sizeof(T) * (size_t)count, st));
   }
   void release() {
-    if (p) cudaFreeAsync(p, s);
+    if (p) {
+      if (g_free_sync) cudaFree(p);
+      else cudaFreeAsync(p, s);
+    }
     p = nullptr;
     n = 0;
   }

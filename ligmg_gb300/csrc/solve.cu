@@ -13,7 +13,7 @@
 namespace lg {
 
 // ---------------------------------------------------------------------------
-int entries_per_step(int value_bytes, int k) {
+int split_unit(int value_bytes, int k) {
   int W = value_bytes == 4 ? 4 : 2;
   int VW = (k % W == 0) ? W : 1;
   int L = std::max(1, k / VW);
@@ -363,15 +363,9 @@ __global__ void k_cheb_init_zero(i64 n, int k, const T *b, const T *invd, T thet
 }
 
 template <typename T>
-__global__ void k_restrict_agg(i64 nc, int k, const i64 *mrp, const i32 *members, const T *r,
-                               T *bc) {
+__global__ void k_fill(i64 cnt, T *x, T v) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nc * k) return;
-  i64 I = t / k;
-  int c = (int)(t % k);
-  T s = 0;
-  for (i64 m = mrp[I]; m < mrp[I + 1]; m++) s += r[(i64)members[m] * k + c];
-  bc[t] = s;
+  if (t < cnt) x[t] = v;
 }
 
 template <typename T>
@@ -1005,9 +999,9 @@ void cheb_init_zero(i64 n, int k, const T *b, const T *invd, double theta, T *d,
   LG_LAUNCH();
 }
 template <typename T>
-void restrict_agg(i64 nc, int k, const i64 *mrp, const i32 *members, const T *r, T *bc,
-                  cudaStream_t s) {
-  k_restrict_agg<T><<<grid_for(nc * k, 256), 256, 0, s>>>(nc, k, mrp, members, r, bc);
+void fill_value(i64 cnt, T *x, T v, cudaStream_t s) {
+  if (cnt <= 0) return;
+  k_fill<T><<<grid_for(cnt, 256), 256, 0, s>>>(cnt, x, v);
   LG_LAUNCH();
 }
 template <typename T>
@@ -1102,8 +1096,7 @@ void scal_beta(int k, const double *zq, const double *eta_prev, double *beta, cu
                              cudaStream_t);                                                    \
   template void col_dot1<T>(i64, int, const T *, const T *, double *, double *, cudaStream_t); \
   template void cheb_init_zero<T>(i64, int, const T *, const T *, double, T *, cudaStream_t); \
-  template void restrict_agg<T>(i64, int, const i64 *, const i32 *, const T *, T *,          \
-                                cudaStream_t);                                                 \
+  template void fill_value<T>(i64, T *, T, cudaStream_t);                                    \
   template void prolong_agg<T>(i64, int, const i32 *, const T *, T *, cudaStream_t);         \
   template void coarse_apply<T>(i64, int, const T *, const T *, T *, cudaStream_t);          \
   template void scale_vec<T>(i64, int, T *, double, cudaStream_t);                           \

@@ -26,8 +26,8 @@ struct MatView {
 };
 
 // Hub-row schedule owned by a level (built once at setup).
-// A row is split when it needs more than 64 warp steps (E nonzeros per step),
-// into at most 256 chunks of at least 32 steps.
+// A row is split when it holds more than 64 units of U nonzeros, into at most
+// 256 chunks of at least 32 units (U from split_unit).
 template <typename T>
 struct HubPlan {
   i64 thresh = 0, nchunks = 0, nhubs = 0;
@@ -37,11 +37,12 @@ struct HubPlan {
   DBuf<T> partial;
   int kcap = 0;
   bool built = false;
-  void build(const i64 *rp_host, i64 n, int entries_per_step, int kmax, cudaStream_t s);
+  void build(const i64 *rp_host, i64 n, int unit, int kmax, cudaStream_t s);
   void fill(MatView<T> &m) const;
 };
-// nonzeros a 32-lane group advances per step for k right-hand sides
-int entries_per_step(int value_bytes, int k);
+// Hub split unit U for k right-hand sides: the nonzeros a 32-lane group
+// advances per step (E = 32 / (k / VW) entry slots).
+int split_unit(int value_bytes, int k);
 
 enum class Epi {
   Store,       // y = A x
@@ -85,8 +86,7 @@ void split_df(i64 count, const double *v, float2 *out, cudaStream_t s);
 template <typename T>
 void cheb_init_zero(i64 n, int k, const T *b, const T *invd, double theta, T *d, cudaStream_t s);
 template <typename T>
-void restrict_agg(i64 nc, int k, const i64 *mrp, const i32 *members, const T *r, T *bc,
-                  cudaStream_t s);
+void fill_value(i64 cnt, T *x, T v, cudaStream_t s);
 template <typename T>
 void prolong_agg(i64 n, int k, const i32 *agg, const T *xc, T *x, cudaStream_t s);
 template <typename T>
