@@ -396,6 +396,9 @@ def run_ours(args):
             "profile_ms_per_step_by_level": by_key(stats, "level", args.steps),
             "profile_ms_per_step_by_kind": by_key(stats, "kind", args.steps),
             "profiled_ms_per_step": profiled_ms / args.steps,
+            "profile_table": [[r["level"], r["kind"], round(r["launches"] / args.steps, 1),
+                               round(r["seconds"] * 1e3 / args.steps, 3)]
+                              for r in sorted(stats, key=lambda r: -r["seconds"])],
         },
         "roofline": roof,
         "cpu_baseline": cpu,
