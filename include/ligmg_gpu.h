@@ -125,6 +125,12 @@ typedef struct ligmg_options {
   int32_t device;             /* CUDA device ordinal (0) */
   int32_t use_graphs;         /* 1: replay each preconditioner application
                                  from a captured CUDA graph (default 1) */
+  int32_t autotune;           /* 1: on first use of each (level, precision,
+                                 k), time the SpMM launch shapes (block size,
+                                 hub chunk size, lanes per row) on that
+                                 level and keep the fastest; 0: fixed
+                                 defaults, identical launch shapes on every
+                                 run (default 1) */
 } ligmg_options;
 
 /* ConvergenceInfo (util.hpp:143-170) of one solve.  For a batched solve the

@@ -74,6 +74,7 @@ class Options(C.Structure):
         ("verbose", C.c_int32),
         ("device", C.c_int32),
         ("use_graphs", C.c_int32),
+        ("autotune", C.c_int32),
     ]
 
 
@@ -137,6 +138,7 @@ def default_options(**overrides) -> Options:
     o.verbose = 0
     o.device = 0
     o.use_graphs = 1
+    o.autotune = 1
     for k, v in overrides.items():
         if k in ("smoother_type",) and isinstance(v, str):
             v = SMOOTHER[v]

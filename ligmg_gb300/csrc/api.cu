@@ -182,6 +182,7 @@ struct Level {
   mutable std::map<int, HubPlan<float>> hA32k, hR32k;
   std::vector<i64> rp_host, rrp_host;
   int lanesA = 32, lanesR = 32, lanesP = 4;
+  bool autotune = true;  // options.autotune at creation
   // Chebyshev coefficients
   double theta = 1, delta = 1;
   std::vector<double> c1, c2;
@@ -228,16 +229,111 @@ std::map<int, HubPlan<float>> &plans<float>(const Level &L, bool isR) {
 }
 
 template <typename T>
+const T *valsA(const Level &L);
+template <typename T>
+const T *valsR(const Level &L);
+
+// The level's matrix (isR: its restriction) without a hub plan.
+template <typename T>
+MatView<T> bare_view(const Level &L, bool isR) {
+  MatView<T> m;
+  if (!isR) {
+    m.n = L.A.n; m.rp = L.A.rp.p; m.ci = L.A.ci.p; m.v = valsA<T>(L); m.lanes_per_row = L.lanesA;
+  } else if (L.type == LIGMG_LEVEL_AGG) {
+    m.n = L.nc; m.rp = L.agg.mrp.p; m.ci = L.agg.members.p; m.v = valsR<T>(L);
+    m.lanes_per_row = L.lanesR;
+  } else {
+    m.n = L.elim.R.n; m.rp = L.elim.R.rp.p; m.ci = L.elim.R.ci.p; m.v = valsR<T>(L);
+    m.lanes_per_row = L.lanesR;
+  }
+  return m;
+}
+
+// SpMM launch-shape autotuner.  On first use of a (level, matrix, precision,
+// k), every candidate shape is timed on this level's own matrix (y = A x,
+// x = 0, one warm-up and three timed launches on the handle's stream) and the
+// fastest is kept with the plan:
+//   hub chunk size   split unit x {1, 2, 4}: long rows stay whole longer on
+//                    levels with many rows, are cut finer on small levels
+//   threads/block    {64, 128, 256}: small blocks free their slot as soon as
+//                    their rows finish (rows differ widely in length)
+//   lanes per row    {4, 8, 16, 32} for k = 1 on levels without hub rows
+// The choice only changes launch shapes and, on hub rows, how a row's sum is
+// split into chunk partials (its rounding); autotune = 0 uses the defaults
+// (factor 1, 64 threads for k > 1, 256 for k = 1, the level's lanes).
+template <typename T>
+void build_plan(const Level &L, bool isR, int k, HubPlan<T> &best, bool autotune,
+                cudaStream_t s) {
+  const std::vector<i64> &rp = isR ? L.rrp_host : L.rp_host;
+  const i64 n = (i64)rp.size() - 1;
+  const int unit = split_unit(sizeof(T), k);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  LG_CUDA(cudaStreamIsCapturing(s, &cs));
+  if (!autotune || cs != cudaStreamCaptureStatusNone || n <= 0) {
+    best.build(rp.data(), n, unit, k, s);
+    best.tb = k > 1 ? 64 : 256;
+    return;
+  }
+  const MatView<T> base = bare_view<T>(L, isR);
+  DBuf<T> X(L.A.n * k, s), Y(n * k, s);
+  X.zero();
+  cudaEvent_t e0, e1;
+  LG_CUDA(cudaEventCreate(&e0));
+  LG_CUDA(cudaEventCreate(&e1));
+  float best_ms = 1e30f;
+  bool have = false;
+  bool chunks_seen = true;
+  for (int f : {1, 2, 4}) {
+    if (!chunks_seen) break;  // no hub rows at a smaller unit: none at larger ones
+    HubPlan<T> cand;
+    cand.build(rp.data(), n, unit * f, k, s);
+    chunks_seen = cand.nchunks > 0;
+    std::vector<int> lane_opts{0};
+    if (k == 1 && cand.nchunks == 0) lane_opts = {4, 8, 16, 32};
+    float cand_ms = 1e30f;
+    int cand_tb = 256, cand_lanes = 0;
+    for (int lanes : lane_opts)
+      for (int tb : {64, 128, 256}) {
+        MatView<T> m = base;
+        cand.fill(m);
+        m.tb = tb;
+        if (lanes) m.lanes_per_row = lanes;
+        EpiArgs a;
+        a.y = Y.p;
+        spmm<T>(m, X.p, k, Epi::Store, a, s);
+        LG_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < 3; r++) spmm<T>(m, X.p, k, Epi::Store, a, s);
+        LG_CUDA(cudaEventRecord(e1, s));
+        LG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        LG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < cand_ms) {
+          cand_ms = ms;
+          cand_tb = tb;
+          cand_lanes = lanes;
+        }
+      }
+    if (!have || cand_ms < best_ms) {
+      best = std::move(cand);
+      best.tb = cand_tb;
+      best.lanes = cand_lanes;
+      best.factor = f;
+      best_ms = cand_ms;
+      have = true;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  LG_CUDA(cudaStreamSynchronize(s));
+}
+
+template <typename T>
 const HubPlan<T> &plan_for(const Level &L, bool isR, int k, cudaStream_t s) {
   if constexpr (sizeof(T) == 8) {
     if (!isR && k == 1) return L.hubA64;
   }
   HubPlan<T> &p = plans<T>(L, isR)[k];
-  if (!p.built) {
-    const std::vector<i64> &rp = isR ? L.rrp_host : L.rp_host;
-    i64 n = (i64)rp.size() - 1;
-    p.build(rp.data(), n, split_unit(sizeof(T), k), k, s);
-  }
+  if (!p.built) build_plan<T>(L, isR, k, p, L.autotune, s);
   return p;
 }
 
@@ -258,21 +354,13 @@ const T *valsR(const Level &L) {
 
 template <typename T>
 MatView<T> viewA(const Level &L, int k, cudaStream_t s) {
-  MatView<T> m;
-  m.n = L.A.n; m.rp = L.A.rp.p; m.ci = L.A.ci.p; m.v = valsA<T>(L); m.lanes_per_row = L.lanesA;
+  MatView<T> m = bare_view<T>(L, false);
   plan_for<T>(L, false, k, s).fill(m);
   return m;
 }
 template <typename T>
 MatView<T> viewR(const Level &L, int k, cudaStream_t s) {
-  MatView<T> m;
-  if (L.type == LIGMG_LEVEL_AGG) {
-    m.n = L.nc; m.rp = L.agg.mrp.p; m.ci = L.agg.members.p;
-  } else {
-    m.n = L.elim.R.n; m.rp = L.elim.R.rp.p; m.ci = L.elim.R.ci.p;
-  }
-  m.v = valsR<T>(L);
-  m.lanes_per_row = L.lanesR;
+  MatView<T> m = bare_view<T>(L, true);
   plan_for<T>(L, true, k, s).fill(m);
   return m;
 }
@@ -860,6 +948,7 @@ void finish_level(Handle &H, Level &L) {
   k_invdiag<<<grid_for(L.A.n, 256), 256, 0, s>>>(L.A.rp.p, L.A.ci.p, L.A.v.p, L.A.n, L.invd.p);
   LG_LAUNCH();
   L.lanesA = lanes_for(L.A.nnz, L.A.n);
+  L.autotune = H.opts.autotune != 0;
   L.rp_host = L.A.rp.to_host();
   L.hubA64.build(L.rp_host.data(), L.A.n, split_unit(8, 1), 1, s);
   if (L.type == LIGMG_LEVEL_ELIM) {
@@ -1547,6 +1636,7 @@ void ligmg_default_options(ligmg_options *o) {
   o->verbose = 0;
   o->device = 0;
   o->use_graphs = 1;
+  o->autotune = 1;
 }
 
 const char *ligmg_status_string(ligmg_status s) {

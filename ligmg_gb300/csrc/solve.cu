@@ -77,6 +77,8 @@ void HubPlan<T>::fill(MatView<T> &m) const {
   m.ch_cnt = cnt.p;
   m.hub_counter = counter.p;
   m.partial = partial.p;
+  m.tb = tb;
+  if (lanes > 0) m.lanes_per_row = lanes;
 }
 template struct HubPlan<float>;
 template struct HubPlan<double>;
@@ -302,7 +304,8 @@ void launch_spmm(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t
   constexpr int RPW = 32 / G;
   i64 warps = cdiv(A.n, RPW) + ((G == 32) ? A.nchunks : 0);
   if (warps == 0) return;
-  k_spmm<T, K, G, EP><<<grid_for(warps * 32, 256), 256, 0, s>>>(A, X, a);
+  const int tb = (A.tb == 64 || A.tb == 128) ? A.tb : 256;
+  k_spmm<T, K, G, EP><<<grid_for(warps * 32, tb), tb, 0, s>>>(A, X, a);
   LG_LAUNCH();
 }
 

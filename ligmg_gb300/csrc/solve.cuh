@@ -23,6 +23,7 @@ struct MatView {
   int *hub_counter = nullptr;  // one per hub row, zero between launches
   T *partial = nullptr;        // nchunks x K
   int lanes_per_row = 32;      // 4, 8, 16 or 32 (single-RHS layout)
+  int tb = 256;                // threads per block of the launch (64, 128 or 256)
 };
 
 // Hub-row schedule owned by a level (built once at setup).
@@ -37,6 +38,10 @@ struct HubPlan {
   DBuf<T> partial;
   int kcap = 0;
   bool built = false;
+  // launch shape kept with the plan (picked by the autotuner or defaults)
+  int tb = 256;    // threads per block
+  int lanes = 0;   // lanes per row for k = 1 (0: the level's default)
+  int factor = 1;  // split unit multiplier the chunks were built with
   void build(const i64 *rp_host, i64 n, int unit, int kmax, cudaStream_t s);
   void fill(MatView<T> &m) const;
 };

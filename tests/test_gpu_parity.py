@@ -172,11 +172,29 @@ def test_batched_matches_single(prec, k):
 def test_graph_replay_matches_direct_launches():
     L = GRAPHS["rmat14"]()
     B = G.rhs(L.n, k=8, seed=3)
-    kw = dict(precision="fp32", kcycle=1, outer_ksp_type="fcg")
+    # fixed launch shapes: two handles then run identical kernels
+    kw = dict(precision="fp32", kcycle=1, outer_ksp_type="fcg", autotune=0)
     a = Solver(L, **kw).solve_batched(B)
     b = Solver(L, use_graphs=0, **kw).solve_batched(B)
     assert a.iters() == b.iters()
     assert np.array_equal(a.solution, b.solution)
+
+
+def test_autotuned_shapes_match_fixed_shapes():
+    # the tuner changes launch shapes and hub-row chunking only: same
+    # iterations, solutions equal to rounding
+    L = GRAPHS["rmat14"]()
+    B = G.rhs(L.n, k=32, seed=5)
+    kw = dict(precision="fp32", kcycle=1, outer_ksp_type="fcg")
+    a = Solver(L, autotune=1, **kw).solve_batched(B)
+    b = Solver(L, autotune=0, **kw).solve_batched(B)
+    assert a.converged and b.converged
+    assert abs(a.iters() - b.iters()) <= 1
+    assert _relerr(a.solution, b.solution) <= 1e-6
+    c = Solver(L, autotune=1, precision="fp64", kcycle=1, outer_ksp_type="fcg")
+    x1 = c.solve(B[:, 0].copy())
+    x2 = c.solve(B[:, 0].copy())  # same handle, same tuned plans: identical
+    assert np.array_equal(x1.solution, x2.solution)
 
 
 def test_profiled_solve_reports_kernels():
@@ -259,10 +277,11 @@ def test_cycle_on_imported_oracle_hierarchy(name, tmp_path):
 
 def test_gpu_dump_import_round_trip(tmp_path):
     L = GRAPHS["rmat12"]()
-    S = Solver(L, kcycle=1, outer_ksp_type="fcg")
+    S = Solver(L, kcycle=1, outer_ksp_type="fcg", autotune=0)
     S.dump_hierarchy(str(tmp_path))
     from ligmg_gb300 import petsc_io
-    T = Solver.import_hierarchy(petsc_io.load(tmp_path), kcycle=1, outer_ksp_type="fcg")
+    T = Solver.import_hierarchy(petsc_io.load(tmp_path), kcycle=1, outer_ksp_type="fcg",
+                                autotune=0)
     b = G.rhs(L.n, seed=8)
     a, c = S.solve(b), T.solve(b)
     assert a.iters() == c.iters() and np.array_equal(a.solution, c.solution)
