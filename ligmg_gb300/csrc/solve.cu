@@ -440,12 +440,22 @@ __global__ void __launch_bounds__(256) k_colred(i64 n, int k, const T *x, const 
   }
 }
 
-__global__ void k_colred_final(int nb, int width, const double *part, double *out) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= width) return;
+// one block per output column: 128 threads take strided block partials, then
+// a fixed shared-memory tree (deterministic order)
+__global__ void __launch_bounds__(128) k_colred_final(int nb, int width, const double *part,
+                                                      double *out) {
+  __shared__ double sh[128];
+  const int j = blockIdx.x, tid = threadIdx.x;
   double s = 0;
-  for (int b = 0; b < nb; b++) s += part[(i64)b * width + j];
-  out[j] = s;
+#pragma unroll 4
+  for (int b = tid; b < nb; b += 128) s += part[(i64)b * width + j];
+  sh[tid] = s;
+  __syncthreads();
+  for (int st = 64; st >= 1; st >>= 1) {
+    if (tid < st) sh[tid] += sh[tid + st];
+    __syncthreads();
+  }
+  if (tid == 0) out[j] = sh[0];
 }
 
 int colred_blocks(i64 n, int k) {
@@ -567,13 +577,31 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   if (!last) return;
   __threadfence();
+  {
+    // all 256 threads: column c, block partials rsub, rsub + rstride, ...; then
+    // the same fixed tree over the slots (deterministic order)
+    double tb[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) tb[v] = 0;
+#pragma unroll 4
+    for (unsigned b = rsub; b < gridDim.x; b += rstride)
+#pragma unroll
+      for (int v = 0; v < NV; v++) tb[v] += __ldcg(part + ((i64)b * NV + v) * k + c);
+    __syncthreads();
+#pragma unroll
+    for (int v = 0; v < NV; v++) sh[v][tid] = tb[v];
+    __syncthreads();
+    for (int st = 128; st >= k; st >>= 1) {
+      if (tid < st)
+#pragma unroll
+        for (int v = 0; v < NV; v++) sh[v][tid] += sh[v][tid + st];
+      __syncthreads();
+    }
+  }
   if (tid < k) {
     double tot[NV];
 #pragma unroll
-    for (int v = 0; v < NV; v++) tot[v] = 0;
-    for (unsigned b = 0; b < gridDim.x; b++)
-#pragma unroll
-      for (int v = 0; v < NV; v++) tot[v] += __ldcg(part + ((i64)b * NV + v) * k + tid);
+    for (int v = 0; v < NV; v++) tot[v] = sh[v][tid];
     if constexpr (OP == 0 || OP == 1) {
       out[tid] = tot[0];
     } else if constexpr (OP == 2) {
@@ -1048,7 +1076,7 @@ void col_reduce(i64 n, int k, Red op, const T *x, const T *y, double *out, doubl
       break;
   }
   LG_LAUNCH();
-  k_colred_final<<<(width + 127) / 128, 128, 0, s>>>(nb, width, scratch, out);
+  k_colred_final<<<width, 128, 0, s>>>(nb, width, scratch, out);
   LG_LAUNCH();
 }
 
