@@ -402,31 +402,48 @@ __global__ void k_convert(i64 cnt, const S *src, D *dst) {
   if (t < cnt) dst[t] = (D)src[t];
 }
 
-// column reductions
-template <typename T, int OP>
-__global__ void __launch_bounds__(256) k_colred(i64 n, int k, const T *x, const T *y,
+// column reductions.  Thread t of a BS-thread block takes column t % k and
+// rows t / k, t / k + BS / k, ... (four rows per pass, loads issued first).
+// Large inputs (>= 2^20 elements): one 1024-thread block per SM at most, so
+// few block partials remain for the final pass; smaller inputs: 256-thread
+// blocks (shorter trees, more blocks).
+constexpr int kRedBS = 1024;
+constexpr i64 kRedBig = i64(1) << 20;
+template <typename T, int OP, int BS>
+__global__ void __launch_bounds__(BS) k_colred(i64 n, int k, const T *x, const T *y,
                                                 i64 rows_per_block, double *part) {
-  __shared__ double sh0[256], sh1[256];
+  __shared__ double sh0[BS], sh1[BS];
   const int tid = threadIdx.x;
-  const int c = tid % k, rsub = tid / k, rstride = 256 / k;
+  const int c = tid % k, rsub = tid / k, rstride = BS / k;
   const i64 r0 = (i64)blockIdx.x * rows_per_block;
   const i64 r1 = min(n, r0 + rows_per_block);
   double a0 = 0, a1 = 0;
-  for (i64 r = r0 + rsub; r < r1; r += rstride) {
-    double xv = (double)x[r * k + c];
-    if constexpr (OP == 0) {
-      a0 += xv;
-    } else if constexpr (OP == 1) {
-      a0 += xv * (double)y[r * k + c];
-    } else {
-      a0 += xv;
-      a1 += xv * (double)y[r * k + c];
+  for (i64 r = r0 + rsub; r < r1; r += 4 * (i64)rstride) {
+    T xv[4], yv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const i64 rr = r + (i64)u * rstride;
+      const bool ok = rr < r1;
+      xv[u] = ok ? x[rr * k + c] : (T)0;
+      if constexpr (OP != 0) yv[u] = ok ? y[rr * k + c] : (T)0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const double xd = (double)xv[u];
+      if constexpr (OP == 0) {
+        a0 += xd;
+      } else if constexpr (OP == 1) {
+        a0 += xd * (double)yv[u];
+      } else {
+        a0 += xd;
+        a1 += xd * (double)yv[u];
+      }
     }
   }
   sh0[tid] = a0;
   sh1[tid] = a1;
   __syncthreads();
-  for (int s = 128; s >= k; s >>= 1) {
+  for (int s = BS / 2; s >= k; s >>= 1) {
     if (tid < s) {
       sh0[tid] += sh0[tid + s];
       sh1[tid] += sh1[tid + s];
@@ -458,9 +475,11 @@ __global__ void __launch_bounds__(128) k_colred_final(int nb, int width, const d
   if (tid == 0) out[j] = sh[0];
 }
 
+int red_threads(i64 n, int k) { return n * k >= kRedBig ? kRedBS : 256; }
 int colred_blocks(i64 n, int k) {
-  i64 nb = cdiv(n * k, 256 * 8);
-  return (int)std::max<i64>(1, std::min<i64>(nb, 4 * kSMs));
+  if (n * k >= kRedBig)
+    return (int)std::max<i64>(1, std::min<i64>(cdiv(n * k, (i64)kRedBS * 16), kSMs));
+  return (int)std::max<i64>(1, std::min<i64>(cdiv(n * k, 256 * 8), 2 * kSMs));
 }
 
 template <typename T>
@@ -522,43 +541,59 @@ __global__ void k_scal_beta(int k, const double *zq, const double *eta_prev, dou
 // ---- fused reductions ------------------------------------------------------
 // OP 0: [sum x]            OP 1: [sum x.y]
 // OP 2: [sum x, sum x.y, sum y]   (FCG beta)     OP 3: [sum x.y, sum x.w]  (alpha)
-template <typename T, int OP>
-__global__ void __launch_bounds__(256)
+template <typename T, int OP, int BS>
+__global__ void __launch_bounds__(BS)
     k_fused_red(i64 n, int k, const T *x, const T *y, const T *w, i64 rows_per_block,
                 double *scratch, FcgScalars sc, double *out) {
   constexpr int NV = (OP == 2) ? 3 : (OP == 3 ? 2 : 1);
-  __shared__ double sh[NV][256];
+  __shared__ double sh[NV][BS];
   __shared__ int last;
   const int tid = threadIdx.x;
-  const int c = tid % k, rsub = tid / k, rstride = 256 / k;
+  const int c = tid % k, rsub = tid / k, rstride = BS / k;
   const i64 r0 = (i64)blockIdx.x * rows_per_block;
   const i64 r1 = min(n, r0 + rows_per_block);
   double a[NV];
 #pragma unroll
   for (int v = 0; v < NV; v++) a[v] = 0;
-  for (i64 r = r0 + rsub; r < r1; r += rstride) {
-    const i64 o = r * k + c;
-    double xv = (double)x[o];
-    if constexpr (OP == 0) {
-      a[0] += xv;
-    } else if constexpr (OP == 1) {
-      a[0] += xv * (double)y[o];
-    } else if constexpr (OP == 2) {
-      a[0] += xv;
-      if (y) {
-        double yv = (double)y[o];
-        a[1] += xv * yv;
-        a[2] += yv;
+  // four rows per pass, all loads issued before the (row-ordered) adds
+  constexpr bool HAS_Y = OP != 0;
+  constexpr bool HAS_W = OP == 3;
+  const bool use_y = HAS_Y && y != nullptr;
+  for (i64 r = r0 + rsub; r < r1; r += 4 * (i64)rstride) {
+    T xv[4], yv[4], wv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const i64 rr = r + (i64)u * rstride;
+      const bool ok = rr < r1;
+      const i64 o = rr * k + c;
+      xv[u] = ok ? x[o] : (T)0;
+      yv[u] = (ok && use_y) ? y[o] : (T)0;
+      if constexpr (HAS_W) wv[u] = ok ? w[o] : (T)0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const double xd = (double)xv[u];
+      if constexpr (OP == 0) {
+        a[0] += xd;
+      } else if constexpr (OP == 1) {
+        a[0] += xd * (double)yv[u];
+      } else if constexpr (OP == 2) {
+        a[0] += xd;
+        if (use_y) {
+          const double yd = (double)yv[u];
+          a[1] += xd * yd;
+          a[2] += yd;
+        }
+      } else {
+        a[0] += xd * (double)yv[u];
+        a[1] += xd * (double)wv[u];
       }
-    } else {
-      a[0] += xv * (double)y[o];
-      a[1] += xv * (double)w[o];
     }
   }
 #pragma unroll
   for (int v = 0; v < NV; v++) sh[v][tid] = a[v];
   __syncthreads();
-  for (int st = 128; st >= k; st >>= 1) {
+  for (int st = BS / 2; st >= k; st >>= 1) {
     if (tid < st)
 #pragma unroll
       for (int v = 0; v < NV; v++) sh[v][tid] += sh[v][tid + st];
@@ -578,7 +613,7 @@ __global__ void __launch_bounds__(256)
   if (!last) return;
   __threadfence();
   {
-    // all 256 threads: column c, block partials rsub, rsub + rstride, ...; then
+    // all threads: column c, block partials rsub, rsub + rstride, ...; then
     // the same fixed tree over the slots (deterministic order)
     double tb[NV];
 #pragma unroll
@@ -591,7 +626,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int v = 0; v < NV; v++) sh[v][tid] = tb[v];
     __syncthreads();
-    for (int st = 128; st >= k; st >>= 1) {
+    for (int st = BS / 2; st >= k; st >>= 1) {
       if (tid < st)
 #pragma unroll
         for (int v = 0; v < NV; v++) sh[v][tid] += sh[v][tid + st];
@@ -800,8 +835,7 @@ __global__ void k_split_df(i64 cnt, const double *v, float2 *o) {
 }
 
 int fused_blocks(i64 n, int k) {
-  i64 nb = cdiv(n * k, 256 * 8);
-  return (int)std::max<i64>(1, std::min<i64>(nb, 2 * kSMs));
+  return colred_blocks(n, k);
 }
 
 }  // namespace
@@ -972,7 +1006,10 @@ template <typename T>
 void fcg_beta(i64 n, int k, const T *z, const T *qp, FcgScalars sc, double *scratch,
               cudaStream_t s) {
   int nb = fused_blocks(n, k);
-  k_fused_red<T, 2><<<nb, 256, 0, s>>>(n, k, z, qp, nullptr, cdiv(n, nb), scratch, sc, nullptr);
+  if (red_threads(n, k) == kRedBS)
+    k_fused_red<T, 2, kRedBS><<<nb, kRedBS, 0, s>>>(n, k, z, qp, nullptr, cdiv(n, nb), scratch, sc, nullptr);
+  else
+    k_fused_red<T, 2, 256><<<nb, 256, 0, s>>>(n, k, z, qp, nullptr, cdiv(n, nb), scratch, sc, nullptr);
   LG_LAUNCH();
 }
 template <typename T>
@@ -1013,14 +1050,20 @@ template <typename T>
 void fcg_alpha(i64 n, int k, const T *p, const T *q, const T *r, FcgScalars sc,
                double *scratch, cudaStream_t s) {
   int nb = fused_blocks(n, k);
-  k_fused_red<T, 3><<<nb, 256, 0, s>>>(n, k, p, q, r, cdiv(n, nb), scratch, sc, nullptr);
+  if (red_threads(n, k) == kRedBS)
+    k_fused_red<T, 3, kRedBS><<<nb, kRedBS, 0, s>>>(n, k, p, q, r, cdiv(n, nb), scratch, sc, nullptr);
+  else
+    k_fused_red<T, 3, 256><<<nb, 256, 0, s>>>(n, k, p, q, r, cdiv(n, nb), scratch, sc, nullptr);
   LG_LAUNCH();
 }
 template <typename T>
 void col_dot1(i64 n, int k, const T *x, const T *y, double *out, double *scratch, cudaStream_t s) {
   int nb = fused_blocks(n, k);
   FcgScalars none{};
-  k_fused_red<T, 1><<<nb, 256, 0, s>>>(n, k, x, y, nullptr, cdiv(n, nb), scratch, none, out);
+  if (red_threads(n, k) == kRedBS)
+    k_fused_red<T, 1, kRedBS><<<nb, kRedBS, 0, s>>>(n, k, x, y, nullptr, cdiv(n, nb), scratch, none, out);
+  else
+    k_fused_red<T, 1, 256><<<nb, 256, 0, s>>>(n, k, x, y, nullptr, cdiv(n, nb), scratch, none, out);
   LG_LAUNCH();
 }
 
@@ -1063,15 +1106,23 @@ template <typename T>
 void col_reduce(i64 n, int k, Red op, const T *x, const T *y, double *out, double *scratch,
                 i64 scratch_len, cudaStream_t s) {
   if (256 % k != 0) throw Error(LIGMG_ERR_UNSUPPORTED, "reduction width");
+  const bool big = red_threads(n, k) == kRedBS;
   int nb = colred_blocks(n, k);
   if ((i64)nb * 2 * k > scratch_len) throw Error(LIGMG_ERR_INTERNAL, "reduction scratch");
   i64 rpb = cdiv(n, nb);
   int width = k;
   switch (op) {
-    case Red::Sum: k_colred<T, 0><<<nb, 256, 0, s>>>(n, k, x, y, rpb, scratch); break;
-    case Red::Dot: k_colred<T, 1><<<nb, 256, 0, s>>>(n, k, x, y, rpb, scratch); break;
+    case Red::Sum:
+      if (big) k_colred<T, 0, kRedBS><<<nb, kRedBS, 0, s>>>(n, k, x, y, rpb, scratch);
+      else k_colred<T, 0, 256><<<nb, 256, 0, s>>>(n, k, x, y, rpb, scratch);
+      break;
+    case Red::Dot:
+      if (big) k_colred<T, 1, kRedBS><<<nb, kRedBS, 0, s>>>(n, k, x, y, rpb, scratch);
+      else k_colred<T, 1, 256><<<nb, 256, 0, s>>>(n, k, x, y, rpb, scratch);
+      break;
     case Red::Sum2Dot:
-      k_colred<T, 2><<<nb, 256, 0, s>>>(n, k, x, y, rpb, scratch);
+      if (big) k_colred<T, 2, kRedBS><<<nb, kRedBS, 0, s>>>(n, k, x, y, rpb, scratch);
+      else k_colred<T, 2, 256><<<nb, 256, 0, s>>>(n, k, x, y, rpb, scratch);
       width = 2 * k;
       break;
   }
