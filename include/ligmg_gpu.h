@@ -131,6 +131,13 @@ typedef struct ligmg_options {
                                  level and keep the fastest; 0: fixed
                                  defaults, identical launch shapes on every
                                  run (default 1) */
+  int64_t tail_rows;          /* the coarse end of the hierarchy, from the
+                                 first level below which every level has at
+                                 most this many rows, runs as one persistent
+                                 kernel per visit (k in 1, 8, 16, 32); with
+                                 autotune it is kept only where it times
+                                 faster than the launched levels; 0: every
+                                 level launches its own kernels (default 0) */
 } ligmg_options;
 
 /* ConvergenceInfo (util.hpp:143-170) of one solve.  For a batched solve the
@@ -250,6 +257,7 @@ ligmg_status ligmg_spmv(ligmg_handle h, int32_t level, const double *x,
 #define LIGMG_KERNEL_KRYLOV 9        /* K-cycle inner FCG reductions and updates */
 #define LIGMG_KERNEL_VECTOR 10       /* smoother start, copies, scaling, conversions */
 #define LIGMG_KERNEL_OUTER 11        /* outer Krylov reductions, updates, projection */
+#define LIGMG_KERNEL_TAIL 12         /* the coarse tail as one persistent kernel */
 typedef struct ligmg_kernel_stat {
   int32_t level;
   int32_t kind;      /* LIGMG_KERNEL_* */

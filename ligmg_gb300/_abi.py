@@ -75,6 +75,7 @@ class Options(C.Structure):
         ("device", C.c_int32),
         ("use_graphs", C.c_int32),
         ("autotune", C.c_int32),
+        ("tail_rows", C.c_int64),
     ]
 
 
@@ -139,6 +140,7 @@ def default_options(**overrides) -> Options:
     o.device = 0
     o.use_graphs = 1
     o.autotune = 1
+    o.tail_rows = 0
     for k, v in overrides.items():
         if k in ("smoother_type",) and isinstance(v, str):
             v = SMOOTHER[v]
@@ -158,7 +160,7 @@ def default_options(**overrides) -> Options:
 
 KERNEL_KINDS = {0: "spmv", 1: "resid", 2: "cheb_a", 3: "cheb_b", 4: "elim_interp",
                 5: "elim_restrict", 6: "agg_restrict", 7: "agg_prolong", 8: "coarse",
-                9: "krylov", 10: "vector", 11: "outer"}
+                9: "krylov", 10: "vector", 11: "outer", 12: "tail"}
 
 
 class KernelStat(C.Structure):

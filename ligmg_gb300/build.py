@@ -23,6 +23,7 @@ UNITS = {
     "prims.cu": [],
     "setup.cu": ["--fmad=false"],
     "solve.cu": [],
+    "tail.cu": [],
     "api.cu": [],
 }
 
@@ -35,7 +36,7 @@ def nvcc():
 
 def _deps():
     return [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [
-        os.path.join(HERE, "..", "include", "ligmg_gpu.h")]
+        os.path.join(HERE, "..", "include", "ligmg_gpu.h"), os.path.abspath(__file__)]
 
 
 def up_to_date():
@@ -67,7 +68,9 @@ def build(force=False, verbose=False, extra=()):
 
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(one, UNITS.items()))
-    cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+    # -z defs: a symbol left undefined fails the link, not the first call
+    cmd = [cc, *ARCH, "-shared", "-Xlinker", "-z", "-Xlinker", "defs", "-o", LIB, *objs,
+           "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

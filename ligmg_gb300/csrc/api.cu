@@ -19,6 +19,7 @@
 #include "prims.cuh"
 #include "setup.cuh"
 #include "solve.cuh"
+#include "tail.cuh"
 
 namespace lg {
 namespace {
@@ -404,10 +405,25 @@ struct LevelWork {
   double *sslot(int s) { return segsc.p + (i64)s * nseg; }
 };
 
+// The recorded coarse-tail program of one Work (k columns).
+template <typename T>
+struct TailState {
+  bool tried = false;   // build attempted
+  bool on = false;
+  float best_ms = 0;    // autotune: tail launch time at the chosen G
+  int start = -1;       // first level of the tail
+  int G = 0;            // CTAs of the persistent launch
+  int nops = 0;
+  DBuf<TOp<T>> ops;
+  DBuf<double> partial;
+  DBuf<TailSync> sync;
+};
+
 template <typename T>
 struct Work {
   int k = 0;
   std::vector<LevelWork<T>> lw;
+  TailState<T> tail;
 };
 
 // batch-mode outer scalars (one per graph)
@@ -668,6 +684,296 @@ Work<T> &work_for(Handle &H, int k) {
 }
 
 // ---------------------------------------------------------------------------
+// Coarse-tail program: the operations Engine below issues for one visit of
+// the levels from `start` down, recorded (same order, buffers and scalars)
+// instead of launched.  Mirrors Engine::smooth / cycle / recurse / fcg_fixed.
+template <typename T>
+struct TailBuilder {
+  Handle &H;
+  Work<T> &W;
+  int k;
+  cudaStream_t s;
+  std::vector<TOp<T>> ops;
+  TailBuilder(Handle &h, Work<T> &w) : H(h), W(w), k(w.k), s(h.s) {}
+  const ligmg_options &o() const { return H.opts; }
+
+  void spmm(const MatView<T> &A, const T *X, Epi e, const EpiArgs &a) {
+    TOp<T> op;
+    op.kind = TOpKind::Spmm;
+    op.epi = e;
+    op.n = A.n;
+    op.A = A;
+    op.x0 = X;
+    op.a = a;
+    ops.push_back(op);
+  }
+  void elem(TOpKind kind, i64 n, const T *x0, const T *x1, T *y0, double f = 1) {
+    TOp<T> op;
+    op.kind = kind;
+    op.n = n;
+    op.x0 = x0;
+    op.x1 = x1;
+    op.y0 = y0;
+    op.f = f;
+    ops.push_back(op);
+  }
+
+  void smooth(size_t l, T *x, const T *b, int iters, bool x_zero) {
+    Level &L = *H.h[l];
+    LevelWork<T> &w = W.lw[l];
+    i64 n = L.A.n;
+    MatView<T> A = viewA<T>(L, k, s);
+    const T *invd = invdT<T>(L);
+    if (o().smoother_type == LIGMG_SMOOTHER_JACOBI) {
+      const double omega = 2.0 / 3.0;
+      if (x_zero) {
+        elem(TOpKind::Cheb0, n, b, invd, x, 1.0 / omega);
+        return;
+      }
+      EpiArgs a;
+      a.b = b; a.invd = invd; a.xin = x; a.y = w.xt.p; a.c1 = omega;
+      spmm(A, x, Epi::Jacobi, a);
+      elem(TOpKind::Copy, n, w.xt.p, nullptr, x);
+      return;
+    }
+    if (iters <= 0) return;
+    const T *r_cur;
+    const T *x_cur;
+    T *d_cur;
+    T *d_other = w.d1.p;
+    if (x_zero) {
+      T *d0 = iters == 1 ? x : w.d0.p;
+      elem(TOpKind::Cheb0, n, b, invd, d0, L.theta);
+      if (iters == 1) return;
+      d_cur = w.d0.p;
+      x_cur = w.d0.p;
+      r_cur = b;
+    } else {
+      EpiArgs a;
+      a.b = b; a.invd = invd; a.xin = x; a.rout = w.r.p; a.dout = w.d0.p; a.xout = w.xt.p;
+      a.theta = L.theta;
+      spmm(A, x, Epi::ChebA, a);
+      d_cur = w.d0.p;
+      x_cur = w.xt.p;
+      r_cur = w.r.p;
+      if (iters == 1) {
+        elem(TOpKind::Copy, n, w.xt.p, nullptr, x);
+        return;
+      }
+    }
+    for (int it = 1; it < iters; it++) {
+      bool last = it == iters - 1;
+      EpiArgs a;
+      a.invd = invd;
+      a.rin = r_cur;
+      a.din = d_cur;
+      a.xin = x_cur;
+      a.c1 = L.c1[it - 1];
+      a.c2 = L.c2[it - 1];
+      a.rout = last ? nullptr : w.r.p;
+      a.dout = last ? nullptr : d_other;
+      a.xout = last ? x : w.xt.p;
+      spmm(A, d_cur, Epi::ChebB, a);
+      if (!last) {
+        r_cur = w.r.p;
+        std::swap(d_cur, d_other);
+        x_cur = w.xt.p;
+      }
+    }
+  }
+
+  void cycle(size_t l, const T *b, T *x) {
+    Level &L = *H.h[l];
+    i64 n = L.A.n;
+    if (L.type == LIGMG_LEVEL_COARSE) {
+      elem(TOpKind::Coarse, n, b, pinvT<T>(L), x);
+      return;
+    }
+    LevelWork<T> &nw = W.lw[l + 1];
+    if (L.type == LIGMG_LEVEL_ELIM) {
+      EpiArgs a;
+      a.y = nw.in.p;
+      spmm(viewR<T>(L, k, s), b, Epi::Store, a);
+      recurse(l, nw.in.p, nw.out.p);
+      EpiArgs c;
+      c.y = x; c.b = b; c.q = QT<T>(L);
+      spmm(viewP<T>(L), nw.out.p, Epi::ElimInterp, c);
+      return;
+    }
+    LevelWork<T> &w = W.lw[l];
+    smooth(l, x, b, o().pre_smooth, true);
+    EpiArgs a;
+    a.y = w.r.p;
+    a.b = b;
+    spmm(viewA<T>(L, k, s), x, Epi::Resid, a);
+    EpiArgs rs;
+    rs.y = nw.in.p;
+    spmm(viewR<T>(L, k, s), w.r.p, Epi::Store, rs);
+    recurse(l, nw.in.p, nw.out.p);
+    TOp<T> pr;
+    pr.kind = TOpKind::Prolong;
+    pr.n = n;
+    pr.x0 = nw.out.p;
+    pr.y0 = x;
+    pr.idx = L.agg.agg.p;
+    ops.push_back(pr);
+    smooth(l, x, b, o().post_smooth, false);
+    if (o().constant_correction) elem(TOpKind::Scale, n, nullptr, nullptr, x, 4.0 / 3.0);
+  }
+
+  void recurse(size_t l, T *bc, T *xc) {
+    const Level &N = *H.h[l + 1];
+    if (!o().kcycle || N.is_exact() || N.type == LIGMG_LEVEL_COARSE) {
+      cycle(l + 1, bc, xc);
+      return;
+    }
+    fcg_fixed(l + 1, bc, xc, o().kcycle_iters);
+  }
+
+  void fcg_fixed(size_t l, T *b, T *x, int iters) {
+    Level &L = *H.h[l];
+    LevelWork<T> &w = W.lw[l];
+    i64 n = L.A.n;
+    MatView<T> A = viewA<T>(L, k, s);
+    elem(TOpKind::Zero, n, nullptr, nullptr, x);
+    T *r = b;
+    T *p = w.fp0.p, *pp = w.fp1.p, *q = w.fq0.p, *qp = w.fq1.p;
+    FcgScalars sc{w.slot(S_SUM, k), w.slot(S_BETA, k), w.slot(S_ETA0, k), w.slot(S_ETA1, k),
+                  w.slot(S_ALPHA, k), nullptr};
+    for (int it = 0; it < iters; it++) {
+      cycle(l, r, w.fz.p);
+      TOp<T> rb;
+      rb.kind = TOpKind::RedBeta;
+      rb.n = n;
+      rb.x0 = w.fz.p;
+      rb.x1 = it > 0 ? qp : nullptr;
+      rb.flag = it > 0;
+      ops.push_back(rb);
+      TOp<T> d;
+      d.kind = TOpKind::Dir;
+      d.n = n;
+      d.x0 = w.fz.p;
+      d.x1 = it > 0 ? pp : nullptr;
+      d.y0 = p;
+      d.flag = it > 0;
+      d.sc = sc;
+      ops.push_back(d);
+      EpiArgs a;
+      a.y = q;
+      spmm(A, p, Epi::Store, a);
+      TOp<T> ra;
+      ra.kind = TOpKind::RedAlpha;
+      ra.n = n;
+      ra.x0 = p;
+      ra.x1 = q;
+      ra.x2 = r;
+      ops.push_back(ra);
+      TOp<T> u;
+      u.kind = TOpKind::Update;
+      u.n = n;
+      u.x0 = p;
+      u.x1 = q;
+      u.y0 = x;
+      u.y1 = r;
+      u.flag = it + 1 < iters;
+      u.sc = sc;
+      ops.push_back(u);
+      std::swap(p, pp);
+      std::swap(q, qp);
+      std::swap(sc.eta, sc.eta_prev);
+    }
+  }
+};
+
+// First level of the tail: every level from it down has at most tail_rows
+// rows; at least level 1, since the tail is entered from Engine::recurse of
+// the level above (0: no tail).
+inline size_t tail_start_level(const Handle &H) {
+  const i64 lim = H.opts.tail_rows;
+  if (lim <= 0 || H.h.size() < 2) return 0;
+  size_t t = H.h.size();
+  while (t > 1 && H.h[t - 1]->A.n <= lim) t--;
+  return t < H.h.size() ? t : 0;
+}
+
+// Record and upload the tail program of W (entered as recurse(start - 1)),
+// then pick the CTA count by timing the candidates (the restriction input
+// bc is saved and restored around each timing run: the program updates it).
+template <typename T>
+void tail_prepare(Handle &H, Work<T> &W, size_t start) {
+  TailState<T> &ts = W.tail;
+  ts.tried = true;
+  const int k = W.k;
+  cudaStream_t s = H.s;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  LG_CUDA(cudaStreamIsCapturing(s, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return;
+  const int maxG = tail_max_ctas<T>(k);
+  if (maxG <= 0) return;
+  TailBuilder<T> B(H, W);
+  LevelWork<T> &top = W.lw[start];
+  B.recurse(start - 1, top.in.p, top.out.p);
+  ts.nops = (int)B.ops.size();
+  ts.ops.alloc(ts.nops, s);
+  ts.ops.upload(B.ops.data(), ts.nops);
+  ts.sync.alloc(1, s);
+  ts.sync.zero();
+  const int G0 = std::min(maxG, kSMs);
+  ts.partial.alloc((i64)G0 * 3 * k, s);
+  ts.start = (int)start;
+  ts.G = G0;
+  if (H.opts.autotune) {
+    const i64 nin = H.h[start]->A.n * k;
+    DBuf<T> save(nin, s);
+    LG_CUDA(cudaMemcpyAsync(save.p, top.in.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
+    cudaEvent_t e0, e1;
+    LG_CUDA(cudaEventCreate(&e0));
+    LG_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    // one CTA (block barriers only) or several (grid barriers)
+    for (int G : {1, 4, 16, G0 / 4, G0}) {
+      if (G < 1 || G > G0) continue;
+      float tot = 0;
+      for (int rep = 0; rep < 3; rep++) {
+        LG_CUDA(cudaMemcpyAsync(top.in.p, save.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
+        LG_CUDA(cudaEventRecord(e0, s));
+        launch_tail<T>(ts.ops.p, ts.nops, k, G, ts.partial.p, ts.sync.p, s);
+        LG_CUDA(cudaEventRecord(e1, s));
+        LG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        LG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0) tot += ms;
+      }
+      if (tot < best) {
+        best = tot;
+        ts.G = G;
+      }
+    }
+    ts.best_ms = best / 2;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    LG_CUDA(cudaMemcpyAsync(top.in.p, save.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
+    LG_CUDA(cudaStreamSynchronize(s));
+  }
+  ts.on = true;
+}
+
+// Error raised by a persistent tail launch (a grid barrier that gave up).
+template <typename T>
+void tail_check(Work<T> &W, cudaStream_t s) {
+  if (!W.tail.on) return;
+  TailSync h{};
+  LG_CUDA(cudaMemcpyAsync(&h, W.tail.sync.p, sizeof(TailSync), cudaMemcpyDeviceToHost, s));
+  LG_CUDA(cudaStreamSynchronize(s));
+  if (h.err) {
+    // an abandoned barrier leaves the arrival counter mid-way: start clean
+    W.tail.sync.zero();
+    LG_CUDA(cudaStreamSynchronize(s));
+    throw Error(LIGMG_ERR_INTERNAL, "coarse-tail kernel: grid barrier gave up");
+  }
+}
+
+// ---------------------------------------------------------------------------
 template <typename T>
 struct Engine {
   Handle &H;
@@ -807,12 +1113,97 @@ struct Engine {
   }
 
   void recurse(size_t l, T *bc, T *xc) {
+    if (try_tail(l + 1, bc, xc)) return;
+    recurse_launched(l, bc, xc);
+  }
+  void recurse_launched(size_t l, T *bc, T *xc) {
     const Level &N = *H.h[l + 1];
     if (!o().kcycle || N.is_exact() || N.type == LIGMG_LEVEL_COARSE) {
       cycle(l + 1, bc, xc);
       return;
     }
     fcg_fixed(l + 1, bc, xc, o().kcycle_iters);
+  }
+
+  // Autotune: the launched path over the same levels, captured into a CUDA
+  // graph (as the solve replays it) and timed like the tail (bc saved and
+  // restored around each replay; the inner FCG updates it).
+  float time_launched(size_t start, T *bc, T *xc) {
+    const i64 nin = H.h[start]->A.n * k;
+    DBuf<T> save(nin, s);
+    LG_CUDA(cudaMemcpyAsync(save.p, bc, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
+    LG_CUDA(cudaStreamSynchronize(s));
+    const bool susp = H.prof.suspended;
+    H.prof.suspended = true;  // no profiler events inside this capture
+    const int64_t c0 = launches_now();
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    LG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      recurse_launched(start - 1, bc, xc);
+    } catch (...) {
+      cudaStreamEndCapture(s, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      H.prof.suspended = susp;
+      add_launches(c0 - launches_now());
+      throw;
+    }
+    H.prof.suspended = susp;
+    add_launches(c0 - launches_now());  // recorded, not run
+    LG_CUDA(cudaStreamEndCapture(s, &graph));
+    cudaError_t ierr = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    LG_CUDA(ierr);
+    cudaEvent_t e0, e1;
+    LG_CUDA(cudaEventCreate(&e0));
+    LG_CUDA(cudaEventCreate(&e1));
+    float tot = 0;
+    for (int rep = 0; rep < 3; rep++) {
+      LG_CUDA(cudaMemcpyAsync(bc, save.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
+      LG_CUDA(cudaEventRecord(e0, s));
+      LG_CUDA(cudaGraphLaunch(exec, s));
+      LG_CUDA(cudaEventRecord(e1, s));
+      LG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      LG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (rep > 0) tot += ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaGraphExecDestroy(exec);
+    LG_CUDA(cudaMemcpyAsync(bc, save.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
+    LG_CUDA(cudaStreamSynchronize(s));
+    return tot / 2;
+  }
+
+  // The levels from `start` down as one persistent launch when that level
+  // starts the tail (program recorded on first use, outside graph capture).
+  bool try_tail(size_t start, T *bc, T *xc) {
+    TailState<T> &ts = W.tail;
+    if (ts.tried && !ts.on) return false;
+    if (ts.on) {
+      if ((size_t)ts.start != start || bc != W.lw[start].in.p || xc != W.lw[start].out.p)
+        return false;
+    } else {
+      if (start != tail_start_level(H) || start == 0) return false;
+      if (H.h[start]->seginfo().nseg > 0) {  // batch mode keeps per-graph kernels
+        ts.tried = true;
+        return false;
+      }
+      if (bc != W.lw[start].in.p || xc != W.lw[start].out.p) return false;
+      tail_prepare<T>(H, W, start);
+      if (!ts.on) return false;
+      // keep the persistent kernel only where it beats the launched levels
+      // (it does when each level visit is latency-bound, e.g. k = 1)
+      if (o().autotune && time_launched(start, bc, xc) <= ts.best_ms) {
+        ts.on = false;
+        return false;
+      }
+    }
+    timed(H, (int)start, LIGMG_KERNEL_TAIL, k, sizeof(T) == 8, 0.0, [&] {
+      launch_tail<T>(ts.ops.p, ts.nops, k, ts.G, ts.partial.p, ts.sync.p, s);
+    });
+    return true;
   }
 
   // K-cycle inner FCG with a fixed number of iterations, x0 = 0; r = b is
@@ -1463,6 +1854,12 @@ SolveResult outer_solve_seg(Handle &H, size_t base, OuterWork &w) {
 }
 
 // full solve: B (n0 x k) in w.Bfull -> w.Xfull; fills info
+// Raise the error of any persistent tail launch of this handle.
+void check_tails(Handle &H) {
+  for (auto &w : H.w32) tail_check<float>(*w.second, H.s);
+  for (auto &w : H.w64) tail_check<double>(*w.second, H.s);
+}
+
 ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *dX,
                           ligmg_info *info) {
   auto t0 = std::chrono::steady_clock::now();
@@ -1566,6 +1963,7 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
       info->history_len = m;
     }
   }
+  check_tails(H);
   return res.converged ? LIGMG_OK : LIGMG_NOT_CONVERGED;
 }
 
@@ -1637,6 +2035,7 @@ void ligmg_default_options(ligmg_options *o) {
   o->device = 0;
   o->use_graphs = 1;
   o->autotune = 1;
+  o->tail_rows = 0;
 }
 
 const char *ligmg_status_string(ligmg_status s) {
@@ -2100,6 +2499,7 @@ ligmg_status ligmg_cycle(ligmg_handle h, int32_t level, const double *b, double 
     }
     dx.download(x, n);
     LG_CUDA(cudaStreamSynchronize(h->s));
+    check_tails(*h);
     return LIGMG_OK;
   });
 }

@@ -8,7 +8,7 @@
 // epilogue on their VW columns.  The matrix is read once per k vectors.
 #include <algorithm>
 
-#include "solve.cuh"
+#include "spmm_dev.cuh"
 
 namespace lg {
 
@@ -86,217 +86,13 @@ template struct HubPlan<double>;
 // ---------------------------------------------------------------------------
 namespace {
 
-template <typename T>
-struct VT;
-template <>
-struct VT<float> {
-  static constexpr int W = 4;
-};
-template <>
-struct VT<double> {
-  static constexpr int W = 2;
-};
-
-template <typename T, int VW>
-__device__ __forceinline__ void vload(const T *p, T (&o)[VW]) {
-  if constexpr (VW == 4 && sizeof(T) == 4) {
-    float4 t = *reinterpret_cast<const float4 *>(p);
-    o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
-  } else if constexpr (VW == 2 && sizeof(T) == 8) {
-    double2 t = *reinterpret_cast<const double2 *>(p);
-    o[0] = t.x; o[1] = t.y;
-  } else {
-#pragma unroll
-    for (int q = 0; q < VW; q++) o[q] = p[q];
-  }
-}
-template <typename T, int VW>
-__device__ __forceinline__ void vldg(const T *p, T (&o)[VW]) {
-  if constexpr (VW == 4 && sizeof(T) == 4) {
-    float4 t = __ldg(reinterpret_cast<const float4 *>(p));
-    o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
-  } else if constexpr (VW == 2 && sizeof(T) == 8) {
-    double2 t = __ldg(reinterpret_cast<const double2 *>(p));
-    o[0] = t.x; o[1] = t.y;
-  } else {
-#pragma unroll
-    for (int q = 0; q < VW; q++) o[q] = __ldg(p + q);
-  }
-}
-template <typename T, int VW>
-__device__ __forceinline__ void vstore(T *p, const T (&o)[VW]) {
-  if constexpr (VW == 4 && sizeof(T) == 4) {
-    *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
-  } else if constexpr (VW == 2 && sizeof(T) == 8) {
-    *reinterpret_cast<double2 *>(p) = make_double2(o[0], o[1]);
-  } else {
-#pragma unroll
-    for (int q = 0; q < VW; q++) p[q] = o[q];
-  }
-}
-
-template <typename T, int K, int VW, Epi E>
-__device__ __forceinline__ void epilogue(const EpiArgs &a, i64 r, int c0, T (&acc)[VW]) {
-  const i64 off = r * K + c0;
-  if constexpr (E == Epi::Store) {
-    vstore<T, VW>((T *)a.y + off, acc);
-  } else if constexpr (E == Epi::Resid) {
-    T b[VW];
-    vload<T, VW>((const T *)a.b + off, b);
-#pragma unroll
-    for (int q = 0; q < VW; q++) b[q] = b[q] - acc[q];
-    vstore<T, VW>((T *)a.y + off, b);
-  } else if constexpr (E == Epi::ChebA) {
-    T b[VW], x[VW], d[VW];
-    vload<T, VW>((const T *)a.b + off, b);
-    vload<T, VW>((const T *)a.xin + off, x);
-    const T iv = ((const T *)a.invd)[r];
-    const T th = (T)a.theta;
-#pragma unroll
-    for (int q = 0; q < VW; q++) {
-      b[q] = b[q] - acc[q];
-      d[q] = iv * b[q] / th;
-      x[q] = x[q] + d[q];
-    }
-    vstore<T, VW>((T *)a.rout + off, b);
-    vstore<T, VW>((T *)a.dout + off, d);
-    vstore<T, VW>((T *)a.xout + off, x);
-  } else if constexpr (E == Epi::ChebB) {
-    T rr[VW], d[VW], x[VW];
-    vload<T, VW>((const T *)a.rin + off, rr);
-    vload<T, VW>((const T *)a.din + off, d);
-    vload<T, VW>((const T *)a.xin + off, x);
-    const T iv = ((const T *)a.invd)[r];
-    const T c1 = (T)a.c1, c2 = (T)a.c2;
-#pragma unroll
-    for (int q = 0; q < VW; q++) {
-      rr[q] = rr[q] - acc[q];
-      d[q] = c1 * d[q] + c2 * (iv * rr[q]);
-      x[q] = x[q] + d[q];
-    }
-    if (a.rout) vstore<T, VW>((T *)a.rout + off, rr);
-    if (a.dout) vstore<T, VW>((T *)a.dout + off, d);
-    vstore<T, VW>((T *)a.xout + off, x);
-  } else if constexpr (E == Epi::ElimInterp) {
-    T b[VW];
-    vload<T, VW>((const T *)a.b + off, b);
-    const T qd = ((const T *)a.q)[r];
-#pragma unroll
-    for (int q = 0; q < VW; q++) b[q] = acc[q] + qd * b[q];
-    vstore<T, VW>((T *)a.y + off, b);
-  } else {  // Jacobi: for a Laplacian, sum over negative entries = (A x)_i - a_ii x_i
-    T b[VW], x[VW];
-    vload<T, VW>((const T *)a.b + off, b);
-    vload<T, VW>((const T *)a.xin + off, x);
-    const T wi = (T)a.c1 * ((const T *)a.invd)[r];
-#pragma unroll
-    for (int q = 0; q < VW; q++) x[q] = x[q] + wi * (b[q] - acc[q]);
-    vstore<T, VW>((T *)a.y + off, x);
-  }
-}
-
-template <typename T, int K, int VW, int E>
-__device__ __forceinline__ void row_accumulate(const MatView<T> &A, const T *__restrict__ X, i64 k,
-                                               i64 e, int ch, T (&acc)[VW]) {
-  const T *__restrict__ av = A.v;
-  const i32 *__restrict__ ac = A.ci;
-  for (; k + 3 * E < e; k += 4 * E) {
-    T a0 = __ldg(av + k), a1 = __ldg(av + k + E), a2 = __ldg(av + k + 2 * E),
-      a3 = __ldg(av + k + 3 * E);
-    i32 j0 = __ldg(ac + k), j1 = __ldg(ac + k + E), j2 = __ldg(ac + k + 2 * E),
-        j3 = __ldg(ac + k + 3 * E);
-    T x0[VW], x1[VW], x2[VW], x3[VW];
-    vldg<T, VW>(X + (i64)j0 * K + ch * VW, x0);
-    vldg<T, VW>(X + (i64)j1 * K + ch * VW, x1);
-    vldg<T, VW>(X + (i64)j2 * K + ch * VW, x2);
-    vldg<T, VW>(X + (i64)j3 * K + ch * VW, x3);
-#pragma unroll
-    for (int q = 0; q < VW; q++) acc[q] += a0 * x0[q];
-#pragma unroll
-    for (int q = 0; q < VW; q++) acc[q] += a1 * x1[q];
-#pragma unroll
-    for (int q = 0; q < VW; q++) acc[q] += a2 * x2[q];
-#pragma unroll
-    for (int q = 0; q < VW; q++) acc[q] += a3 * x3[q];
-  }
-  for (; k < e; k += E) {
-    T a0 = __ldg(av + k);
-    i32 j0 = __ldg(ac + k);
-    T x0[VW];
-    vldg<T, VW>(X + (i64)j0 * K + ch * VW, x0);
-#pragma unroll
-    for (int q = 0; q < VW; q++) acc[q] += a0 * x0[q];
-  }
-}
-
-template <typename T, int VW, int L, int G>
-__device__ __forceinline__ void reduce_slots(T (&acc)[VW]) {
-#pragma unroll
-  for (int o = L; o < G; o <<= 1)
-#pragma unroll
-    for (int q = 0; q < VW; q++) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
-}
+using namespace dev;
 
 template <typename T, int K, int G, Epi EP>
 __global__ void __launch_bounds__(256) k_spmm(const MatView<T> A, const T *__restrict__ X,
                                               const EpiArgs a) {
-  constexpr int VW = (K % VT<T>::W == 0) ? VT<T>::W : 1;
-  constexpr int L = K / VW;
-  static_assert(L <= G && G <= 32 && (G % L) == 0, "bad SpMM layout");
-  constexpr int E = G / L;
-  constexpr int RPW = 32 / G;
-  const int lane = threadIdx.x & 31;
-  const int g = lane % G, slot = g / L, ch = g % L;
   const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const i64 nregw = (A.n + RPW - 1) / RPW;
-  T acc[VW];
-#pragma unroll
-  for (int q = 0; q < VW; q++) acc[q] = (T)0;
-  if (warp < nregw) {
-    const i64 r = warp * RPW + lane / G;
-    bool act = r < A.n;
-    i64 b = 0, e = 0;
-    if (act) {
-      b = A.rp[r];
-      e = A.rp[r + 1];
-      if (A.hub_thresh > 0 && e - b > A.hub_thresh) act = false;
-    }
-    if (act) row_accumulate<T, K, VW, E>(A, X, b + slot, e, ch, acc);
-    reduce_slots<T, VW, L, G>(acc);
-    if (act && slot == 0) epilogue<T, K, VW, EP>(a, r, ch * VW, acc);
-    return;
-  }
-  if constexpr (G == 32) {
-    const i64 c = warp - nregw;
-    if (c >= A.nchunks) return;
-    row_accumulate<T, K, VW, E>(A, X, A.ch_beg[c] + slot, A.ch_end[c], ch, acc);
-    reduce_slots<T, VW, L, G>(acc);
-    if (slot == 0) vstore<T, VW>(A.partial + c * K + ch * VW, acc);
-    __threadfence();
-    __syncwarp();
-    int last = 0;
-    if (lane == 0) last = atomicAdd(&A.hub_counter[A.ch_hub[c]], 1) == A.ch_cnt[c] - 1;
-    last = __shfl_sync(0xffffffffu, last, 0);
-    if (!last) return;
-    __threadfence();
-    {
-      // every slot sums a strided subset of the chunk partials; the slot
-      // partials are combined in a fixed shuffle tree (deterministic)
-      const i64 first = A.ch_first[c];
-      const int cnt = A.ch_cnt[c];
-      T s[VW];
-#pragma unroll
-      for (int q = 0; q < VW; q++) s[q] = (T)0;
-#pragma unroll 4
-      for (int t = slot; t < cnt; t += E) {
-#pragma unroll
-        for (int q = 0; q < VW; q++) s[q] += __ldcg(A.partial + (first + t) * K + ch * VW + q);
-      }
-      reduce_slots<T, VW, L, G>(s);
-      if (slot == 0) epilogue<T, K, VW, EP>(a, A.ch_row[c], ch * VW, s);
-    }
-    if (lane == 0) A.hub_counter[A.ch_hub[c]] = 0;
-  }
+  dev::spmm_unit<T, K, G, EP>(A, X, a, warp, threadIdx.x & 31);
 }
 
 template <typename T, int K, int G, Epi EP>

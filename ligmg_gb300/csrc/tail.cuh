@@ -1,0 +1,72 @@
+// tail.cuh — the coarse end of the cycle as one persistent kernel.
+//
+// Below a size threshold every level visit of the K-/V-cycle is a handful of
+// small, dependent kernels; in a CUDA graph each costs a few microseconds of
+// launch and drain whatever its size, and the coarse levels are visited
+// exponentially often by the K-cycle.  The host records the exact operation
+// sequence of one visit of the tail (the same operations, pointers and
+// scalars the launched path would issue) as a program of TOp records; one
+// cooperative launch of k_tail executes the program with every CTA resident,
+// separated by software grid barriers.
+#pragma once
+#include "solve.cuh"
+
+namespace lg {
+
+enum class TOpKind : int {
+  Spmm,      // y = A X with epilogue `epi` (hub chunks included)
+  Cheb0,     // d = D^-1 b / theta                       (first Chebyshev step)
+  Prolong,   // x += xc[agg]
+  Coarse,    // x = pinv b (dense)
+  Scale,     // x *= f
+  Zero,      // x = 0
+  Copy,      // y = X
+  RedBeta,   // partial sums of z, z.qp, qp (FCG beta)
+  Dir,       // finish beta; p = z - mu - beta pp
+  RedAlpha,  // partial sums of p.q, p.r (FCG alpha)
+  Update,    // finish alpha; x += alpha p; r -= alpha q
+};
+
+template <typename T>
+struct TOp {
+  TOpKind kind = TOpKind::Zero;
+  Epi epi = Epi::Store;
+  int flag = 0;             // RedBeta/Dir: previous direction present; Update: update r
+  i64 n = 0;                // rows
+  MatView<T> A;             // Spmm
+  EpiArgs a;                // Spmm epilogue
+  const T *x0 = nullptr;    // Spmm X; Cheb0 b; Prolong xc; Coarse b; Copy src;
+                            // RedBeta z; Dir z; RedAlpha p; Update p
+  const T *x1 = nullptr;    // Cheb0 invd; Coarse pinv; RedBeta qp; Dir pp; RedAlpha q; Update q
+  const T *x2 = nullptr;    // RedAlpha r
+  T *y0 = nullptr;          // Cheb0 d; Prolong/Coarse/Scale/Zero x; Copy dst; Dir p; Update x
+  T *y1 = nullptr;          // Update r
+  const i32 *idx = nullptr; // Prolong agg
+  double f = 1;             // Cheb0 theta; Scale factor
+  FcgScalars sc{};          // Dir/Update
+};
+
+// Grid barrier state, zero-initialised.  Every completed barrier adds exactly
+// 2^31 to `arrive` (CTA 0 adds 2^31 - (G - 1), the others 1), so its low 31
+// bits are zero at each barrier's start and bit 31 flips exactly when the
+// last CTA arrives.  err != 0: a wait ran out of its iteration limit; every
+// CTA then leaves the kernel (the host resets the state).
+struct TailSync {
+  unsigned arrive;
+  int err;
+  int pad[2];
+};
+
+constexpr int kTailThreads = 1024;
+
+// Launch the program (cooperative launch, G CTAs of kTailThreads threads).
+// partial: G x 3 x k doubles of reduction scratch.
+template <typename T>
+void launch_tail(const TOp<T> *ops, int nops, int k, int G, double *partial, TailSync *sync,
+                 cudaStream_t s);
+// CTAs of kTailThreads threads that can be resident at once on this device
+// for the k-column program (0: the tail kernel is unavailable for k).
+template <typename T>
+int tail_max_ctas(int k);
+
+}  // namespace lg

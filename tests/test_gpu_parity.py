@@ -80,11 +80,14 @@ def test_setup_options_bit_exact(opt):
         assert (S.level_matrix(l)[2].view(np.int64) == R.level_matrix(l)[2].view(np.int64)).all()
 
 
+@pytest.mark.parametrize("tail", [0, 1 << 20])
 @pytest.mark.parametrize("kcycle", [0, 1])
 @pytest.mark.parametrize("name", ["grid48_logn", "my_matrix", "rmat12", "grid3d_12"])
-def test_cycle_fp64_matches_oracle(name, kcycle):
+def test_cycle_fp64_matches_oracle(name, kcycle, tail):
+    # tail > 0: the levels below the first one run as the persistent kernel
+    # (autotune off, so it is used whatever its speed)
     L = GRAPHS[name]()
-    S = Solver(L, kcycle=kcycle)
+    S = Solver(L, kcycle=kcycle, tail_rows=tail, autotune=0 if tail else 1)
     R = O.OracleSolver(L, kcycle=kcycle)
     rng = np.random.default_rng(7)
     for level in range(R.num_levels):
@@ -178,6 +181,27 @@ def test_graph_replay_matches_direct_launches():
     b = Solver(L, use_graphs=0, **kw).solve_batched(B)
     assert a.iters() == b.iters()
     assert np.array_equal(a.solution, b.solution)
+
+
+@pytest.mark.parametrize("prec,k", [("fp32", 32), ("fp32", 8), ("fp64", 1), ("fp32", 1)])
+def test_persistent_tail_matches_launched_levels(prec, k):
+    # tail_rows = 0: every level launches its own kernels; the default runs
+    # the coarse end as one persistent kernel.  Same operations, so the same
+    # iterations and solutions equal to rounding of the reductions.
+    L = GRAPHS["rmat14"]()
+    B = G.rhs(L.n, k=k, seed=9)
+    if k == 1:
+        B = B.reshape(L.n, 1)
+    kw = dict(precision=prec, kcycle=1, outer_ksp_type="fcg", autotune=0)
+    a = Solver(L, tail_rows=0, **kw).solve_batched(B)
+    b = Solver(L, tail_rows=1 << 20, **kw).solve_batched(B)
+    assert a.converged and b.converged
+    assert a.iters() == b.iters()
+    tol = 1e-5 if prec == "fp32" else 1e-10
+    assert _relerr(a.solution, b.solution) <= tol
+    c = Solver(L, tail_rows=500, **kw).solve_batched(B)  # a shorter tail
+    assert c.converged and c.iters() == a.iters()
+    assert _relerr(a.solution, c.solution) <= tol
 
 
 def test_autotuned_shapes_match_fixed_shapes():
