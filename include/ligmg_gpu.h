@@ -131,13 +131,17 @@ typedef struct ligmg_options {
                                  level and keep the fastest; 0: fixed
                                  defaults, identical launch shapes on every
                                  run (default 1) */
-  int64_t tail_rows;          /* the coarse end of the hierarchy, from the
-                                 first level below which every level has at
-                                 most this many rows, runs as one persistent
-                                 kernel per visit (k in 1, 8, 16, 32); with
-                                 autotune it is kept only where it times
-                                 faster than the launched levels; 0: every
-                                 level launches its own kernels (default 0) */
+  int64_t tail_rows;          /* the coarse end of the hierarchy as one
+                                 persistent kernel per visit; with autotune
+                                 it is kept only where it times faster than
+                                 the launched levels.  0 (default): from the
+                                 shallowest level whose program, matrices and
+                                 work vectors fit in shared memory, each CTA
+                                 alone on a slice of the k columns; > 0: all
+                                 CTAs with grid barriers (k in 1, 8, 16, 32),
+                                 from the first level below which every level
+                                 has at most this many rows; < 0: every level
+                                 launches its own kernels */
 } ligmg_options;
 
 /* ConvergenceInfo (util.hpp:143-170) of one solve.  For a batched solve the

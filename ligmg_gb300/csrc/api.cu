@@ -13,6 +13,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <type_traits>
 #include <memory>
 #include <new>
 
@@ -408,12 +409,19 @@ struct LevelWork {
 // The recorded coarse-tail program of one Work (k columns).
 template <typename T>
 struct TailState {
-  bool tried = false;   // build attempted
+  bool planned = false; // start level decided
+  bool tried = false;   // program built and timed
+  bool decided = false; // autotune: kept or dropped against the launched levels
   bool on = false;
-  float best_ms = 0;    // autotune: tail launch time at the chosen G
-  int start = -1;       // first level of the tail
-  int G = 0;            // CTAs of the persistent launch
+  float best_ms = 0;    // autotune: time of one launch in the chosen shape
+  int start = 0;        // first level of the tail (0: none)
+  bool smem_mode = false;
+  int G = 0;            // grid mode: CTAs of the cooperative launch
   int nops = 0;
+  double bytes = 0;     // compulsory bytes of a visit: its input and output
+                        // vectors and one read of every tail level's matrix
+  TailSmemLaunch sl;    // shared-memory mode launch (image in `image`)
+  DBuf<unsigned char> image;
   DBuf<TOp<T>> ops;
   DBuf<double> partial;
   DBuf<TailSync> sync;
@@ -885,9 +893,9 @@ struct TailBuilder {
   }
 };
 
-// First level of the tail: every level from it down has at most tail_rows
-// rows; at least level 1, since the tail is entered from Engine::recurse of
-// the level above (0: no tail).
+// First level of the grid-mode tail (tail_rows > 0): every level from it
+// down has at most tail_rows rows; at least level 1, since the tail is
+// entered from Engine::recurse of the level above (0: none).
 inline size_t tail_start_level(const Handle &H) {
   const i64 lim = H.opts.tail_rows;
   if (lim <= 0 || H.h.size() < 2) return 0;
@@ -896,64 +904,332 @@ inline size_t tail_start_level(const Handle &H) {
   return t < H.h.size() ? t : 0;
 }
 
-// Record and upload the tail program of W (entered as recurse(start - 1)),
-// then pick the CTA count by timing the candidates (the restriction input
-// bc is saved and restored around each timing run: the program updates it).
+// Record the tail program entered as recurse(start - 1).  With smem_avail >
+// 0 it is laid out for the shared-memory launch with kl columns per CTA:
+//   [program | read-only arrays the program reads | work vector slices]
+// where the work vectors are every buffer of the levels from `start` down
+// (the start level's input and output included: staged in and out); each
+// CTA holds an n x kl slice of each (the Krylov scalar slots whole).  The
+// program's pointers into them are rewritten as kSmemTag | offset.
+// `consts` lists the read-only arrays to copy into the image.  Returns false
+// when the layout needs more than smem_avail bytes or an SpMM of the tail
+// splits hub rows (its chunk partials would be shared by all CTAs).
+struct TailCopy {
+  const void *src;
+  size_t off, bytes;
+};
 template <typename T>
-void tail_prepare(Handle &H, Work<T> &W, size_t start) {
+bool tail_record(Handle &H, Work<T> &W, size_t start, int smem_avail, int kl,
+                 std::vector<TOp<T>> &ops, TailSmemLaunch &sl, std::vector<TailCopy> &consts) {
+  TailBuilder<T> B(H, W);
+  LevelWork<T> &top = W.lw[start];
+  B.recurse(start - 1, top.in.p, top.out.p);
+  ops = std::move(B.ops);
+  sl = TailSmemLaunch{};
+  consts.clear();
+  if (smem_avail <= 0) return true;
+  const int k = W.k;
+  for (const TOp<T> &op : ops)
+    if (op.kind == TOpKind::Spmm && op.A.nchunks > 0) return false;
+  // regions: global extent [base, base + gbytes), `bytes` of shared memory
+  struct Reg {
+    const char *base;
+    size_t gbytes, bytes;
+    long long off;
+    bool inside(const void *p) const {
+      const char *c = (const char *)p;
+      return c >= base && c < base + gbytes;
+    }
+  };
+  std::vector<Reg> vecs, scs, cons;  // n x k vectors (sliced), scalar slots, read-only arrays
+  for (size_t l = start; l < W.lw.size(); l++) {
+    LevelWork<T> &w = W.lw[l];
+    for (DBuf<T> *b : {&w.in, &w.out, &w.r, &w.d0, &w.d1, &w.xt, &w.fz, &w.fp0, &w.fp1, &w.fq0,
+                       &w.fq1})
+      if (b->p && b->n)
+        vecs.push_back({(const char *)b->p, sizeof(T) * (size_t)b->n,
+                        sizeof(T) * (size_t)(b->n / k * kl), -1});
+    if (w.sc.p && w.sc.n) {
+      const size_t nb = sizeof(double) * (size_t)w.sc.n;
+      scs.push_back({(const char *)w.sc.p, nb, nb, -1});
+    }
+    const Level &L = *H.h[l];
+    auto add = [&](const void *p, size_t bytes) {
+      if (p && bytes) cons.push_back({(const char *)p, bytes, bytes, -1});
+    };
+    const size_t n = (size_t)L.A.n, sv = sizeof(T);
+    add(L.A.rp.p, 8 * (n + 1));
+    add(L.A.ci.p, 4 * (size_t)L.A.nnz);
+    add(valsA<T>(L), sv * (size_t)L.A.nnz);
+    add(invdT<T>(L), sv * n);
+    if (L.type == LIGMG_LEVEL_AGG) {
+      add(L.agg.agg.p, 4 * n);
+      add(L.agg.mrp.p, 8 * ((size_t)L.nc + 1));
+      add(L.agg.members.p, 4 * n);
+      add(valsR<T>(L), sv * n);
+    } else if (L.type == LIGMG_LEVEL_ELIM) {
+      const DCsr<double> &R = L.elim.R, &P = L.elim.P;
+      add(R.rp.p, 8 * ((size_t)R.n + 1));
+      add(R.ci.p, 4 * (size_t)R.nnz);
+      add(valsR<T>(L), sv * (size_t)R.nnz);
+      add(P.rp.p, 8 * ((size_t)P.n + 1));
+      add(P.ci.p, 4 * (size_t)P.nnz);
+      if constexpr (sizeof(T) == 8) add(P.v.p, sv * (size_t)P.nnz);
+      else add(L.Pv32.p, sv * (size_t)P.nnz);
+      add(QT<T>(L), sv * n);
+    } else {
+      add(pinvT<T>(L), sv * n * n);
+    }
+  }
+  auto owner = [](std::vector<Reg> &regs, const void *p) -> Reg * {
+    if (!p) return nullptr;
+    for (Reg &r : regs)
+      if (r.inside(p)) return &r;
+    return nullptr;
+  };
+  auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  size_t total = up16(sizeof(TOp<T>) * ops.size());
+  auto claim = [&](Reg *r) {
+    if (r && r->off < 0) {
+      r->off = (long long)total;
+      total += up16(r->bytes);
+    }
+  };
+  auto vec_fields = [](TOp<T> &op, auto &&f) {
+    f(op.x0); f(op.x1); f(op.x2); f(op.y0); f(op.y1);
+    f(op.a.y); f(op.a.b); f(op.a.xin); f(op.a.xout); f(op.a.rin); f(op.a.rout);
+    f(op.a.din); f(op.a.dout);
+  };
+  auto sc_fields = [](TOp<T> &op, auto &&f) {
+    f(op.sc.mu); f(op.sc.beta); f(op.sc.eta); f(op.sc.eta_prev); f(op.sc.alpha);
+  };
+  auto con_fields = [](TOp<T> &op, auto &&f) {
+    f(op.A.rp); f(op.A.ci); f(op.A.v); f(op.a.invd); f(op.a.q); f(op.x1); f(op.idx);
+  };
+  // image first (program, then read-only arrays), then the writable regions
+  for (TOp<T> &op : ops)
+    con_fields(op, [&](auto &p) {
+      if (!owner(vecs, p)) claim(owner(cons, p));
+    });
+  sl.image_bytes = (int)total;
+  bool ok = true;
+  for (TOp<T> &op : ops) {
+    vec_fields(op, [&](auto &p) {
+      if (!p || owner(cons, p)) return;
+      Reg *r = owner(vecs, p);
+      if (!r) {
+        ok = false;  // a vector outside the tail's buffers
+        return;
+      }
+      if ((const char *)p != r->base) ok = false;  // slices need buffer bases
+      claim(r);
+    });
+    sc_fields(op, [&](auto &p) {
+      if (p) claim(owner(scs, p));
+    });
+  }
+  claim(owner(vecs, top.in.p));
+  claim(owner(vecs, top.out.p));
+  if (!ok || total > (size_t)smem_avail) return false;
+  auto tag = [](auto &p, long long off) {
+    p = reinterpret_cast<std::remove_reference_t<decltype(p)>>(kSmemTag | (unsigned long long)off);
+  };
+  for (TOp<T> &op : ops) {
+    con_fields(op, [&](auto &p) {
+      if (owner(vecs, p)) return;
+      Reg *r = owner(cons, p);
+      if (r) tag(p, r->off + ((const char *)p - r->base));
+    });
+    vec_fields(op, [&](auto &p) {
+      Reg *r = owner(vecs, p);
+      if (r) tag(p, r->off);
+    });
+    sc_fields(op, [&](auto &p) {
+      Reg *r = owner(scs, p);
+      if (r) tag(p, r->off + ((const char *)p - r->base));
+    });
+  }
+  for (const Reg &r : cons)
+    if (r.off >= 0) consts.push_back({r.base, (size_t)r.off, r.bytes});
+  sl.kl = kl;
+  sl.nops = (int)ops.size();
+  sl.smem = (int)std::max<size_t>(total, 16);
+  sl.gin = top.in.p;
+  sl.gout = top.out.p;
+  sl.n = H.h[start]->A.n;
+  sl.in_off = (unsigned)owner(vecs, top.in.p)->off;
+  sl.out_off = (unsigned)owner(vecs, top.out.p)->off;
+  return true;
+}
+
+// Columns per CTA tried by the shared-memory mode for k columns.
+inline std::vector<int> tail_slices(int k) {
+  std::vector<int> v;
+  for (int kl : {1, 4, 8})
+    if (kl <= k && k % kl == 0) v.push_back(kl);
+  return v;
+}
+
+// Decide the tail's start level (planning only; no program is kept).
+//   tail_rows > 0: grid-mode program from tail_start_level;
+//   tail_rows = 0: shared-memory program from the shallowest level whose
+//                  program, read-only arrays and one-column work-vector
+//                  slices fit in one CTA's shared memory;
+//   tail_rows < 0: none.
+template <typename T>
+void tail_plan(Handle &H, Work<T> &W) {
+  TailState<T> &ts = W.tail;
+  ts.planned = true;
+  ts.start = 0;
+  const i64 lim = H.opts.tail_rows;
+  if (lim < 0 || H.h.size() < 2) return;
+  if (H.h[0]->seginfo().nseg > 0) return;  // batch mode keeps per-graph kernels
+  if (lim > 0) {
+    if (tail_max_ctas<T>(W.k) <= 0) return;
+    ts.start = (int)tail_start_level(H);
+    return;
+  }
+  if (tail_slices(W.k).empty()) return;
+  const int avail = tail_smem_prepare<T>(1, 0);
+  std::vector<TOp<T>> ops;
+  std::vector<TailCopy> consts;
+  TailSmemLaunch sl;
+  for (size_t t = 1; t < H.h.size(); t++) {
+    if (tail_record<T>(H, W, t, avail, 1, ops, sl, consts)) {
+      ts.start = (int)t;
+      ts.smem_mode = true;
+      return;
+    }
+  }
+}
+
+// One launch of the current shape.
+template <typename T>
+void tail_launch(Handle &H, Work<T> &W, int G) {
+  TailState<T> &ts = W.tail;
+  if (ts.smem_mode) {
+    ts.sl.image = ts.image.p;
+    launch_tail_smem<T>(ts.sl, W.k, ts.sync.p, H.s);
+  } else {
+    launch_tail_grid<T>(ts.ops.p, ts.nops, W.k, G, ts.partial.p, ts.sync.p, H.s);
+  }
+}
+
+// Upload the shared-memory image of `kl` columns per CTA (program followed by
+// the read-only arrays).
+template <typename T>
+bool tail_build_smem(Handle &H, Work<T> &W, int kl) {
+  TailState<T> &ts = W.tail;
+  const int avail = tail_smem_prepare<T>(kl, 0);
+  std::vector<TOp<T>> ops;
+  std::vector<TailCopy> consts;
+  TailSmemLaunch sl;
+  if (!tail_record<T>(H, W, (size_t)ts.start, avail, kl, ops, sl, consts)) return false;
+  tail_smem_prepare<T>(kl, sl.smem);
+  ts.image.alloc(sl.image_bytes, H.s);
+  LG_CUDA(cudaMemcpyAsync(ts.image.p, ops.data(), sizeof(TOp<T>) * ops.size(),
+                          cudaMemcpyHostToDevice, H.s));
+  for (const TailCopy &c : consts)
+    LG_CUDA(cudaMemcpyAsync(ts.image.p + c.off, c.src, c.bytes, cudaMemcpyDeviceToDevice, H.s));
+  LG_CUDA(cudaStreamSynchronize(H.s));  // `ops` is pageable host memory
+  ts.sl = sl;
+  ts.nops = sl.nops;
+  return true;
+}
+
+// Build the program of the planned start level and pick its launch shape by
+// timing (grid mode: CTA count; shared-memory mode: columns per CTA).  The
+// restriction input bc is saved and restored around each timing run (the
+// program updates it).  best_ms: the chosen shape's time, for the autotune
+// choice against the launched levels.
+template <typename T>
+void tail_prepare(Handle &H, Work<T> &W) {
   TailState<T> &ts = W.tail;
   ts.tried = true;
   const int k = W.k;
   cudaStream_t s = H.s;
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  LG_CUDA(cudaStreamIsCapturing(s, &cs));
-  if (cs != cudaStreamCaptureStatusNone) return;
-  const int maxG = tail_max_ctas<T>(k);
-  if (maxG <= 0) return;
-  TailBuilder<T> B(H, W);
+  const size_t start = (size_t)ts.start;
   LevelWork<T> &top = W.lw[start];
-  B.recurse(start - 1, top.in.p, top.out.p);
-  ts.nops = (int)B.ops.size();
-  ts.ops.alloc(ts.nops, s);
-  ts.ops.upload(B.ops.data(), ts.nops);
+  const i64 nin = H.h[start]->A.n * k;
+  DBuf<T> save(nin, s);
+  LG_CUDA(cudaMemcpyAsync(save.p, top.in.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
   ts.sync.alloc(1, s);
   ts.sync.zero();
-  const int G0 = std::min(maxG, kSMs);
-  ts.partial.alloc((i64)G0 * 3 * k, s);
-  ts.start = (int)start;
-  ts.G = G0;
-  if (H.opts.autotune) {
-    const i64 nin = H.h[start]->A.n * k;
-    DBuf<T> save(nin, s);
-    LG_CUDA(cudaMemcpyAsync(save.p, top.in.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
-    cudaEvent_t e0, e1;
-    LG_CUDA(cudaEventCreate(&e0));
-    LG_CUDA(cudaEventCreate(&e1));
-    float best = 1e30f;
-    // one CTA (block barriers only) or several (grid barriers)
-    for (int G : {1, 4, 16, G0 / 4, G0}) {
-      if (G < 1 || G > G0) continue;
-      float tot = 0;
-      for (int rep = 0; rep < 3; rep++) {
-        LG_CUDA(cudaMemcpyAsync(top.in.p, save.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
-        LG_CUDA(cudaEventRecord(e0, s));
-        launch_tail<T>(ts.ops.p, ts.nops, k, G, ts.partial.p, ts.sync.p, s);
-        LG_CUDA(cudaEventRecord(e1, s));
-        LG_CUDA(cudaEventSynchronize(e1));
-        float ms = 0;
-        LG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (rep > 0) tot += ms;
+  ts.bytes = 2.0 * H.h[start]->A.n * k * sizeof(T);
+  for (size_t l = start; l < H.h.size(); l++)
+    ts.bytes += 8.0 * (H.h[l]->A.n + 1) + (double)H.h[l]->A.nnz * (4 + sizeof(T));
+  cudaEvent_t e0, e1;
+  LG_CUDA(cudaEventCreate(&e0));
+  LG_CUDA(cudaEventCreate(&e1));
+  auto time_once = [&](int G) {
+    float tot = 0;
+    for (int rep = 0; rep < 3; rep++) {
+      LG_CUDA(cudaMemcpyAsync(top.in.p, save.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
+      LG_CUDA(cudaEventRecord(e0, s));
+      tail_launch<T>(H, W, G);
+      LG_CUDA(cudaEventRecord(e1, s));
+      LG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      LG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (rep > 0) tot += ms;
+    }
+    return tot / 2;
+  };
+  float best = 1e30f;
+  if (ts.smem_mode) {
+    int best_kl = 0;
+    std::vector<int> kls = tail_slices(k);
+    if (!H.opts.autotune) kls = {kls.back()};  // fewest CTAs
+    for (int kl : kls) {
+      if (!tail_build_smem<T>(H, W, kl)) continue;
+      const float ms = time_once(0);
+      if (ms < best) {
+        best = ms;
+        best_kl = kl;
       }
-      if (tot < best) {
-        best = tot;
+    }
+    if (best_kl == 0) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return;
+    }
+    if (best_kl != ts.sl.kl) tail_build_smem<T>(H, W, best_kl);
+  } else {
+    std::vector<TOp<T>> ops;
+    std::vector<TailCopy> consts;
+    TailSmemLaunch unused;
+    tail_record<T>(H, W, start, 0, 0, ops, unused, consts);
+    ts.nops = (int)ops.size();
+    ts.ops.alloc(ts.nops, s);
+    ts.ops.upload(ops.data(), ts.nops);
+    LG_CUDA(cudaStreamSynchronize(s));
+    const int G0 = std::min(tail_max_ctas<T>(k), kSMs);
+    ts.partial.alloc((i64)G0 * 3 * k, s);
+    ts.G = G0;
+    std::vector<int> cands{G0};
+    if (H.opts.autotune) cands = {1, 4, 16, G0 / 4, G0};
+    for (int G : cands) {
+      if (G < 1 || G > G0) continue;
+      const float ms = time_once(G);
+      if (ms < best) {
+        best = ms;
         ts.G = G;
       }
     }
-    ts.best_ms = best / 2;
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    LG_CUDA(cudaMemcpyAsync(top.in.p, save.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
+  }
+  ts.best_ms = best;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  LG_CUDA(cudaMemcpyAsync(top.in.p, save.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
+  LG_CUDA(cudaStreamSynchronize(s));
+  // a barrier that gave up during the timing runs (never expected) turns the
+  // tail off rather than failing the solve
+  TailSync h{};
+  LG_CUDA(cudaMemcpy(&h, ts.sync.p, sizeof(TailSync), cudaMemcpyDeviceToHost));
+  if (h.err) {
+    ts.sync.zero();
     LG_CUDA(cudaStreamSynchronize(s));
+    return;
   }
   ts.on = true;
 }
@@ -1125,84 +1401,32 @@ struct Engine {
     fcg_fixed(l + 1, bc, xc, o().kcycle_iters);
   }
 
-  // Autotune: the launched path over the same levels, captured into a CUDA
-  // graph (as the solve replays it) and timed like the tail (bc saved and
-  // restored around each replay; the inner FCG updates it).
-  float time_launched(size_t start, T *bc, T *xc) {
-    const i64 nin = H.h[start]->A.n * k;
-    DBuf<T> save(nin, s);
-    LG_CUDA(cudaMemcpyAsync(save.p, bc, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
-    LG_CUDA(cudaStreamSynchronize(s));
-    const bool susp = H.prof.suspended;
-    H.prof.suspended = true;  // no profiler events inside this capture
-    const int64_t c0 = launches_now();
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    LG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    try {
-      recurse_launched(start - 1, bc, xc);
-    } catch (...) {
-      cudaStreamEndCapture(s, &graph);
-      if (graph) cudaGraphDestroy(graph);
-      H.prof.suspended = susp;
-      add_launches(c0 - launches_now());
-      throw;
-    }
-    H.prof.suspended = susp;
-    add_launches(c0 - launches_now());  // recorded, not run
-    LG_CUDA(cudaStreamEndCapture(s, &graph));
-    cudaError_t ierr = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    LG_CUDA(ierr);
-    cudaEvent_t e0, e1;
-    LG_CUDA(cudaEventCreate(&e0));
-    LG_CUDA(cudaEventCreate(&e1));
-    float tot = 0;
-    for (int rep = 0; rep < 3; rep++) {
-      LG_CUDA(cudaMemcpyAsync(bc, save.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
-      LG_CUDA(cudaEventRecord(e0, s));
-      LG_CUDA(cudaGraphLaunch(exec, s));
-      LG_CUDA(cudaEventRecord(e1, s));
-      LG_CUDA(cudaEventSynchronize(e1));
-      float ms = 0;
-      LG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      if (rep > 0) tot += ms;
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaGraphExecDestroy(exec);
-    LG_CUDA(cudaMemcpyAsync(bc, save.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
-    LG_CUDA(cudaStreamSynchronize(s));
-    return tot / 2;
-  }
-
   // The levels from `start` down as one persistent launch when that level
-  // starts the tail (program recorded on first use, outside graph capture).
+  // starts the tail (planned and built on first use, outside graph capture;
+  // with autotune, apply_prec keeps it only where a whole preconditioner
+  // application runs faster with it).
   bool try_tail(size_t start, T *bc, T *xc) {
     TailState<T> &ts = W.tail;
-    if (ts.tried && !ts.on) return false;
-    if (ts.on) {
-      if ((size_t)ts.start != start || bc != W.lw[start].in.p || xc != W.lw[start].out.p)
-        return false;
-    } else {
-      if (start != tail_start_level(H) || start == 0) return false;
-      if (H.h[start]->seginfo().nseg > 0) {  // batch mode keeps per-graph kernels
-        ts.tried = true;
-        return false;
-      }
-      if (bc != W.lw[start].in.p || xc != W.lw[start].out.p) return false;
-      tail_prepare<T>(H, W, start);
-      if (!ts.on) return false;
-      // keep the persistent kernel only where it beats the launched levels
-      // (it does when each level visit is latency-bound, e.g. k = 1)
-      if (o().autotune && time_launched(start, bc, xc) <= ts.best_ms) {
-        ts.on = false;
-        return false;
-      }
+    if (!ts.planned || !ts.tried) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      LG_CUDA(cudaStreamIsCapturing(s, &cs));
+      if (cs != cudaStreamCaptureStatusNone) return false;
     }
-    timed(H, (int)start, LIGMG_KERNEL_TAIL, k, sizeof(T) == 8, 0.0, [&] {
-      launch_tail<T>(ts.ops.p, ts.nops, k, ts.G, ts.partial.p, ts.sync.p, s);
-    });
+    if (!ts.planned) tail_plan<T>(H, W);
+    if (ts.start <= 0 || (size_t)ts.start != start) return false;
+    if (bc != W.lw[start].in.p || xc != W.lw[start].out.p) return false;
+    if (!ts.tried) {
+      tail_prepare<T>(H, W);
+      if (ts.on && o().verbose)
+        fprintf(stderr, "[ligmg] tail k=%d from level %zu (%s, %d ops, %d CTAs, %d B shared): "
+                        "%.1f us per visit alone\n",
+                k, start, ts.smem_mode ? "shared" : "grid", ts.nops,
+                ts.smem_mode ? k / ts.sl.kl : ts.G, ts.smem_mode ? ts.sl.smem : 0,
+                1e3 * ts.best_ms);
+    }
+    if (!ts.on) return false;
+    timed(H, (int)start, LIGMG_KERNEL_TAIL, k, sizeof(T) == 8, ts.bytes,
+          [&] { tail_launch<T>(H, W, ts.G); });
     return true;
   }
 
@@ -1556,8 +1780,43 @@ template <typename T>
 void apply_prec(Handle &H, int k, size_t base, const double *r, double *z, double *sum,
                 double *scratch, i64 scratch_len) {
   auto body = [&] { apply_prec_body<T>(H, k, base, r, z, sum, scratch, scratch_len); };
+  TailState<T> &ts = work_for<T>(H, k).tail;
+  // autotune: the persistent tail stays only if a whole application is
+  // faster with it (z is recomputed from r each time, so runs repeat)
+  auto decide_tail = [&](auto &&run_on, auto &&run_off) {
+    ts.decided = true;
+    cudaEvent_t e0, e1;
+    LG_CUDA(cudaEventCreate(&e0));
+    LG_CUDA(cudaEventCreate(&e1));
+    auto time3 = [&](auto &&run) {
+      run();
+      LG_CUDA(cudaEventRecord(e0, H.s));
+      run();
+      run();
+      LG_CUDA(cudaEventRecord(e1, H.s));
+      LG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      LG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      return ms / 2;
+    };
+    const float t_on = time3(run_on);
+    const float t_off = time3(run_off);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (H.opts.verbose)
+      fprintf(stderr, "[ligmg] preconditioner k=%d: %.1f us with the tail, %.1f us without\n",
+              k, 1e3 * t_on, 1e3 * t_off);
+    return t_on < t_off;
+  };
+  auto decide = [&] { return H.opts.autotune && ts.on && !ts.decided && !H.prof.on; };
   if (!H.opts.use_graphs) {
     body();
+    if (decide()) {
+      auto on = [&] { ts.on = true; body(); };
+      auto off = [&] { ts.on = false; body(); };
+      ts.on = decide_tail(on, off);
+      body();
+    }
     return;
   }
   PrecGraph &g = H.pgraphs[std::make_tuple(k, (int)sizeof(T), (int)base)];
@@ -1570,27 +1829,54 @@ void apply_prec(Handle &H, int k, size_t base, const double *r, double *z, doubl
   }
   g.reset();
   body();  // direct run: produces this application's result
-  cudaGraph_t graph = nullptr;
-  H.prof.capture_tmpl.clear();
-  H.prof.capturing = H.prof.on;
-  const int64_t c0 = launches_now();
-  LG_CUDA(cudaStreamBeginCapture(H.s, cudaStreamCaptureModeThreadLocal));
-  try {
-    body();
-  } catch (...) {
-    cudaStreamEndCapture(H.s, &graph);
-    if (graph) cudaGraphDestroy(graph);
+  auto capture = [&](int64_t &kernels) {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    H.prof.capture_tmpl.clear();
+    H.prof.capturing = H.prof.on;
+    const int64_t c0 = launches_now();
+    LG_CUDA(cudaStreamBeginCapture(H.s, cudaStreamCaptureModeThreadLocal));
+    try {
+      body();
+    } catch (...) {
+      cudaStreamEndCapture(H.s, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      H.prof.capturing = false;
+      add_launches(c0 - launches_now());
+      throw;
+    }
     H.prof.capturing = false;
-    add_launches(c0 - launches_now());
-    throw;
+    kernels = launches_now() - c0;
+    add_launches(-kernels);
+    LG_CUDA(cudaStreamEndCapture(H.s, &graph));
+    cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    LG_CUDA(e);
+    return exec;
+  };
+  const bool dec = decide();  // after the direct run, which prepares the tail
+  g.exec = capture(g.kernels);
+  if (dec) {
+    int64_t k_off = 0;
+    ts.on = false;
+    cudaGraphExec_t off = capture(k_off);
+    auto run_on = [&] {
+      LG_CUDA(cudaGraphLaunch(g.exec, H.s));
+      add_launches(g.kernels);
+    };
+    auto run_off = [&] {
+      LG_CUDA(cudaGraphLaunch(off, H.s));
+      add_launches(k_off);
+    };
+    if (decide_tail(run_on, run_off)) {
+      cudaGraphExecDestroy(off);
+      ts.on = true;
+    } else {
+      cudaGraphExecDestroy(g.exec);
+      g.exec = off;
+      g.kernels = k_off;
+    }
   }
-  H.prof.capturing = false;
-  g.kernels = launches_now() - c0;
-  add_launches(-g.kernels);
-  LG_CUDA(cudaStreamEndCapture(H.s, &graph));
-  cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
-  cudaGraphDestroy(graph);
-  LG_CUDA(e);
   g.r = r;
   g.z = z;
   g.prof = H.prof.on;

@@ -63,6 +63,18 @@ __device__ __forceinline__ void vstore(T *p, const T (&o)[VW]) {
   }
 }
 
+// matrix arrays: read-only cache loads from global memory (GX) or generic loads
+template <bool GX, typename V>
+__device__ __forceinline__ V mld(const V *p) {
+  if constexpr (GX) return __ldg(p);
+  else return *p;
+}
+template <typename T, int VW, bool GX>
+__device__ __forceinline__ void xload(const T *p, T (&o)[VW]) {
+  if constexpr (GX) vldg<T, VW>(p, o);
+  else vload<T, VW>(p, o);
+}
+
 template <typename T, int K, int VW, Epi E>
 __device__ __forceinline__ void epilogue(const EpiArgs &a, i64 r, int c0, T (&acc)[VW]) {
   const i64 off = r * K + c0;
@@ -123,21 +135,23 @@ __device__ __forceinline__ void epilogue(const EpiArgs &a, i64 r, int c0, T (&ac
   }
 }
 
-template <typename T, int K, int VW, int E>
+// GX: matrix and X in global memory (read-only cache loads); otherwise they
+// may be staged in shared memory and are read with generic loads.
+template <typename T, int K, int VW, int E, bool GX = true>
 __device__ __forceinline__ void row_accumulate(const MatView<T> &A, const T *__restrict__ X, i64 k,
                                                i64 e, int ch, T (&acc)[VW]) {
   const T *__restrict__ av = A.v;
   const i32 *__restrict__ ac = A.ci;
   for (; k + 3 * E < e; k += 4 * E) {
-    T a0 = __ldg(av + k), a1 = __ldg(av + k + E), a2 = __ldg(av + k + 2 * E),
-      a3 = __ldg(av + k + 3 * E);
-    i32 j0 = __ldg(ac + k), j1 = __ldg(ac + k + E), j2 = __ldg(ac + k + 2 * E),
-        j3 = __ldg(ac + k + 3 * E);
+    T a0 = mld<GX>(av + k), a1 = mld<GX>(av + k + E), a2 = mld<GX>(av + k + 2 * E),
+      a3 = mld<GX>(av + k + 3 * E);
+    i32 j0 = mld<GX>(ac + k), j1 = mld<GX>(ac + k + E), j2 = mld<GX>(ac + k + 2 * E),
+        j3 = mld<GX>(ac + k + 3 * E);
     T x0[VW], x1[VW], x2[VW], x3[VW];
-    vldg<T, VW>(X + (i64)j0 * K + ch * VW, x0);
-    vldg<T, VW>(X + (i64)j1 * K + ch * VW, x1);
-    vldg<T, VW>(X + (i64)j2 * K + ch * VW, x2);
-    vldg<T, VW>(X + (i64)j3 * K + ch * VW, x3);
+    xload<T, VW, GX>(X + (i64)j0 * K + ch * VW, x0);
+    xload<T, VW, GX>(X + (i64)j1 * K + ch * VW, x1);
+    xload<T, VW, GX>(X + (i64)j2 * K + ch * VW, x2);
+    xload<T, VW, GX>(X + (i64)j3 * K + ch * VW, x3);
 #pragma unroll
     for (int q = 0; q < VW; q++) acc[q] += a0 * x0[q];
 #pragma unroll
@@ -148,10 +162,10 @@ __device__ __forceinline__ void row_accumulate(const MatView<T> &A, const T *__r
     for (int q = 0; q < VW; q++) acc[q] += a3 * x3[q];
   }
   for (; k < e; k += E) {
-    T a0 = __ldg(av + k);
-    i32 j0 = __ldg(ac + k);
+    T a0 = mld<GX>(av + k);
+    i32 j0 = mld<GX>(ac + k);
     T x0[VW];
-    vldg<T, VW>(X + (i64)j0 * K + ch * VW, x0);
+    xload<T, VW, GX>(X + (i64)j0 * K + ch * VW, x0);
 #pragma unroll
     for (int q = 0; q < VW; q++) acc[q] += a0 * x0[q];
   }
@@ -169,7 +183,7 @@ __device__ __forceinline__ void reduce_slots(T (&acc)[VW]) {
 // rows) for warp < ceil(n / RPW), else hub chunk warp - ceil(n / RPW); the
 // warp that completes a hub row's last chunk sums the chunk partials in a
 // fixed order and runs the epilogue.
-template <typename T, int K, int G, Epi EP>
+template <typename T, int K, int G, Epi EP, bool GX = true>
 __device__ __forceinline__ void spmm_unit(const MatView<T> &A, const T *__restrict__ X,
                                           const EpiArgs &a, i64 warp, int lane) {
   constexpr int VW = (K % VT<T>::W == 0) ? VT<T>::W : 1;
@@ -191,7 +205,7 @@ __device__ __forceinline__ void spmm_unit(const MatView<T> &A, const T *__restri
       e = A.rp[r + 1];
       if (A.hub_thresh > 0 && e - b > A.hub_thresh) act = false;
     }
-    if (act) row_accumulate<T, K, VW, E>(A, X, b + slot, e, ch, acc);
+    if (act) row_accumulate<T, K, VW, E, GX>(A, X, b + slot, e, ch, acc);
     reduce_slots<T, VW, L, G>(acc);
     if (act && slot == 0) epilogue<T, K, VW, EP>(a, r, ch * VW, acc);
     return;
@@ -199,7 +213,7 @@ __device__ __forceinline__ void spmm_unit(const MatView<T> &A, const T *__restri
   if constexpr (G == 32) {
     const i64 c = warp - nregw;
     if (c >= A.nchunks) return;
-    row_accumulate<T, K, VW, E>(A, X, A.ch_beg[c] + slot, A.ch_end[c], ch, acc);
+    row_accumulate<T, K, VW, E, GX>(A, X, A.ch_beg[c] + slot, A.ch_end[c], ch, acc);
     reduce_slots<T, VW, L, G>(acc);
     if (slot == 0) vstore<T, VW>(A.partial + c * K + ch * VW, acc);
     __threadfence();

@@ -1,15 +1,24 @@
 // tail.cu — persistent kernel executing the recorded coarse-tail program.
 //
-// All G CTAs are resident (cooperative launch).  Operations run in program
-// order; between two operations every CTA passes a grid barrier, so an
-// operation sees all writes of the previous ones.  Work inside an operation:
-//   Spmm       warp units (rows, then hub chunks) strided over the G*32 warps,
-//              the same per-warp code as the launched SpMM (spmm_dev.cuh)
-//   elementwise  n*k elements strided over all G*1024 threads
+// Two modes.
+// Grid mode: all G CTAs are resident (cooperative launch) and cooperate on
+//   every operation; operations run in program order with a grid barrier
+//   between two operations, so an operation sees all writes of the previous
+//   ones.
+// Shared-memory mode: the columns of the k right-hand sides are independent
+//   through the whole cycle, so CTA g alone runs the program on columns
+//   [g*KL, (g+1)*KL): its slice of every work vector, a copy of the program
+//   and of every read-only array the program reads live in its shared memory;
+//   only block barriers are needed.  The start level's input slice is staged
+//   in at the beginning and its output slice written back at the end.
+// Work inside an operation (cooperating CTAs c = 0..C-1):
+//   Spmm        warp units (rows, then hub chunks) strided over the C*32
+//               warps, the same per-warp code as the launched SpMM
+//   elementwise n*KL elements strided over all C*NT threads
 //   RedBeta/RedAlpha  CTA c reduces rows [c*rpc, (c+1)*rpc) into partial[c]
-//   Dir/Update       every CTA sums the G partials in the same fixed order
-//              (so all CTAs hold identical scalars), CTA 0 publishes them, and
-//              the elementwise update follows without another barrier.
+//   Dir/Update  every CTA sums the C partials in the same fixed order (so all
+//               hold identical scalars), CTA 0 publishes them, and the
+//               elementwise update follows without another barrier.
 #include "spmm_dev.cuh"
 #include "tail.cuh"
 
@@ -22,9 +31,9 @@ constexpr long long kBarrierSpins = 1ll << 23;  // ~0.3 s at 32 ns a spin
 
 // Returns false when the barrier gave up (error recorded) or another CTA
 // reported an error: the caller leaves the kernel.
-__device__ __forceinline__ bool grid_barrier(TailSync *gs, int *sh_abort) {
+__device__ __forceinline__ bool grid_barrier(TailSync *gs, int *sh_abort, int ncta) {
   __syncthreads();
-  if (gridDim.x == 1) return true;  // one CTA: the block barrier orders everything
+  if (ncta == 1) return true;  // one cooperating CTA: the block barrier orders everything
   if (threadIdx.x == 0) {
     const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
     __threadfence();
@@ -50,14 +59,45 @@ __device__ __forceinline__ bool grid_barrier(TailSync *gs, int *sh_abort) {
   return *sh_abort == 0;
 }
 
-template <typename T, int K>
+// Shared-memory mode: the host tags pointers into the launch's dynamic shared
+// memory as kSmemTag | byte offset.
+extern __shared__ __align__(16) unsigned char tail_smem[];
+
+template <bool SM, typename P>
+__device__ __forceinline__ P *res(P *p) {
+  if constexpr (SM) {
+    const unsigned long long u = (unsigned long long)p;
+    if ((u & ~kSmemOffMask) == kSmemTag) return (P *)(tail_smem + (u & kSmemOffMask));
+  }
+  return p;
+}
+
+template <typename T, int K, bool SM>
 __device__ void run_spmm(const TOp<T> &op, i64 gwarp, i64 nwarps, int lane) {
   const i64 units = op.A.n + op.A.nchunks;
+  EpiArgs a = op.a;
+  MatView<T> A = op.A;
+  const T *X = res<SM>(op.x0);
+  if constexpr (SM) {
+    A.rp = res<SM>(A.rp);
+    A.ci = res<SM>(A.ci);
+    A.v = res<SM>(A.v);
+    a.invd = res<SM>(a.invd);
+    a.q = res<SM>(a.q);
+    a.y = res<SM>(a.y);
+    a.b = res<SM>(a.b);
+    a.xin = res<SM>(a.xin);
+    a.xout = res<SM>(a.xout);
+    a.rin = res<SM>(a.rin);
+    a.rout = res<SM>(a.rout);
+    a.din = res<SM>(a.din);
+    a.dout = res<SM>(a.dout);
+  }
   switch (op.epi) {
 #define LG_TAIL_EPI(E)                                                        \
   case E:                                                                     \
     for (i64 u = gwarp; u < units; u += nwarps)                               \
-      spmm_unit<T, K, 32, E>(op.A, op.x0, op.a, u, lane);                     \
+      spmm_unit<T, K, 32, E, !SM>(A, X, a, u, lane);                          \
     break;
     LG_TAIL_EPI(Epi::Store)
     LG_TAIL_EPI(Epi::Resid)
@@ -69,15 +109,16 @@ __device__ void run_spmm(const TOp<T> &op, i64 gwarp, i64 nwarps, int lane) {
   }
 }
 
-// CTA-level partial sums over this CTA's row range: NV values per column.
-template <typename T, int K, int NV>
-__device__ void block_partials(const T *x, const T *y, const T *w, bool use_y, i64 n,
-                               double *partial, double (*sh)[kTailThreads]) {
+// Partial sums over cooperating CTA `cta`'s row range: NV values per column.
+// One cooperating CTA: the totals stay in sh[v][c < K] for the next operation.
+template <typename T, int K, int NV, int NT>
+__device__ void block_partials(const T *x, const T *y, const T *w, bool use_y, i64 n, int cta,
+                               int ncta, double *partial, double (*sh)[NT]) {
   const int tid = threadIdx.x;
-  constexpr int RS = kTailThreads / K;
+  constexpr int RS = NT / K;
   const int c = tid % K, rsub = tid / K;
-  const i64 rpc = (n + gridDim.x - 1) / gridDim.x;
-  const i64 r0 = (i64)blockIdx.x * rpc, r1 = min(n, r0 + rpc);
+  const i64 rpc = (n + ncta - 1) / ncta;
+  const i64 r0 = (i64)cta * rpc, r1 = min(n, r0 + rpc);
   double a[NV];
 #pragma unroll
   for (int v = 0; v < NV; v++) a[v] = 0;
@@ -99,35 +140,36 @@ __device__ void block_partials(const T *x, const T *y, const T *w, bool use_y, i
 #pragma unroll
   for (int v = 0; v < NV; v++) sh[v][tid] = a[v];
   __syncthreads();
-  for (int st = kTailThreads / 2; st >= K; st >>= 1) {
+  for (int st = NT / 2; st >= K; st >>= 1) {
     if (tid < st)
 #pragma unroll
       for (int v = 0; v < NV; v++) sh[v][tid] += sh[v][tid + st];
     __syncthreads();
   }
-  if (tid < K)
+  if (ncta > 1 && tid < K)
 #pragma unroll
-    for (int v = 0; v < NV; v++) partial[((i64)blockIdx.x * 3 + v) * K + tid] = sh[v][tid];
+    for (int v = 0; v < NV; v++) partial[((i64)cta * 3 + v) * K + tid] = sh[v][tid];
 }
 
-// Sum of the G CTA partials (fixed order, identical in every CTA) into
-// sh[v][c] for c < K.
-template <int K, int NV>
-__device__ void finish_partials(const double *partial, double (*sh)[kTailThreads]) {
+// Sum of the cooperating CTAs' partials (fixed order, identical in every
+// CTA) into sh[v][c] for c < K.
+template <int K, int NV, int NT>
+__device__ void finish_partials(const double *partial, int ncta, double (*sh)[NT]) {
+  if (ncta == 1) return;  // totals left in sh by block_partials
   const int tid = threadIdx.x;
-  constexpr int RS = kTailThreads / K;
+  constexpr int RS = NT / K;
   const int c = tid % K, rsub = tid / K;
   double a[NV];
 #pragma unroll
   for (int v = 0; v < NV; v++) a[v] = 0;
-  for (unsigned b = rsub; b < gridDim.x; b += RS)
+  for (int b = rsub; b < ncta; b += RS)
 #pragma unroll
     for (int v = 0; v < NV; v++) a[v] += __ldcg(partial + ((i64)b * 3 + v) * K + c);
   __syncthreads();
 #pragma unroll
   for (int v = 0; v < NV; v++) sh[v][tid] = a[v];
   __syncthreads();
-  for (int st = kTailThreads / 2; st >= K; st >>= 1) {
+  for (int st = NT / 2; st >= K; st >>= 1) {
     if (tid < st)
 #pragma unroll
       for (int v = 0; v < NV; v++) sh[v][tid] += sh[v][tid + st];
@@ -135,113 +177,160 @@ __device__ void finish_partials(const double *partial, double (*sh)[kTailThreads
   }
 }
 
-template <typename T, int K>
-__global__ void __launch_bounds__(kTailThreads, 1)
-    k_tail(const TOp<T> *__restrict__ ops, int nops, double *partial, TailSync *gs) {
-  __shared__ double sh[3][kTailThreads];
+// Interface of a shared-memory launch: the start level's input and output
+// (n x kg, global) and their slices' offsets in shared memory (n x K).
+template <typename T>
+struct TailIO {
+  const T *gin;
+  T *gout;
+  i64 n;
+  int kg;
+  unsigned in_off, out_off;
+};
+
+// NT threads per CTA: 1024 in grid mode; 256 in shared-memory mode, where an
+// operation has little work and every warp pays its preamble (reading the
+// record, resolving its pointers).
+template <typename T, int K, bool SM, int NT>
+__global__ void __launch_bounds__(NT, 1)
+    k_tail(const TOp<T> *__restrict__ ops, int nops, double *partial, TailSync *gs,
+           const uint4 *__restrict__ image, int image_vec, TailIO<T> io) {
+  static_assert(NT % K == 0 && NT >= 64, "tail block size");
+  __shared__ double sh[3][NT];
   __shared__ double scal[2][64];
   __shared__ int sh_abort;
+  // cooperating CTAs: all of them (grid mode) or this one (shared-memory mode)
+  const int cta = SM ? 0 : (int)blockIdx.x;
+  const int ncta = SM ? 1 : (int)gridDim.x;
+  if constexpr (SM) {
+    // stage the program, the read-only arrays and this CTA's column slice of
+    // the start level's input
+    uint4 *dst = reinterpret_cast<uint4 *>(tail_smem);
+    for (int w = threadIdx.x; w < image_vec; w += NT) dst[w] = __ldg(image + w);
+    T *sin = reinterpret_cast<T *>(tail_smem + io.in_off);
+    const int c0 = (int)blockIdx.x * K;
+    for (i64 t = threadIdx.x; t < io.n * K; t += NT)
+      sin[t] = io.gin[(t / K) * io.kg + c0 + (t % K)];
+    __syncthreads();
+    ops = reinterpret_cast<const TOp<T> *>(tail_smem);
+  }
   const int lane = threadIdx.x & 31;
-  const i64 gwarp = ((i64)blockIdx.x * kTailThreads + threadIdx.x) >> 5;
-  const i64 nwarps = (i64)gridDim.x * (kTailThreads / 32);
-  const i64 gthr = (i64)blockIdx.x * kTailThreads + threadIdx.x;
-  const i64 nthr = (i64)gridDim.x * kTailThreads;
+  const i64 gwarp = ((i64)cta * NT + threadIdx.x) >> 5;
+  const i64 nwarps = (i64)ncta * (NT / 32);
+  const i64 gthr = (i64)cta * NT + threadIdx.x;
+  const i64 nthr = (i64)ncta * NT;
   for (int i = 0; i < nops; i++) {
     const TOp<T> &op = ops[i];
     const i64 nk = op.n * K;
+    const T *x0 = res<SM>(op.x0), *x1 = res<SM>(op.x1), *x2 = res<SM>(op.x2);
+    T *y0 = res<SM>(op.y0), *y1 = res<SM>(op.y1);
+    const i32 *idx = res<SM>(op.idx);
+    FcgScalars sc = op.sc;
+    if constexpr (SM) {
+      sc.mu = res<SM>(sc.mu);
+      sc.beta = res<SM>(sc.beta);
+      sc.eta = res<SM>(sc.eta);
+      sc.eta_prev = res<SM>(sc.eta_prev);
+      sc.alpha = res<SM>(sc.alpha);
+    }
     switch (op.kind) {
       case TOpKind::Spmm:
-        run_spmm<T, K>(op, gwarp, nwarps, lane);
+        run_spmm<T, K, SM>(op, gwarp, nwarps, lane);
         break;
       case TOpKind::Cheb0: {
         const T th = (T)op.f;
-        for (i64 t = gthr; t < nk; t += nthr) op.y0[t] = op.x1[t / K] * op.x0[t] / th;
+        for (i64 t = gthr; t < nk; t += nthr) y0[t] = x1[t / K] * x0[t] / th;
         break;
       }
       case TOpKind::Prolong:
-        for (i64 t = gthr; t < nk; t += nthr)
-          op.y0[t] += op.x0[(i64)op.idx[t / K] * K + (t % K)];
+        for (i64 t = gthr; t < nk; t += nthr) y0[t] += x0[(i64)idx[t / K] * K + (t % K)];
         break;
       case TOpKind::Coarse:
         for (i64 t = gthr; t < nk; t += nthr) {
           const i64 r = t / K;
           const int c = (int)(t % K);
           T s = 0;
-          for (i64 j = 0; j < op.n; j++) s += op.x1[r * op.n + j] * op.x0[j * K + c];
-          op.y0[t] = s;
+          for (i64 j = 0; j < op.n; j++) s += x1[r * op.n + j] * x0[j * K + c];
+          y0[t] = s;
         }
         break;
       case TOpKind::Scale: {
         const T f = (T)op.f;
-        for (i64 t = gthr; t < nk; t += nthr) op.y0[t] = op.y0[t] * f;
+        for (i64 t = gthr; t < nk; t += nthr) y0[t] = y0[t] * f;
         break;
       }
       case TOpKind::Zero:
-        for (i64 t = gthr; t < nk; t += nthr) op.y0[t] = (T)0;
+        for (i64 t = gthr; t < nk; t += nthr) y0[t] = (T)0;
         break;
       case TOpKind::Copy:
-        for (i64 t = gthr; t < nk; t += nthr) op.y0[t] = op.x0[t];
+        for (i64 t = gthr; t < nk; t += nthr) y0[t] = x0[t];
         break;
       case TOpKind::RedBeta:
-        block_partials<T, K, 3>(op.x0, op.x1, nullptr, op.flag != 0, op.n, partial, sh);
+        block_partials<T, K, 3, NT>(x0, x1, nullptr, op.flag != 0, op.n, cta, ncta, partial, sh);
         break;
       case TOpKind::RedAlpha:
-        block_partials<T, K, 2>(op.x0, op.x1, op.x2, true, op.n, partial, sh);
+        block_partials<T, K, 2, NT>(x0, x1, x2, true, op.n, cta, ncta, partial, sh);
         break;
       case TOpKind::Dir: {
-        finish_partials<K, 3>(partial, sh);
+        finish_partials<K, 3, NT>(partial, ncta, sh);
         if (threadIdx.x < K) {
           const int c = threadIdx.x;
           const double mu = sh[0][c] / (double)op.n;
           double beta = 0.0;
           if (op.flag) {
-            const double e = op.sc.eta_prev[c];
+            const double e = sc.eta_prev[c];
             beta = e == 0.0 ? 0.0 : (sh[1][c] - mu * sh[2][c]) / e;
           }
           scal[0][c] = mu;
           scal[1][c] = beta;
-          if (blockIdx.x == 0) {
-            op.sc.mu[c] = mu;
-            op.sc.beta[c] = beta;
+          if (cta == 0) {
+            sc.mu[c] = mu;
+            sc.beta[c] = beta;
           }
         }
         __syncthreads();
         for (i64 t = gthr; t < nk; t += nthr) {
           const int c = (int)(t % K);
-          T v = op.x0[t] - (T)scal[0][c];
-          if (op.flag) v = v - (T)scal[1][c] * op.x1[t];
-          op.y0[t] = v;
+          T v = x0[t] - (T)scal[0][c];
+          if (op.flag) v = v - (T)scal[1][c] * x1[t];
+          y0[t] = v;
         }
         break;
       }
       case TOpKind::Update: {
-        finish_partials<K, 2>(partial, sh);
+        finish_partials<K, 2, NT>(partial, ncta, sh);
         if (threadIdx.x < K) {
           const int c = threadIdx.x;
           const double eta = sh[0][c];
           const double alpha = eta == 0.0 ? 0.0 : sh[1][c] / eta;
           scal[0][c] = alpha;
-          if (blockIdx.x == 0) {
-            op.sc.eta[c] = eta;
-            op.sc.alpha[c] = alpha;
+          if (cta == 0) {
+            sc.eta[c] = eta;
+            sc.alpha[c] = alpha;
           }
         }
         __syncthreads();
         for (i64 t = gthr; t < nk; t += nthr) {
           const T a = (T)scal[0][(int)(t % K)];
-          op.y0[t] = op.y0[t] + a * op.x0[t];
-          if (op.flag) op.y1[t] = op.y1[t] - a * op.x1[t];
+          y0[t] = y0[t] + a * x0[t];
+          if (op.flag) y1[t] = y1[t] - a * x1[t];
         }
         break;
       }
     }
-    if (!grid_barrier(gs, &sh_abort)) return;
+    if (!grid_barrier(gs, &sh_abort, ncta)) return;
+  }
+  if constexpr (SM) {  // write this CTA's column slice of the output back
+    const T *sout = reinterpret_cast<const T *>(tail_smem + io.out_off);
+    const int c0 = (int)blockIdx.x * K;
+    for (i64 t = threadIdx.x; t < io.n * K; t += NT)
+      io.gout[(t / K) * io.kg + c0 + (t % K)] = sout[t];
   }
 }
 
 template <typename T, int K>
-void launch_k(const TOp<T> *ops, int nops, int G, double *partial, TailSync *sync,
-              cudaStream_t s) {
+void launch_grid(const TOp<T> *ops, int nops, int G, double *partial, TailSync *sync,
+                 cudaStream_t s) {
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeCooperative;
   at[0].val.cooperative = 1;
@@ -252,7 +341,17 @@ void launch_k(const TOp<T> *ops, int nops, int G, double *partial, TailSync *syn
   cfg.stream = s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  LG_CUDA(cudaLaunchKernelEx(&cfg, k_tail<T, K>, ops, nops, partial, sync));
+  TailIO<T> io{};
+  LG_CUDA(cudaLaunchKernelEx(&cfg, k_tail<T, K, false, kTailThreads>, ops, nops, partial, sync,
+                             (const uint4 *)nullptr, 0, io));
+  LG_LAUNCH();
+}
+
+template <typename T, int KL>
+void launch_smem(const TailSmemLaunch &L, int k, TailSync *sync, cudaStream_t s) {
+  TailIO<T> io{(const T *)L.gin, (T *)L.gout, L.n, k, L.in_off, L.out_off};
+  k_tail<T, KL, true, kTailSmemThreads><<<k / KL, kTailSmemThreads, L.smem, s>>>(
+      nullptr, L.nops, nullptr, sync, (const uint4 *)L.image, L.image_bytes / 16, io);
   LG_LAUNCH();
 }
 
@@ -261,21 +360,47 @@ int max_ctas_k() {
   int dev = 0, sms = 0, per = 0;
   LG_CUDA(cudaGetDevice(&dev));
   LG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  LG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tail<T, K>, kTailThreads, 0));
+  LG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tail<T, K, false, kTailThreads>,
+                                                        kTailThreads, 0));
   return per * sms;
+}
+
+template <typename T, int KL>
+int smem_limit_k(int want) {
+  int dev = 0, optin = 0;
+  LG_CUDA(cudaGetDevice(&dev));
+  LG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa{};
+  LG_CUDA(cudaFuncGetAttributes(&fa, k_tail<T, KL, true, kTailSmemThreads>));
+  const int avail = optin - (int)fa.sharedSizeBytes;
+  if (want > 0 && want <= avail)
+    LG_CUDA(cudaFuncSetAttribute(k_tail<T, KL, true, kTailSmemThreads>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, want));
+  return avail;
 }
 
 }  // namespace
 
 template <typename T>
-void launch_tail(const TOp<T> *ops, int nops, int k, int G, double *partial, TailSync *sync,
-                 cudaStream_t s) {
+void launch_tail_grid(const TOp<T> *ops, int nops, int k, int G, double *partial,
+                      TailSync *sync, cudaStream_t s) {
   switch (k) {
-    case 1: return launch_k<T, 1>(ops, nops, G, partial, sync, s);
-    case 8: return launch_k<T, 8>(ops, nops, G, partial, sync, s);
-    case 16: return launch_k<T, 16>(ops, nops, G, partial, sync, s);
-    case 32: return launch_k<T, 32>(ops, nops, G, partial, sync, s);
+    case 1: return launch_grid<T, 1>(ops, nops, G, partial, sync, s);
+    case 8: return launch_grid<T, 8>(ops, nops, G, partial, sync, s);
+    case 16: return launch_grid<T, 16>(ops, nops, G, partial, sync, s);
+    case 32: return launch_grid<T, 32>(ops, nops, G, partial, sync, s);
     default: throw Error(LIGMG_ERR_UNSUPPORTED, "tail program: k must be 1, 8, 16 or 32");
+  }
+}
+
+template <typename T>
+void launch_tail_smem(const TailSmemLaunch &L, int k, TailSync *sync, cudaStream_t s) {
+  if (L.kl <= 0 || k % L.kl != 0) throw Error(LIGMG_ERR_INTERNAL, "tail column slice");
+  switch (L.kl) {
+    case 1: return launch_smem<T, 1>(L, k, sync, s);
+    case 4: return launch_smem<T, 4>(L, k, sync, s);
+    case 8: return launch_smem<T, 8>(L, k, sync, s);
+    default: throw Error(LIGMG_ERR_UNSUPPORTED, "tail program: columns per CTA must be 1, 4 or 8");
   }
 }
 
@@ -290,11 +415,25 @@ int tail_max_ctas(int k) {
   }
 }
 
-template void launch_tail<float>(const TOp<float> *, int, int, int, double *, TailSync *,
-                                 cudaStream_t);
-template void launch_tail<double>(const TOp<double> *, int, int, int, double *, TailSync *,
-                                  cudaStream_t);
+template <typename T>
+int tail_smem_prepare(int kl, int bytes) {
+  switch (kl) {
+    case 1: return smem_limit_k<T, 1>(bytes);
+    case 4: return smem_limit_k<T, 4>(bytes);
+    case 8: return smem_limit_k<T, 8>(bytes);
+    default: return 0;
+  }
+}
+
+template void launch_tail_grid<float>(const TOp<float> *, int, int, int, double *, TailSync *,
+                                      cudaStream_t);
+template void launch_tail_grid<double>(const TOp<double> *, int, int, int, double *,
+                                       TailSync *, cudaStream_t);
+template void launch_tail_smem<float>(const TailSmemLaunch &, int, TailSync *, cudaStream_t);
+template void launch_tail_smem<double>(const TailSmemLaunch &, int, TailSync *, cudaStream_t);
 template int tail_max_ctas<float>(int);
 template int tail_max_ctas<double>(int);
+template int tail_smem_prepare<float>(int, int);
+template int tail_smem_prepare<double>(int, int);
 
 }  // namespace lg

@@ -2,12 +2,13 @@
 //
 // Below a size threshold every level visit of the K-/V-cycle is a handful of
 // small, dependent kernels; in a CUDA graph each costs a few microseconds of
-// launch and drain whatever its size, and the coarse levels are visited
-// exponentially often by the K-cycle.  The host records the exact operation
-// sequence of one visit of the tail (the same operations, pointers and
-// scalars the launched path would issue) as a program of TOp records; one
-// cooperative launch of k_tail executes the program with every CTA resident,
-// separated by software grid barriers.
+// launch and dependent memory latency whatever its size, and the coarse
+// levels are visited exponentially often by the K-cycle.  The host records
+// the exact operation sequence of one visit of the tail (the same operations,
+// pointers and scalars the launched path would issue) as a program of TOp
+// records; one launch of k_tail executes it, either by all CTAs with grid
+// barriers, or column slice by column slice, each CTA alone with everything
+// it touches in its shared memory.
 #pragma once
 #include "solve.cuh"
 
@@ -57,16 +58,45 @@ struct TailSync {
   int pad[2];
 };
 
-constexpr int kTailThreads = 1024;
+constexpr int kTailThreads = 1024;      // grid mode
+constexpr int kTailSmemThreads = 256;   // shared-memory mode
 
-// Launch the program (cooperative launch, G CTAs of kTailThreads threads).
-// partial: G x 3 x k doubles of reduction scratch.
+// Shared-memory mode: a pointer equal to kSmemTag | offset names byte
+// `offset` of the launch's dynamic shared memory; any other pointer is global.
+constexpr unsigned long long kSmemTag = 1ull << 62;
+constexpr unsigned long long kSmemOffMask = (1ull << 32) - 1;
+
+// Grid mode: cooperative launch of G CTAs of kTailThreads threads with grid
+// barriers, running `ops` from global memory (k columns).  partial: G x 3 x k
+// doubles of reduction scratch.
 template <typename T>
-void launch_tail(const TOp<T> *ops, int nops, int k, int G, double *partial, TailSync *sync,
-                 cudaStream_t s);
-// CTAs of kTailThreads threads that can be resident at once on this device
-// for the k-column program (0: the tail kernel is unavailable for k).
+void launch_tail_grid(const TOp<T> *ops, int nops, int k, int G, double *partial,
+                      TailSync *sync, cudaStream_t s);
+
+// Shared-memory mode: k / kl CTAs, CTA g on columns [g*kl, (g+1)*kl).  Each
+// copies `image` (the program followed by every read-only array the program
+// reads, image_bytes, a multiple of 16) to the start of its dynamic shared
+// memory (smem bytes in all), stages its slice of gin (n x k) at in_off,
+// runs the program and writes its slice of the result at out_off to gout.
+struct TailSmemLaunch {
+  int kl = 0, nops = 0, smem = 0, image_bytes = 0;
+  const void *image = nullptr;
+  const void *gin = nullptr;
+  void *gout = nullptr;
+  i64 n = 0;
+  unsigned in_off = 0, out_off = 0;
+};
+template <typename T>
+void launch_tail_smem(const TailSmemLaunch &L, int k, TailSync *sync, cudaStream_t s);
+
+// CTAs of kTailThreads threads that can be resident at once for the
+// k-column grid-mode kernel (0: unavailable for k).
 template <typename T>
 int tail_max_ctas(int k);
+// Shared-memory mode with kl columns per CTA: the dynamic shared memory
+// available to one CTA; when 0 < bytes <= that, the kernel is opted in to
+// `bytes`.  0: kl not available.
+template <typename T>
+int tail_smem_prepare(int kl, int bytes);
 
 }  // namespace lg

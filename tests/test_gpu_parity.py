@@ -80,14 +80,15 @@ def test_setup_options_bit_exact(opt):
         assert (S.level_matrix(l)[2].view(np.int64) == R.level_matrix(l)[2].view(np.int64)).all()
 
 
-@pytest.mark.parametrize("tail", [0, 1 << 20])
+@pytest.mark.parametrize("tail", [-1, 0, 1 << 20])
 @pytest.mark.parametrize("kcycle", [0, 1])
 @pytest.mark.parametrize("name", ["grid48_logn", "my_matrix", "rmat12", "grid3d_12"])
 def test_cycle_fp64_matches_oracle(name, kcycle, tail):
-    # tail > 0: the levels below the first one run as the persistent kernel
-    # (autotune off, so it is used whatever its speed)
+    # tail -1: every level launched; 0: the coarse end as the shared-memory
+    # program; 1 << 20: every level below the first as the grid-barrier
+    # program (autotune off, so the tail runs whatever its speed)
     L = GRAPHS[name]()
-    S = Solver(L, kcycle=kcycle, tail_rows=tail, autotune=0 if tail else 1)
+    S = Solver(L, kcycle=kcycle, tail_rows=tail, autotune=0 if tail >= 0 else 1)
     R = O.OracleSolver(L, kcycle=kcycle)
     rng = np.random.default_rng(7)
     for level in range(R.num_levels):
@@ -183,17 +184,20 @@ def test_graph_replay_matches_direct_launches():
     assert np.array_equal(a.solution, b.solution)
 
 
-@pytest.mark.parametrize("prec,k", [("fp32", 32), ("fp32", 8), ("fp64", 1), ("fp32", 1)])
+@pytest.mark.parametrize("prec,k", [("fp32", 32), ("fp32", 8), ("fp64", 1), ("fp32", 1),
+                                    ("fp32", 4), ("fp32", 2), ("fp64", 2)])
 def test_persistent_tail_matches_launched_levels(prec, k):
-    # tail_rows = 0: every level launches its own kernels; the default runs
-    # the coarse end as one persistent kernel.  Same operations, so the same
+    # tail_rows = -1: every level launches its own kernels; otherwise the
+    # coarse end runs as one persistent kernel (grid barriers for > 0; for 0,
+    # column slices of 8, 4 or 1 columns per CTA in shared memory: k = 32 and
+    # 8 use 8, k = 4 uses 4, k = 2 and 1 use 1).  Same operations, so the same
     # iterations and solutions equal to rounding of the reductions.
     L = GRAPHS["rmat14"]()
     B = G.rhs(L.n, k=k, seed=9)
     if k == 1:
         B = B.reshape(L.n, 1)
     kw = dict(precision=prec, kcycle=1, outer_ksp_type="fcg", autotune=0)
-    a = Solver(L, tail_rows=0, **kw).solve_batched(B)
+    a = Solver(L, tail_rows=-1, **kw).solve_batched(B)
     b = Solver(L, tail_rows=1 << 20, **kw).solve_batched(B)
     assert a.converged and b.converged
     assert a.iters() == b.iters()
@@ -202,6 +206,12 @@ def test_persistent_tail_matches_launched_levels(prec, k):
     c = Solver(L, tail_rows=500, **kw).solve_batched(B)  # a shorter tail
     assert c.converged and c.iters() == a.iters()
     assert _relerr(a.solution, c.solution) <= tol
+    d = Solver(L, tail_rows=0, **kw)  # shared-memory column slices
+    S = d.solve_batched(B)
+    assert S.converged and S.iters() == a.iters()
+    assert _relerr(a.solution, S.solution) <= tol
+    S2 = d.solve_batched(B)  # replayed from the captured graph: identical
+    assert np.array_equal(S.solution, S2.solution)
 
 
 def test_autotuned_shapes_match_fixed_shapes():
