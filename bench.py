@@ -368,8 +368,11 @@ def run_ours(args):
     if rank != 0:
         return
     peak, peak_kind = peaks()
-    # the dominant single kernel (krylov / vector / outer entries group several)
-    single = [r for r in stats if r["kind"] not in ("krylov", "vector", "outer")]
+    # the dominant bandwidth-bound kernel (krylov / vector / outer entries group
+    # several kernels; the persistent coarse-tail kernel is issue-bound, one SM
+    # per column slice, and is reported on its own in config.tail)
+    single = [r for r in stats if r["kind"] not in ("krylov", "vector", "outer", "tail")]
+    tails = [r for r in stats if r["kind"] == "tail"]
     top = max(single, key=lambda r: r["seconds"]) if single else None
     roof = None
     if top:
@@ -415,6 +418,11 @@ def run_ours(args):
             "profile_ms_per_step_by_level": by_key(stats, "level", args.steps),
             "profile_ms_per_step_by_kind": by_key(stats, "kind", args.steps),
             "profiled_ms_per_step": profiled_ms / args.steps,
+            "tail": ({"level": tails[0]["level"], "launches_per_step": tails[0]["launches"] / args.steps,
+                      "us_per_launch": 1e6 * tails[0]["seconds"] / tails[0]["launches"],
+                      "share_of_profiled": tails[0]["seconds"] / (profiled_ms / 1e3),
+                      "note": "coarse levels from `level` down as one persistent kernel in "
+                              "shared memory (kept by the autotuner)"} if tails else None),
             "profile_table": [[r["level"], r["kind"], round(r["launches"] / args.steps, 1),
                                round(r["seconds"] * 1e3 / args.steps, 3)]
                               for r in sorted(stats, key=lambda r: -r["seconds"])],

@@ -702,6 +702,7 @@ struct TailBuilder {
   int k;
   cudaStream_t s;
   std::vector<TOp<T>> ops;
+  bool whole_rows = false;  // no hub-row chunks: one warp takes each row
   TailBuilder(Handle &h, Work<T> &w) : H(h), W(w), k(w.k), s(h.s) {}
   const ligmg_options &o() const { return H.opts; }
 
@@ -711,6 +712,10 @@ struct TailBuilder {
     op.epi = e;
     op.n = A.n;
     op.A = A;
+    if (whole_rows) {
+      op.A.hub_thresh = 0;
+      op.A.nchunks = 0;
+    }
     op.x0 = X;
     op.a = a;
     ops.push_back(op);
@@ -911,9 +916,10 @@ inline size_t tail_start_level(const Handle &H) {
 // (the start level's input and output included: staged in and out); each
 // CTA holds an n x kl slice of each (the Krylov scalar slots whole).  The
 // program's pointers into them are rewritten as kSmemTag | offset.
-// `consts` lists the read-only arrays to copy into the image.  Returns false
-// when the layout needs more than smem_avail bytes or an SpMM of the tail
-// splits hub rows (its chunk partials would be shared by all CTAs).
+// `consts` lists the read-only arrays to copy into the image; every row of
+// the tail's SpMMs is taken whole by one warp (no hub chunks, whose partials
+// are global and would be shared by the CTAs).  Returns false when the layout
+// needs more than smem_avail bytes.
 struct TailCopy {
   const void *src;
   size_t off, bytes;
@@ -922,6 +928,7 @@ template <typename T>
 bool tail_record(Handle &H, Work<T> &W, size_t start, int smem_avail, int kl,
                  std::vector<TOp<T>> &ops, TailSmemLaunch &sl, std::vector<TailCopy> &consts) {
   TailBuilder<T> B(H, W);
+  B.whole_rows = smem_avail > 0;  // a CTA of its own: the chunk partials are global
   LevelWork<T> &top = W.lw[start];
   B.recurse(start - 1, top.in.p, top.out.p);
   ops = std::move(B.ops);
@@ -929,8 +936,6 @@ bool tail_record(Handle &H, Work<T> &W, size_t start, int smem_avail, int kl,
   consts.clear();
   if (smem_avail <= 0) return true;
   const int k = W.k;
-  for (const TOp<T> &op : ops)
-    if (op.kind == TOpKind::Spmm && op.A.nchunks > 0) return false;
   // regions: global extent [base, base + gbytes), `bytes` of shared memory
   struct Reg {
     const char *base;
