@@ -281,6 +281,24 @@ ligmg_status ligmg_get_stream(ligmg_handle h, void **stream);
  * from the library's CUDA graphs are counted on every replay). */
 ligmg_status ligmg_launch_count(int64_t *count);
 
+/* Input preparation on the GPU (the reference CLI's --cc / --adj steps,
+ * src/main.cpp:70-110, with largest_cc of include/ligmg/cc.hpp:24-106).
+ * Input: a host CSR with ascending columns and a symmetric pattern.
+ * LIGMG_PREP_LCC keeps the largest connected component (a tie goes to the
+ * component whose largest vertex index is smallest), vertices renumbered in
+ * ascending order, entries between kept vertices kept in order;
+ * LIGMG_PREP_LAPLACIAN then treats the matrix as weighted adjacency and
+ * returns L = D - A, D the row sums (ascending column order).  Two-call
+ * protocol: with rowptr_out/col_out/val_out null only *n_out and *nnz_out
+ * are written; orig_out (nullable, n_out entries) receives each kept
+ * vertex's input index.  Runs on `device` (its own stream); synchronous. */
+#define LIGMG_PREP_LCC 1
+#define LIGMG_PREP_LAPLACIAN 2
+ligmg_status ligmg_prepare_graph(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                 const double *val, int32_t flags, int32_t device,
+                                 int64_t *n_out, int64_t *nnz_out, int64_t *rowptr_out,
+                                 int32_t *col_out, double *val_out, int64_t *orig_out);
+
 /* Jacobi-preconditioned CG on the input matrix (the reference's own
  * comparison solver, --test-cg: src/main.cpp:168-180 with the InvDiagSR
  * preconditioner z = D^-1 r, smoothing.hpp:56-76), FP64, rtol opts.tol,

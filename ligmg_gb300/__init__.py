@@ -5,4 +5,4 @@ ABI in include/ligmg_gpu.h); this package is its host-side mirror of the
 reference interface ligmg::Solver(A) / solve(b).
 """
 from ._abi import Info, Options, default_options  # noqa: F401
-from .solver import BatchSolver, ConvergenceInfo, Solver  # noqa: F401
+from .solver import BatchSolver, ConvergenceInfo, Solver, prepare_graph  # noqa: F401

@@ -73,6 +73,8 @@ def lib(path=None):
     L.ligmg_spmv_device_noalloc.argtypes = [vp, C.c_int32, vp, vp]
     L.ligmg_forward.argtypes = [vp, vp, vp, P(Info)]
     L.ligmg_solve_pcg_jacobi.argtypes = [vp, vp, vp, P(Info)]
+    L.ligmg_prepare_graph.argtypes = [C.c_int64, vp, vp, vp, C.c_int32, C.c_int32,
+                                      P(C.c_int64), P(C.c_int64), vp, vp, vp, vp]
     L.ligmg_level_prolongation.argtypes = [vp, C.c_int32, P(C.c_int64), vp, vp, vp, vp]
     L.ligmg_import_hierarchy.argtypes = [C.c_int32, P(LevelDesc), P(Options), P(vp)]
     L.ligmg_batch_create.argtypes = [C.c_int32, vp, vp, vp, vp, P(Options), P(vp)]

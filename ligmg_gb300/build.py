@@ -24,6 +24,7 @@ UNITS = {
     "setup.cu": ["--fmad=false"],
     "solve.cu": [],
     "tail.cu": [],
+    "prep.cu": [],
     "api.cu": [],
 }
 

@@ -20,6 +20,7 @@
 #include "prims.cuh"
 #include "setup.cuh"
 #include "solve.cuh"
+#include "prep.cuh"
 #include "tail.cuh"
 
 namespace lg {
@@ -2468,6 +2469,42 @@ ligmg_status ligmg_backward(ligmg_handle h, const double *g, double *dw, double 
     if (db) lam.download(db, n);
     LG_CUDA(cudaStreamSynchronize(h->s));
     return st;
+  });
+}
+
+ligmg_status ligmg_prepare_graph(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                 const double *val, int32_t flags, int32_t device,
+                                 int64_t *n_out, int64_t *nnz_out, int64_t *rowptr_out,
+                                 int32_t *col_out, double *val_out, int64_t *orig_out) {
+  if (n <= 0 || !rowptr || !col || !val || !n_out || !nnz_out ||
+      (flags & ~(LIGMG_PREP_LCC | LIGMG_PREP_LAPLACIAN)))
+    return LIGMG_ERR_INVALID_ARGUMENT;
+  const bool arrays = rowptr_out || col_out || val_out;
+  if (arrays && !(rowptr_out && col_out && val_out)) return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    LG_CUDA(cudaSetDevice(device));
+    cudaStream_t s = nullptr;
+    LG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    PrepResult r;
+    try {
+      prepare_graph(n, rowptr, col, val, (flags & LIGMG_PREP_LCC) != 0,
+                    (flags & LIGMG_PREP_LAPLACIAN) != 0, arrays || orig_out, r, s);
+    } catch (...) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+      throw;
+    }
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    *n_out = r.n;
+    *nnz_out = r.nnz;
+    if (arrays) {
+      std::copy(r.rowptr.begin(), r.rowptr.end(), rowptr_out);
+      std::copy(r.col.begin(), r.col.end(), col_out);
+      std::copy(r.val.begin(), r.val.end(), val_out);
+    }
+    if (orig_out) std::copy(r.orig.begin(), r.orig.end(), orig_out);
+    return LIGMG_OK;
   });
 }
 

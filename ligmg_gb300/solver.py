@@ -336,6 +336,30 @@ class Solver:
                 f"{info.wda()},{setup_time},{info.time()},{nnz},1\n")
 
 
+def prepare_graph(n, rowptr, col, val, lcc=True, laplacian=False, device=0):
+    """The reference CLI's input steps on the GPU (ligmg_prepare_graph):
+    keep the largest connected component (lcc) and/or turn a weighted
+    adjacency matrix into its Laplacian (laplacian).  Returns
+    (graphs.Laplacian, orig) with orig[i] the input index of vertex i."""
+    from .graphs import Laplacian
+    rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    val = np.ascontiguousarray(val, dtype=np.float64)
+    flags = (1 if lcc else 0) | (2 if laplacian else 0)
+    nk, nnz = C.c_int64(), C.c_int64()
+    check(lib().ligmg_prepare_graph(n, _p(rowptr), _p(col), _p(val), flags, device,
+                                    C.byref(nk), C.byref(nnz), None, None, None, None),
+          "ligmg_prepare_graph")
+    rp = np.empty(nk.value + 1, np.int64)
+    ci = np.empty(nnz.value, np.int32)
+    cv = np.empty(nnz.value, np.float64)
+    orig = np.empty(nk.value, np.int64)
+    check(lib().ligmg_prepare_graph(n, _p(rowptr), _p(col), _p(val), flags, device,
+                                    C.byref(nk), C.byref(nnz), _p(rp), _p(ci), _p(cv),
+                                    _p(orig)), "ligmg_prepare_graph")
+    return Laplacian(int(nk.value), rp, ci, cv, "prepared"), orig
+
+
 class BatchSolver:
     """A batch of independent graph Laplacians solved together
     (ligmg_batch_create / ligmg_batch_solve): one block-diagonal hierarchy,

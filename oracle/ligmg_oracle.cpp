@@ -1301,4 +1301,93 @@ int orc_solve(orc_handle H, const double *b, double *x, int from, ligmg_info *in
   return st;
 }
 
+// Input preparation (the reference CLI's --cc then --adj, src/main.cpp:70-110).
+// largest_cc (include/ligmg/cc.hpp:24-106): label = iota; repeat
+// label' = max(label, max over the row's neighbours of label) (the MaxSRing
+// SpMV of cc.hpp:40-50) until nothing changes; count vertices per label; the
+// first label with the largest count (max_element, cc.hpp:67-68); renumber
+// its vertices in ascending order and keep the entries between them
+// (cc.hpp:74-100).  adjacency -> Laplacian (main.cpp:81-106): d_i = row sum
+// (sequential, ascending columns), L = D - A (EWiseApply union with 0).
+// Two-call protocol like ligmg_prepare_graph.
+int orc_prepare_graph(int64_t n, const int64_t *rowptr, const int32_t *col, const double *val,
+                      int32_t flags, int64_t *n_out, int64_t *nnz_out, int64_t *rowptr_out,
+                      int32_t *col_out, double *val_out, int64_t *orig_out) {
+  if (n <= 0) return LIGMG_ERR_INVALID_ARGUMENT;
+  std::vector<int32_t> keep(n, 1);
+  if (flags & LIGMG_PREP_LCC) {
+    std::vector<int64_t> cc(n), old;
+    for (int64_t i = 0; i < n; i++) cc[i] = i;
+    while (true) {
+      old = cc;
+      bool same = true;
+      for (int64_t i = 0; i < n; i++) {
+        int64_t m = old[i];
+        for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++) m = std::max(m, old[col[k]]);
+        cc[i] = m;
+        if (m != old[i]) same = false;
+      }
+      if (same) break;
+    }
+    std::vector<uint64_t> counts(n, 0);
+    for (int64_t i = 0; i < n; i++) counts[cc[i]]++;
+    const int64_t best = std::max_element(counts.begin(), counts.end()) - counts.begin();
+    for (int64_t i = 0; i < n; i++) keep[i] = cc[i] == best;
+  }
+  std::vector<int64_t> nid(n, -1);
+  int64_t nk = 0;
+  for (int64_t i = 0; i < n; i++)
+    if (keep[i]) nid[i] = nk++;
+  const bool lap = (flags & LIGMG_PREP_LAPLACIAN) != 0;
+  std::vector<int64_t> rp(1, 0);
+  std::vector<int32_t> ci;
+  std::vector<double> v;
+  std::vector<int64_t> orig;
+  for (int64_t i = 0; i < n; i++) {
+    if (!keep[i]) continue;
+    const int64_t r = nid[i];
+    orig.push_back(i);
+    double d = 0.0;
+    if (lap)
+      for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++)
+        if (keep[col[k]]) d += val[k];
+    bool placed = false;
+    for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++) {
+      const int32_t j = col[k];
+      if (!keep[j]) continue;
+      const int64_t c = nid[j];
+      if (lap && !placed && c > r) {
+        ci.push_back((int32_t)r);
+        v.push_back(d);
+        placed = true;
+      }
+      double x = val[k];
+      if (lap) {
+        if (c == r) {
+          x = d - x;
+          placed = true;
+        } else {
+          x = -x;
+        }
+      }
+      ci.push_back((int32_t)c);
+      v.push_back(x);
+    }
+    if (lap && !placed) {
+      ci.push_back((int32_t)r);
+      v.push_back(d);
+    }
+    rp.push_back((int64_t)ci.size());
+  }
+  *n_out = nk;
+  *nnz_out = (int64_t)ci.size();
+  if (rowptr_out) {
+    std::copy(rp.begin(), rp.end(), rowptr_out);
+    std::copy(ci.begin(), ci.end(), col_out);
+    std::copy(v.begin(), v.end(), val_out);
+  }
+  if (orig_out) std::copy(orig.begin(), orig.end(), orig_out);
+  return LIGMG_OK;
+}
+
 }  // extern "C"

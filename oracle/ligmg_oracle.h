@@ -67,6 +67,11 @@ int orc_galerkin(int64_t n, const int64_t *rowptr, const int32_t *col,
                  const double *val, int64_t nc, const int64_t *prow,
                  const int32_t *pcol, const double *pval, int64_t *nnz_out,
                  int64_t *crow, int32_t *ccol, double *cval);
+/* --cc / --adj input preparation (largest connected component, adjacency ->
+ * Laplacian); same arguments and two-call protocol as ligmg_prepare_graph. */
+int orc_prepare_graph(int64_t n, const int64_t *rowptr, const int32_t *col, const double *val,
+                      int32_t flags, int64_t *n_out, int64_t *nnz_out, int64_t *rowptr_out,
+                      int32_t *col_out, double *val_out, int64_t *orig_out);
 /* OpenMP threads used by the oracle (<=0: all cores). Returns the count. */
 int orc_set_threads(int nthreads);
 

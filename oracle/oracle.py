@@ -54,6 +54,8 @@ def lib():
         L.orc_galerkin.argtypes = [C.c_int64, vp, vp, vp, C.c_int64, vp, vp, vp,
                                    P(C.c_int64), vp, vp, vp]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_prepare_graph.argtypes = [C.c_int64, vp, vp, vp, C.c_int32, P(C.c_int64),
+                                        P(C.c_int64), vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -92,6 +94,27 @@ def galerkin(L, nc, prow, pcol, pval):
     lib().orc_galerkin(L.n, _p(L.rowptr), _p(L.col), _p(L.val), nc, _p(prow), _p(pcol),
                        _p(pval), C.byref(nnz), _p(rp), _p(ci), _p(cv))
     return rp, ci, cv
+
+
+def prepare_graph(n, rowptr, col, val, lcc=True, laplacian=False):
+    """Largest connected component and/or adjacency -> Laplacian (the reference
+    CLI's --cc and --adj): (rowptr, col, val, orig)."""
+    rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    val = np.ascontiguousarray(val, dtype=np.float64)
+    flags = (1 if lcc else 0) | (2 if laplacian else 0)
+    nk, nnz = C.c_int64(), C.c_int64()
+    lib().orc_prepare_graph(n, _p(rowptr), _p(col), _p(val), flags, C.byref(nk), C.byref(nnz),
+                            None, None, None, None)
+    rp = np.empty(nk.value + 1, np.int64)
+    ci = np.empty(nnz.value, np.int32)
+    cv = np.empty(nnz.value, np.float64)
+    orig = np.empty(nk.value, np.int64)
+    st = lib().orc_prepare_graph(n, _p(rowptr), _p(col), _p(val), flags, C.byref(nk),
+                                 C.byref(nnz), _p(rp), _p(ci), _p(cv), _p(orig))
+    if st:
+        raise OracleError(st)
+    return rp, ci, cv, orig
 
 
 class OracleError(RuntimeError):

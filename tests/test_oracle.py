@@ -176,3 +176,44 @@ def test_invalid_inputs_rejected():
     v[1] = 1.0  # positive off-diagonal, breaks symmetry too
     with pytest.raises(O.OracleError):
         O.OracleSolver(G.Laplacian(L.n, L.rowptr, L.col, v))
+
+
+def _adjacency(L):
+    """Off-diagonal part of a Laplacian as a weighted adjacency CSR."""
+    A = -L.to_scipy().tocoo()
+    m = A.row != A.col
+    import scipy.sparse as sp
+    A = sp.csr_matrix((A.data[m], (A.row[m], A.col[m])), shape=L.to_scipy().shape)
+    A.sort_indices()
+    return A.indptr.astype(np.int64), A.indices.astype(np.int32), A.data.astype(np.float64)
+
+
+def test_prepare_graph_matches_host_pipeline():
+    # R-MAT without the component step has many components; the oracle's
+    # --cc/--adj pipeline must give the host generator's LCC Laplacian
+    for scale, seed in [(10, 3), (12, 1)]:
+        raw = G.rmat(scale, seed=seed, lcc=False)
+        ref = G.rmat(scale, seed=seed, lcc=True)
+        rp, ci, cv = _adjacency(raw)
+        orp, oci, ocv, orig = O.prepare_graph(raw.n, rp, ci, cv, lcc=True, laplacian=True)
+        assert len(orp) - 1 == ref.n
+        assert np.array_equal(orp, ref.rowptr) and np.array_equal(oci, ref.col)
+        assert np.allclose(ocv, ref.val, rtol=1e-14, atol=0)
+        assert np.all(np.diff(orig) > 0)
+        # laplacian rows sum to zero; lcc-only keeps the input entries
+        assert np.abs(ref.to_scipy() @ np.ones(ref.n)).max() <= 1e-12 * np.abs(ref.val).max()
+        lrp, lci, lcv, _ = O.prepare_graph(raw.n, raw.rowptr, raw.col, raw.val, lcc=True)
+        assert np.array_equal(lrp, ref.rowptr) and np.array_equal(lci, ref.col)
+
+
+def test_prepare_graph_tie_takes_smaller_label():
+    # two paths of 3 vertices: {0, 2, 4} and {1, 3, 5}; labels (largest index)
+    # 4 and 5; equal sizes -> the component labelled 4 (max_element, cc.hpp)
+    import scipy.sparse as sp
+    u = np.array([0, 2, 1, 3])
+    v = np.array([2, 4, 3, 5])
+    A = sp.coo_matrix((np.ones(4), (u, v)), shape=(6, 6))
+    A = (A + A.T).tocsr()
+    A.sort_indices()
+    rp, ci, cv, orig = O.prepare_graph(6, A.indptr, A.indices, A.data, lcc=True)
+    assert list(orig) == [0, 2, 4] and len(rp) == 4 and len(ci) == 4
