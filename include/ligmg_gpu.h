@@ -73,6 +73,7 @@ typedef int ligmg_status;
 #define LIGMG_STRENGTH_NONE 2
 #define LIGMG_KSP_CG 0
 #define LIGMG_KSP_FCG 1
+#define LIGMG_KSP_FGMRES 2  /* flexible GMRES(gmres_restart), right preconditioned */
 #define LIGMG_PREC_FP64 0   /* hierarchy, smoothers and cycle in FP64 */
 #define LIGMG_PREC_FP32 1   /* FP32 hierarchy/cycle inside the FP64 outer Krylov */
 
@@ -142,6 +143,7 @@ typedef struct ligmg_options {
                                  from the first level below which every level
                                  has at most this many rows; < 0: every level
                                  launches its own kernels */
+  int32_t gmres_restart;      /* FGMRES restart length (30, PETSc's default) */
 } ligmg_options;
 
 /* ConvergenceInfo (util.hpp:143-170) of one solve.  For a batched solve the

@@ -28,7 +28,7 @@ STATUS_NAMES = {
 SMOOTHER = {"jacobi": 0, "chebyshev": 1}
 AFF_SCALING = {"none": 0, "row": 1, "column": 2, "rowcolumn": 3, "sym": 4, "max": 5}
 STRENGTH = {"affinity": 0, "algebraic-distance": 1, "none": 2}
-KSP = {"cg": 0, "fcg": 1}
+KSP = {"cg": 0, "fcg": 1, "fgmres": 2}
 PRECISION = {"fp64": 0, "fp32": 1}
 LEVEL_TYPES = {0: "elim", 1: "agg", 2: "coarse"}
 
@@ -76,6 +76,7 @@ class Options(C.Structure):
         ("use_graphs", C.c_int32),
         ("autotune", C.c_int32),
         ("tail_rows", C.c_int64),
+        ("gmres_restart", C.c_int32),
     ]
 
 
@@ -141,6 +142,7 @@ def default_options(**overrides) -> Options:
     o.use_graphs = 1
     o.autotune = 1
     o.tail_rows = 0
+    o.gmres_restart = 30
     for k, v in overrides.items():
         if k in ("smoother_type",) and isinstance(v, str):
             v = SMOOTHER[v]

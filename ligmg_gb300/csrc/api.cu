@@ -450,6 +450,9 @@ struct OuterWork {
   DBuf<float2> Pdf;
   DBuf<int> frozen;
   i64 scratch_len = 0;
+  // FGMRES: Arnoldi basis V (m+1 blocks of n x k), preconditioned basis Z
+  // (m blocks), the new direction, dot products and per-column coefficients
+  DBuf<double> fgV, fgZ, fgW, fgH, fgC;
   double *slot(int s) { return sc.p + (i64)s * k * 2; }
 };
 
@@ -2018,6 +2021,173 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
   return res;
 }
 
+// FGMRES(m) outer solve on k columns (PETSc KSPFGMRES semantics, selectable
+// as the reference's outer KSP type, parse_options.hpp:383-384): right
+// preconditioning with the cycle (constant projected out), classical
+// Gram-Schmidt, Givens rotations, the Arnoldi residual estimate as the
+// convergence test, restart after m steps from the true residual.  Every
+// column keeps its own basis; the small Hessenberg arithmetic runs on the host
+// from the device dot products (one synchronisation per step).
+template <typename T>
+SolveResult outer_solve_fgmres(Handle &H, size_t base, OuterWork &w, int k) {
+  const ligmg_options &o = H.opts;
+  cudaStream_t s = H.s;
+  Level &L = *H.h[base];
+  const i64 n = L.A.n, nk = n * k;
+  const int m = std::max(1, o.gmres_restart);
+  MatView<double> A = viewA<double>(L, k, s);
+  SolveResult res;
+  res.col_iters.assign(k, 0);
+  res.rel.assign(k, 1.0);
+  double *sum = w.slot(S_SUM), *rn2 = w.slot(S_PQR);
+  if (w.fgV.n != (i64)(m + 1) * nk) {
+    w.fgV.alloc((i64)(m + 1) * nk, s);
+    w.fgZ.alloc((i64)m * nk, s);
+    w.fgW.alloc(nk, s);
+    w.fgH.alloc((i64)(m + 1) * k, s);
+    w.fgC.alloc((i64)m * k, s);
+  }
+  auto V = [&](int i) { return w.fgV.p + (i64)i * nk; };
+  auto Z = [&](int i) { return w.fgZ.p + (i64)i * nk; };
+  col_reduce<double>(n, k, Red::Sum, w.B.p, nullptr, sum, w.scratch.p, w.scratch_len, s);
+  sub_mean<double>(n, k, w.B.p, sum, s);
+  LG_CUDA(cudaMemsetAsync(w.X.p, 0, sizeof(double) * nk, s));
+  LG_CUDA(cudaMemcpyAsync(w.R.p, w.B.p, sizeof(double) * nk, cudaMemcpyDeviceToDevice, s));
+  auto col_norms = [&](const double *x, std::vector<double> &out) {
+    col_reduce<double>(n, k, Red::Dot, x, x, rn2, w.scratch.p, w.scratch_len, s);
+    out.resize(k);
+    LG_CUDA(cudaMemcpyAsync(out.data(), rn2, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+    LG_CUDA(cudaStreamSynchronize(s));
+    for (double &v : out) v = std::sqrt(v);
+  };
+  std::vector<double> beta, rn0, ttol(k);
+  col_norms(w.R.p, beta);
+  rn0 = beta;
+  std::vector<char> done(k, 0);
+  int active = 0;
+  for (int c = 0; c < k; c++) {
+    ttol[c] = std::max(o.tol * rn0[c], 1e-60);
+    if (rn0[c] == 0) done[c] = 1;
+    else active++;
+  }
+  res.hist0.push_back(rn0[0]);
+  std::vector<double> Hm((size_t)k * (m + 1) * m), cs((size_t)k * m), sn((size_t)k * m),
+      g((size_t)k * (m + 1)), coef(k), hv, ycoef((size_t)m * k);
+  std::vector<int> jc(k);
+  std::vector<char> conv(k);
+  auto Hij = [&](int c, int i, int j) -> double & { return Hm[((size_t)c * (m + 1) + i) * m + j]; };
+  auto scale_into = [&](double *dst, const double *src) {  // dst = coef[c] * src
+    LG_CUDA(cudaMemcpyAsync(w.fgC.p, coef.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    LG_CUDA(cudaMemsetAsync(dst, 0, sizeof(double) * nk, s));
+    axpby_cols<double>(n, k, dst, src, w.fgC.p, 1.0, 0.0, s);
+  };
+  int it = 0;
+  while (active > 0 && it < o.iters) {
+    for (int c = 0; c < k; c++) {
+      coef[c] = (!done[c] && beta[c] > 0) ? 1.0 / beta[c] : 0.0;
+      std::fill(g.begin() + (size_t)c * (m + 1), g.begin() + (size_t)(c + 1) * (m + 1), 0.0);
+      g[(size_t)c * (m + 1)] = done[c] ? 0.0 : beta[c];
+      jc[c] = 0;
+      conv[c] = 0;
+    }
+    scale_into(V(0), w.R.p);
+    int j = 0;
+    int open = active;  // columns still iterating in this cycle
+    while (j < m && it < o.iters && open > 0) {
+      LG_CUDA(cudaMemcpyAsync(w.R.p, V(j), sizeof(double) * nk, cudaMemcpyDeviceToDevice, s));
+      apply_prec<T>(H, k, base, w.R.p, w.Z.p, sum, w.scratch.p, w.scratch_len);
+      LG_CUDA(cudaMemcpyAsync(Z(j), w.Z.p, sizeof(double) * nk, cudaMemcpyDeviceToDevice, s));
+      EpiArgs a;
+      a.y = w.fgW.p;
+      timed(H, (int)base, LIGMG_KERNEL_SPMV, k, 1, core_bytes(n, L.A.nnz, n, k, 8) + 8.0 * nk,
+            [&] { spmm<double>(A, Z(j), k, Epi::Store, a, s); });
+      timed(H, (int)base, LIGMG_KERNEL_OUTER, k, 1, (4.0 * (j + 1) + 1) * 8.0 * nk, [&] {
+        for (int i = 0; i <= j; i++)
+          col_reduce<double>(n, k, Red::Dot, V(i), w.fgW.p, w.fgH.p + (i64)i * k, w.scratch.p,
+                             w.scratch_len, s);
+        for (int i = 0; i <= j; i++)
+          axpby_cols<double>(n, k, w.fgW.p, V(i), w.fgH.p + (i64)i * k, -1.0, 1.0, s);
+        col_reduce<double>(n, k, Red::Dot, w.fgW.p, w.fgW.p, w.fgH.p + (i64)(j + 1) * k,
+                           w.scratch.p, w.scratch_len, s);
+      });
+      hv.resize((size_t)(j + 2) * k);
+      LG_CUDA(cudaMemcpyAsync(hv.data(), w.fgH.p, sizeof(double) * hv.size(),
+                              cudaMemcpyDeviceToHost, s));
+      LG_CUDA(cudaStreamSynchronize(s));
+      if (H.prof.on) H.prof.collect();
+      for (int c = 0; c < k; c++) {
+        coef[c] = 0.0;
+        if (done[c] || conv[c]) continue;
+        for (int i = 0; i <= j; i++) Hij(c, i, j) = hv[(size_t)i * k + c];
+        const double hn = std::sqrt(std::max(hv[(size_t)(j + 1) * k + c], 0.0));
+        Hij(c, j + 1, j) = hn;
+        coef[c] = hn > 0 ? 1.0 / hn : 0.0;
+        double *csc = &cs[(size_t)c * m], *snc = &sn[(size_t)c * m], *gc = &g[(size_t)c * (m + 1)];
+        for (int i = 0; i < j; i++) {
+          const double x = Hij(c, i, j), y = Hij(c, i + 1, j);
+          Hij(c, i, j) = csc[i] * x + snc[i] * y;
+          Hij(c, i + 1, j) = -snc[i] * x + csc[i] * y;
+        }
+        const double x = Hij(c, j, j), y = Hij(c, j + 1, j);
+        const double rho = std::sqrt(x * x + y * y);
+        csc[j] = rho > 0 ? x / rho : 1.0;
+        snc[j] = rho > 0 ? y / rho : 0.0;
+        Hij(c, j, j) = rho;
+        Hij(c, j + 1, j) = 0.0;
+        gc[j + 1] = -snc[j] * gc[j];
+        gc[j] = csc[j] * gc[j];
+        const double rn = std::fabs(gc[j + 1]);
+        jc[c] = j + 1;
+        res.col_iters[c] = it + 1;
+        if (!std::isfinite(rn)) throw Error(LIGMG_ERR_BREAKDOWN, "non-finite residual");
+        if (c == 0) res.hist0.push_back(rn);
+        if (rn <= ttol[c]) {
+          conv[c] = 1;
+          open--;
+          coef[c] = 0.0;
+        }
+      }
+      scale_into(V(j + 1), w.fgW.p);
+      it++;
+      j++;
+    }
+    // x += sum_i y_i Z_i, y from each column's triangular system
+    std::fill(ycoef.begin(), ycoef.end(), 0.0);
+    for (int c = 0; c < k; c++) {
+      if (done[c]) continue;
+      const int jj = jc[c];
+      const double *gc = &g[(size_t)c * (m + 1)];
+      for (int i = jj - 1; i >= 0; i--) {
+        double acc = gc[i];
+        for (int l = i + 1; l < jj; l++) acc -= Hij(c, i, l) * ycoef[(size_t)l * k + c];
+        ycoef[(size_t)i * k + c] = Hij(c, i, i) != 0 ? acc / Hij(c, i, i) : 0.0;
+      }
+    }
+    LG_CUDA(cudaMemcpyAsync(w.fgC.p, ycoef.data(), sizeof(double) * (size_t)j * k,
+                            cudaMemcpyHostToDevice, s));
+    for (int i = 0; i < j; i++)
+      axpby_cols<double>(n, k, w.X.p, Z(i), w.fgC.p + (i64)i * k, 1.0, 1.0, s);
+    EpiArgs a;
+    a.y = w.R.p;
+    a.b = w.B.p;
+    spmm<double>(A, w.X.p, k, Epi::Resid, a, s);  // true residual for the restart
+    col_norms(w.R.p, beta);
+    for (int c = 0; c < k; c++) {
+      if (done[c]) continue;
+      res.rel[c] = beta[c] / rn0[c];
+      if (conv[c] || beta[c] <= ttol[c]) {
+        done[c] = 1;
+        active--;
+      } else if (!std::isfinite(beta[c])) {
+        throw Error(LIGMG_ERR_BREAKDOWN, "non-finite residual");
+      }
+    }
+  }
+  res.iters = it;
+  res.converged = active == 0;
+  return res;
+}
+
 // Batch mode outer FCG: every graph has its own Krylov scalars and its own
 // convergence test, evaluated on the device, so a whole solve needs no host
 // round trip.  kGraphIters iterations are captured into one CUDA graph (the
@@ -2191,9 +2361,14 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
     LG_CUDA(cudaMemcpyAsync(w.B.p, w.Bfull.p, sizeof(double) * n0 * k, cudaMemcpyDeviceToDevice, s));
   }
   SolveResult res;
+  if (seg && H.opts.outer_ksp_type == LIGMG_KSP_FGMRES)
+    throw Error(LIGMG_ERR_UNSUPPORTED, "batch mode runs FCG or CG outer iterations");
   if (seg)
     res = (H.opts.precision == LIGMG_PREC_FP32) ? outer_solve_seg<float>(H, base, w)
                                                 : outer_solve_seg<double>(H, base, w);
+  else if (H.opts.outer_ksp_type == LIGMG_KSP_FGMRES)
+    res = (H.opts.precision == LIGMG_PREC_FP32) ? outer_solve_fgmres<float>(H, base, w, k)
+                                                : outer_solve_fgmres<double>(H, base, w, k);
   else
     res = (H.opts.precision == LIGMG_PREC_FP32) ? outer_solve<float>(H, base, w, k)
                                                 : outer_solve<double>(H, base, w, k);
@@ -2328,6 +2503,7 @@ void ligmg_default_options(ligmg_options *o) {
   o->use_graphs = 1;
   o->autotune = 1;
   o->tail_rows = 0;
+  o->gmres_restart = 30;
 }
 
 const char *ligmg_status_string(ligmg_status s) {
@@ -2363,7 +2539,9 @@ ligmg_status ligmg_create(int64_t n, const int64_t *rowptr, const int32_t *col,
     if (o.kcycle_iters < 1 || o.num_tvs < 0 || o.max_levels < 1 || o.iters < 0 ||
         (o.precision != LIGMG_PREC_FP64 && o.precision != LIGMG_PREC_FP32))
       return LIGMG_ERR_INVALID_ARGUMENT;
-    if (o.smoother_type > LIGMG_SMOOTHER_CHEBYSHEV || o.outer_ksp_type > LIGMG_KSP_FCG ||
+    if (o.outer_ksp_type == LIGMG_KSP_FGMRES && o.gmres_restart < 1)
+      return LIGMG_ERR_INVALID_ARGUMENT;
+    if (o.smoother_type > LIGMG_SMOOTHER_CHEBYSHEV || o.outer_ksp_type > LIGMG_KSP_FGMRES ||
         o.kcycle_ksp_type != LIGMG_KSP_FCG || o.elim_iters > 1 || o.aff_scaling < LIGMG_AFF_NONE || o.aff_scaling > LIGMG_AFF_MAX)
       return LIGMG_ERR_UNSUPPORTED;
     H->device = o.device;

@@ -968,6 +968,78 @@ struct orc_hier {
     return s / (double)nnz0;
   }
 
+  // FGMRES(m) (PETSc KSPFGMRES, selectable as the reference's outer KSP type,
+  // parse_options.hpp:383-384): right preconditioning with the cycle (its
+  // constant projected out), classical Gram-Schmidt, Givens rotations, the
+  // Arnoldi residual estimate as convergence test, restart after m steps
+  // from the true residual.  x = 0, r = b on entry.
+  int fgmres(size_t base, std::vector<double> &x, const std::vector<double> &b,
+             std::vector<double> r, double beta, double ttol, std::vector<double> &hist,
+             int &iters_out) {
+    const Csr &A = h[base].A;
+    const i64 n = A.n;
+    const int m = std::max(1, opts.gmres_restart);
+    std::vector<std::vector<double>> V(m + 1, std::vector<double>(n)), Z(m);
+    std::vector<double> w, Hm((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1);
+    auto Hij = [&](int i, int j) -> double & { return Hm[(size_t)i * m + j]; };
+    int it = 0;
+    while (true) {
+      for (i64 i = 0; i < n; i++) V[0][i] = r[i] / beta;
+      std::fill(g.begin(), g.end(), 0.0);
+      g[0] = beta;
+      int j = 0;
+      bool conv = false;
+      while (j < m && it < opts.iters) {
+        cycle(base, Z[j], V[j]);
+        remove_mean(Z[j]);
+        spmv(A, Z[j], w);
+        for (int i = 0; i <= j; i++) Hij(i, j) = dot(V[i], w);
+        for (int i = 0; i <= j; i++)
+          for (i64 t = 0; t < n; t++) w[t] -= Hij(i, j) * V[i][t];
+        const double hn = std::sqrt(dot(w, w));
+        Hij(j + 1, j) = hn;
+        for (i64 t = 0; t < n; t++) V[j + 1][t] = hn > 0 ? w[t] / hn : 0.0;
+        for (int i = 0; i < j; i++) {
+          const double a = Hij(i, j), c = Hij(i + 1, j);
+          Hij(i, j) = cs[i] * a + sn[i] * c;
+          Hij(i + 1, j) = -sn[i] * a + cs[i] * c;
+        }
+        const double a = Hij(j, j), c = Hij(j + 1, j);
+        const double rho = std::sqrt(a * a + c * c);
+        cs[j] = rho > 0 ? a / rho : 1.0;
+        sn[j] = rho > 0 ? c / rho : 0.0;
+        Hij(j, j) = rho;
+        Hij(j + 1, j) = 0.0;
+        g[j + 1] = -sn[j] * g[j];
+        g[j] = cs[j] * g[j];
+        const double rn = std::fabs(g[j + 1]);
+        hist.push_back(rn);
+        it++;
+        j++;
+        if (!std::isfinite(rn)) return LIGMG_ERR_BREAKDOWN;
+        if (rn <= ttol) {
+          conv = true;
+          break;
+        }
+      }
+      std::vector<double> y(j);
+      for (int i = j - 1; i >= 0; i--) {
+        double s = g[i];
+        for (int l = i + 1; l < j; l++) s -= Hij(i, l) * y[l];
+        y[i] = Hij(i, i) != 0 ? s / Hij(i, i) : 0.0;
+      }
+      for (int i = 0; i < j; i++)
+        for (i64 t = 0; t < n; t++) x[t] += y[i] * Z[i][t];
+      spmv(A, x, w);
+      for (i64 t = 0; t < n; t++) r[t] = b[t] - w[t];
+      beta = std::sqrt(dot(r, r));
+      iters_out = it;
+      if (conv || beta <= ttol) return LIGMG_OK;
+      if (it >= opts.iters) return LIGMG_NOT_CONVERGED;
+      if (!std::isfinite(beta) || beta == 0) return LIGMG_ERR_BREAKDOWN;
+    }
+  }
+
   // outer Krylov (petsc_fcg, cg.hpp:18-116) on h[base]
   int outer(size_t base, std::vector<double> &x, std::vector<double> b,
             std::vector<double> &hist, int &iters_out) {
@@ -984,6 +1056,8 @@ struct orc_hier {
     int mmax = std::max(1, opts.fcg_mmax);
     std::vector<std::vector<double>> P_hist, Q_hist;
     std::vector<double> eta_hist;
+    if (opts.outer_ksp_type == LIGMG_KSP_FGMRES)
+      return fgmres(base, x, b, r, rn0, ttol, hist, iters_out);
     double beta_cg = 0, beta_old = 0;
     bool cg = opts.outer_ksp_type == LIGMG_KSP_CG;
     if (cg) {

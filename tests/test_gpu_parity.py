@@ -331,3 +331,22 @@ def test_pcg_jacobi_baseline():
     assert np.linalg.norm(r) / np.linalg.norm(b) <= 2e-8
     mg = S.solve(b)
     assert mg.iters() < info.iters()  # multigrid needs far fewer iterations
+
+
+@pytest.mark.parametrize("prec,k,restart", [("fp64", 1, 30), ("fp32", 8, 30), ("fp64", 1, 3)])
+def test_fgmres_outer_matches_oracle(prec, k, restart):
+    # FGMRES(m) outer iterations (the reference's --outer-ksp-type fgmres)
+    L = GRAPHS["grid48_logn"]()
+    kw = dict(kcycle=1, outer_ksp_type="fgmres", gmres_restart=restart)
+    S = Solver(L, precision=prec, **kw)
+    R = O.OracleSolver(L, **kw)
+    B = G.rhs(L.n, k=k, seed=11)
+    if k == 1:
+        B = B.reshape(L.n, 1)
+    info = S.solve_batched(B)
+    assert info.converged and (info.col_true_rel_residual <= 2e-8).all()
+    for c in (0, k - 1):
+        xr, ir = R.solve(B[:, c].copy())
+        assert ir["status"] == 0
+        assert abs(int(info.col_iters[c]) - ir["iters"]) <= 1
+        assert _relerr(info.solution[:, c], xr) <= 1e-6

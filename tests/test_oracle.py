@@ -217,3 +217,16 @@ def test_prepare_graph_tie_takes_smaller_label():
     A.sort_indices()
     rp, ci, cv, orig = O.prepare_graph(6, A.indptr, A.indices, A.data, lcc=True)
     assert list(orig) == [0, 2, 4] and len(rp) == 4 and len(ci) == 4
+
+
+@pytest.mark.parametrize("restart", [30, 3])
+def test_oracle_fgmres_matches_dense_solution(restart):
+    L = G.grid2d(24, weights="lognormal", seed=4)
+    b = G.rhs(L.n, seed=5)
+    S = O.OracleSolver(L, kcycle=1, outer_ksp_type="fgmres", gmres_restart=restart)
+    x, info = S.solve(b)
+    assert info["status"] == 0 and info["true_rel_residual"] <= 1e-8
+    xd = np.linalg.lstsq(L.to_scipy().toarray(), b, rcond=None)[0]
+    xd -= xd.mean()
+    x = x - x.mean()
+    assert np.linalg.norm(x - xd) <= 1e-6 * np.linalg.norm(xd)
