@@ -178,13 +178,17 @@ struct Level {
   // agg.mrp / agg.members), so restriction runs through the hub-split SpMM
   DBuf<double> ones64;
   DBuf<float> ones32;
+  // aggregation levels: C = [R | -R A] (nc x 2n), the residual and its
+  // restriction in one SpMM: bc = C [b; x]
+  DCsr<double> Cr;
+  DBuf<float> Cr32;
   // hub-row plans: hubA64 (FP64, k = 1) is built at setup; the others are
   // built on first use per (precision, k) from the cached host row pointers
   HubPlan<double> hubA64;
-  mutable std::map<int, HubPlan<double>> hA64k, hR64k;
-  mutable std::map<int, HubPlan<float>> hA32k, hR32k;
-  std::vector<i64> rp_host, rrp_host;
-  int lanesA = 32, lanesR = 32, lanesP = 4;
+  mutable std::map<int, HubPlan<double>> hA64k, hR64k, hC64k;
+  mutable std::map<int, HubPlan<float>> hA32k, hR32k, hC32k;
+  std::vector<i64> rp_host, rrp_host, crp_host;
+  int lanesA = 32, lanesR = 32, lanesP = 4, lanesC = 32;
   bool autotune = true;  // options.autotune at creation
   // Chebyshev coefficients
   double theta = 1, delta = 1;
@@ -220,27 +224,43 @@ int lanes_for(i64 nnz, i64 n) {
 }
 
 
+// matrices of a level that have hub plans
+enum Mat : int { MAT_A = 0, MAT_R = 1, MAT_C = 2 };
+
 template <typename T>
-std::map<int, HubPlan<T>> &plans(const Level &L, bool isR);
+std::map<int, HubPlan<T>> &plans(const Level &L, int which);
 template <>
-std::map<int, HubPlan<double>> &plans<double>(const Level &L, bool isR) {
-  return isR ? L.hR64k : L.hA64k;
+std::map<int, HubPlan<double>> &plans<double>(const Level &L, int which) {
+  return which == MAT_C ? L.hC64k : which == MAT_R ? L.hR64k : L.hA64k;
 }
 template <>
-std::map<int, HubPlan<float>> &plans<float>(const Level &L, bool isR) {
-  return isR ? L.hR32k : L.hA32k;
+std::map<int, HubPlan<float>> &plans<float>(const Level &L, int which) {
+  return which == MAT_C ? L.hC32k : which == MAT_R ? L.hR32k : L.hA32k;
+}
+inline const std::vector<i64> &plan_rows(const Level &L, int which) {
+  return which == MAT_C ? L.crp_host : which == MAT_R ? L.rrp_host : L.rp_host;
 }
 
 template <typename T>
 const T *valsA(const Level &L);
 template <typename T>
 const T *valsR(const Level &L);
-
-// The level's matrix (isR: its restriction) without a hub plan.
 template <typename T>
-MatView<T> bare_view(const Level &L, bool isR) {
+const T *valsC(const Level &L) {
+  if constexpr (sizeof(T) == 8) return (const T *)L.Cr.v.p;
+  else return (const T *)L.Cr32.p;
+}
+
+// The level's matrix A, its restriction R or its fused residual restriction
+// C (x2 unset), without a hub plan.
+template <typename T>
+MatView<T> bare_view(const Level &L, int which) {
   MatView<T> m;
-  if (!isR) {
+  if (which == MAT_C) {
+    m.n = L.Cr.n; m.rp = L.Cr.rp.p; m.ci = L.Cr.ci.p; m.v = valsC<T>(L);
+    m.lanes_per_row = L.lanesC;
+    m.xsplit = L.A.n;
+  } else if (which == MAT_A) {
     m.n = L.A.n; m.rp = L.A.rp.p; m.ci = L.A.ci.p; m.v = valsA<T>(L); m.lanes_per_row = L.lanesA;
   } else if (L.type == LIGMG_LEVEL_AGG) {
     m.n = L.nc; m.rp = L.agg.mrp.p; m.ci = L.agg.members.p; m.v = valsR<T>(L);
@@ -265,9 +285,9 @@ MatView<T> bare_view(const Level &L, bool isR) {
 // split into chunk partials (its rounding); autotune = 0 uses the defaults
 // (factor 1, 64 threads for k > 1, 256 for k = 1, the level's lanes).
 template <typename T>
-void build_plan(const Level &L, bool isR, int k, HubPlan<T> &best, bool autotune,
+void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotune,
                 cudaStream_t s) {
-  const std::vector<i64> &rp = isR ? L.rrp_host : L.rp_host;
+  const std::vector<i64> &rp = plan_rows(L, which);
   const i64 n = (i64)rp.size() - 1;
   const int unit = split_unit(sizeof(T), k);
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -277,9 +297,11 @@ void build_plan(const Level &L, bool isR, int k, HubPlan<T> &best, bool autotune
     best.tb = k > 1 ? 64 : 256;
     return;
   }
-  const MatView<T> base = bare_view<T>(L, isR);
+  MatView<T> base = bare_view<T>(L, which);
   DBuf<T> X(L.A.n * k, s), Y(n * k, s);
   X.zero();
+  const Epi epi = which == MAT_C ? Epi::Split : Epi::Store;
+  if (which == MAT_C) base.x2 = X.p;  // both halves of the operand
   cudaEvent_t e0, e1;
   LG_CUDA(cudaEventCreate(&e0));
   LG_CUDA(cudaEventCreate(&e1));
@@ -303,9 +325,9 @@ void build_plan(const Level &L, bool isR, int k, HubPlan<T> &best, bool autotune
         if (lanes) m.lanes_per_row = lanes;
         EpiArgs a;
         a.y = Y.p;
-        spmm<T>(m, X.p, k, Epi::Store, a, s);
+        spmm<T>(m, X.p, k, epi, a, s);
         LG_CUDA(cudaEventRecord(e0, s));
-        for (int r = 0; r < 3; r++) spmm<T>(m, X.p, k, Epi::Store, a, s);
+        for (int r = 0; r < 3; r++) spmm<T>(m, X.p, k, epi, a, s);
         LG_CUDA(cudaEventRecord(e1, s));
         LG_CUDA(cudaEventSynchronize(e1));
         float ms = 0;
@@ -331,12 +353,12 @@ void build_plan(const Level &L, bool isR, int k, HubPlan<T> &best, bool autotune
 }
 
 template <typename T>
-const HubPlan<T> &plan_for(const Level &L, bool isR, int k, cudaStream_t s) {
+const HubPlan<T> &plan_for(const Level &L, int which, int k, cudaStream_t s) {
   if constexpr (sizeof(T) == 8) {
-    if (!isR && k == 1) return L.hubA64;
+    if (which == MAT_A && k == 1) return L.hubA64;
   }
-  HubPlan<T> &p = plans<T>(L, isR)[k];
-  if (!p.built) build_plan<T>(L, isR, k, p, L.autotune, s);
+  HubPlan<T> &p = plans<T>(L, which)[k];
+  if (!p.built) build_plan<T>(L, which, k, p, L.autotune, s);
   return p;
 }
 
@@ -363,8 +385,16 @@ MatView<T> viewA(const Level &L, int k, cudaStream_t s) {
 }
 template <typename T>
 MatView<T> viewR(const Level &L, int k, cudaStream_t s) {
-  MatView<T> m = bare_view<T>(L, true);
-  plan_for<T>(L, true, k, s).fill(m);
+  MatView<T> m = bare_view<T>(L, MAT_R);
+  plan_for<T>(L, MAT_R, k, s).fill(m);
+  return m;
+}
+// C with its second operand: bc = C [b; x] = R (b - A x)
+template <typename T>
+MatView<T> viewC(const Level &L, int k, const T *x, cudaStream_t s) {
+  MatView<T> m = bare_view<T>(L, MAT_C);
+  plan_for<T>(L, MAT_C, k, s).fill(m);
+  m.x2 = x;
   return m;
 }
 template <typename T>
@@ -635,6 +665,10 @@ void ensure_fp32(Handle &H) {
       L.pinv32.alloc(L.pinv.n, s);
       convert<double, float>(L.pinv.n, L.pinv.p, L.pinv32.p, s);
     }
+    if (L.type == LIGMG_LEVEL_AGG && L.Cr.nnz) {
+      L.Cr32.alloc(L.Cr.nnz, s);
+      convert<double, float>(L.Cr.nnz, L.Cr.v.p, L.Cr32.p, s);
+    }
     L.has32 = true;
   }
   LG_CUDA(cudaStreamSynchronize(s));
@@ -817,15 +851,10 @@ struct TailBuilder {
       spmm(viewP<T>(L), nw.out.p, Epi::ElimInterp, c);
       return;
     }
-    LevelWork<T> &w = W.lw[l];
     smooth(l, x, b, o().pre_smooth, true);
-    EpiArgs a;
-    a.y = w.r.p;
-    a.b = b;
-    spmm(viewA<T>(L, k, s), x, Epi::Resid, a);
     EpiArgs rs;
     rs.y = nw.in.p;
-    spmm(viewR<T>(L, k, s), w.r.p, Epi::Store, rs);
+    spmm(viewC<T>(L, k, x, s), b, Epi::Split, rs);
     recurse(l, nw.in.p, nw.out.p);
     TOp<T> pr;
     pr.kind = TOpKind::Prolong;
@@ -976,6 +1005,9 @@ bool tail_record(Handle &H, Work<T> &W, size_t start, int smem_avail, int kl,
       add(L.agg.mrp.p, 8 * ((size_t)L.nc + 1));
       add(L.agg.members.p, 4 * n);
       add(valsR<T>(L), sv * n);
+      add(L.Cr.rp.p, 8 * ((size_t)L.Cr.n + 1));
+      add(L.Cr.ci.p, 4 * (size_t)L.Cr.nnz);
+      add(valsC<T>(L), sv * (size_t)L.Cr.nnz);
     } else if (L.type == LIGMG_LEVEL_ELIM) {
       const DCsr<double> &R = L.elim.R, &P = L.elim.P;
       add(R.rp.p, 8 * ((size_t)R.n + 1));
@@ -1005,7 +1037,7 @@ bool tail_record(Handle &H, Work<T> &W, size_t start, int smem_avail, int kl,
     }
   };
   auto vec_fields = [](TOp<T> &op, auto &&f) {
-    f(op.x0); f(op.x1); f(op.x2); f(op.y0); f(op.y1);
+    f(op.x0); f(op.x1); f(op.x2); f(op.y0); f(op.y1); f(op.A.x2);
     f(op.a.y); f(op.a.b); f(op.a.xin); f(op.a.xout); f(op.a.rin); f(op.a.rout);
     f(op.a.din); f(op.a.dout);
   };
@@ -1374,19 +1406,13 @@ struct Engine {
       return;
     }
     // aggregation.hpp:209-241
-    LevelWork<T> &w = W.lw[l];
     smooth(l, x, b, o().pre_smooth, true);
-    EpiArgs a;
-    a.y = w.r.p;
-    a.b = b;
-    timed(H, (int)l, LIGMG_KERNEL_RESID, k, sizeof(T) == 8,
-          core_bytes(n, L.A.nnz, n, k, sizeof(T)) + 2.0 * n * k * sizeof(T),
-          [&] { spmm<T>(viewA<T>(L, k, s), x, k, Epi::Resid, a, s); });
+    // residual and restriction in one SpMM: bc = R (b - A x) = C [b; x]
     EpiArgs rs;
     rs.y = nw.in.p;
     timed(H, (int)l, LIGMG_KERNEL_AGG_RESTRICT, k, sizeof(T) == 8,
-          8.0 * (L.nc + 1) + 4.0 * n + ((double)n + L.nc) * k * sizeof(T),
-          [&] { spmm<T>(viewR<T>(L, k, s), w.r.p, k, Epi::Store, rs, s); });
+          core_bytes(L.nc, L.Cr.nnz, 2 * n, k, sizeof(T)) + (double)L.nc * k * sizeof(T),
+          [&] { spmm<T>(viewC<T>(L, k, x, s), b, k, Epi::Split, rs, s); });
     recurse(l, nw.in.p, nw.out.p);
     timed(H, (int)l, LIGMG_KERNEL_AGG_PROLONG, k, sizeof(T) == 8,
           4.0 * n + (2.0 * n + L.nc) * k * sizeof(T),
@@ -1581,6 +1607,9 @@ void finish_level(Handle &H, Level &L) {
     L.lanesP = lanes_for(L.elim.P.nnz, L.elim.P.n);
   }
   if (L.type == LIGMG_LEVEL_AGG) {
+    gpu_restrict_residual_matrix(L.A, L.agg.agg.p, L.agg.mrp.p, L.agg.members.p, L.nc, L.Cr, s);
+    L.crp_host = L.Cr.rp.to_host();
+    L.lanesC = lanes_for(L.Cr.nnz, L.Cr.n);
     L.rrp_host = L.agg.mrp.to_host();
     L.lanesR = lanes_for(L.A.n, L.nc);
     L.ones64.alloc(L.A.n, s);

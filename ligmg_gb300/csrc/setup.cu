@@ -910,6 +910,97 @@ void gpu_galerkin(const DCsr<double> &A, const DCsr<double> &P, DCsr<double> &C,
   LG_LAUNCH();
 }
 
+namespace {
+__global__ void k_ra_keys(const i64 *rp, const i32 *ci, i64 n, const i32 *agg, int cbits,
+                          u64 *keys, u32 *idx) {
+  const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const u64 hi = (u64)agg[i] << cbits;
+  for (i64 k = rp[i]; k < rp[i + 1]; k++) {
+    keys[k] = hi | (u64)ci[k];
+    idx[k] = (u32)k;
+  }
+}
+__global__ void k_seg_heads(const u64 *keys, i64 m, uint8_t *head) {
+  const i64 p = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < m) head[p] = (p == 0 || keys[p] != keys[p - 1]) ? 1 : 0;
+}
+// one thread per (aggregate, column) segment: the member entries summed in
+// sorted (stable: ascending member row) order; row counts of R A
+__global__ void k_ra_sum(const u64 *keys, const u32 *idx, const double *v, i64 m,
+                         const i32 *starts, i64 nseg, int cbits, u64 cmask, i32 *racol,
+                         double *raval, i64 *rcnt) {
+  const i64 g = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nseg) return;
+  const i64 b = starts[g], e = g + 1 < nseg ? starts[g + 1] : m;
+  double acc = 0.0;
+  for (i64 p = b; p < e; p++) acc = __dadd_rn(acc, v[idx[p]]);
+  racol[g] = (i32)(keys[b] & cmask);
+  raval[g] = acc;
+  atomicAdd((unsigned long long *)&rcnt[keys[b] >> cbits], 1ull);
+}
+__global__ void k_cr_count(i64 nc, const i64 *mrp, const i64 *rarp, i64 *cnt) {
+  const i64 I = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I < nc) cnt[I] = (mrp[I + 1] - mrp[I]) + (rarp[I + 1] - rarp[I]);
+}
+__global__ void k_cr_fill(i64 nc, i64 n, const i64 *mrp, const i32 *members, const i64 *rarp,
+                          const i32 *racol, const double *raval, const i64 *crp, i32 *cci,
+                          double *cv) {
+  const i64 I = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= nc) return;
+  i64 p = crp[I];
+  for (i64 q = mrp[I]; q < mrp[I + 1]; q++) {
+    cci[p] = members[q];
+    cv[p++] = 1.0;
+  }
+  for (i64 q = rarp[I]; q < rarp[I + 1]; q++) {
+    cci[p] = (i32)(n + racol[q]);
+    cv[p++] = -raval[q];
+  }
+}
+}  // namespace
+
+void gpu_restrict_residual_matrix(const DCsr<double> &A, const i32 *agg, const i64 *mrp,
+                                  const i32 *members, i64 nc, DCsr<double> &C, cudaStream_t s) {
+  const i64 n = A.n, nnz = A.nnz;
+  if (2 * n > (i64)INT32_MAX) throw Error(LIGMG_ERR_UNSUPPORTED, "level too large");
+  const int cbits = bits_for(n - 1), abits = bits_for(nc - 1);
+  DBuf<u64> keys(std::max<i64>(nnz, 1), s);
+  DBuf<u32> idx(std::max<i64>(nnz, 1), s);
+  k_ra_keys<<<grid_for(n, 256), 256, 0, s>>>(A.rp.p, A.ci.p, n, agg, cbits, keys.p, idx.p);
+  LG_LAUNCH();
+  radix_sort_pairs(keys.p, idx.p, nnz, cbits + abits, s);
+  DBuf<uint8_t> head(std::max<i64>(nnz, 1), s);
+  k_seg_heads<<<grid_for(nnz, 256), 256, 0, s>>>(keys.p, nnz, head.p);
+  LG_LAUNCH();
+  DBuf<i32> starts(std::max<i64>(nnz, 1), s);
+  const i64 nseg = compact_indices(head.p, nnz, starts.p, s);
+  DBuf<i32> racol(std::max<i64>(nseg, 1), s);
+  DBuf<double> raval(std::max<i64>(nseg, 1), s);
+  DBuf<i64> rcnt(nc + 1, s), rarp(nc + 1, s);
+  rcnt.zero();
+  k_ra_sum<<<grid_for(nseg, 256), 256, 0, s>>>(keys.p, idx.p, A.v.p, nnz, starts.p, nseg, cbits,
+                                               (1ull << cbits) - 1, racol.p, raval.p, rcnt.p);
+  LG_LAUNCH();
+  exclusive_scan<i64>(rcnt.p, rarp.p, nc + 1, s);
+  DBuf<i64> ccnt(nc + 1, s);
+  ccnt.zero();
+  k_cr_count<<<grid_for(nc, 256), 256, 0, s>>>(nc, mrp, rarp.p, ccnt.p);
+  LG_LAUNCH();
+  C.n = nc;
+  C.m = 2 * n;
+  C.rp.alloc(nc + 1, s);
+  DBuf<i64> tot(1, s);
+  exclusive_scan<i64>(ccnt.p, C.rp.p, nc + 1, s, tot.p);
+  C.nnz = read_scalar(tot.p, s);
+  C.ci.alloc(C.nnz, s);
+  C.v.alloc(C.nnz, s);
+  k_cr_fill<<<grid_for(nc, 256), 256, 0, s>>>(nc, n, mrp, members, rarp.p, racol.p, raval.p,
+                                               C.rp.p, C.ci.p, C.v.p);
+  LG_LAUNCH();
+  LG_CUDA(cudaStreamSynchronize(s));
+}
+
 void gpu_galerkin_agg(const DCsr<double> &A, const i32 *agg, i64 nc, DCsr<double> &C,
                       cudaStream_t s) {
   DCsr<double> P;

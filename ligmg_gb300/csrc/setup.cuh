@@ -49,6 +49,14 @@ void gpu_galerkin(const DCsr<double> &A, const DCsr<double> &P, DCsr<double> &C,
 void gpu_galerkin_agg(const DCsr<double> &A, const i32 *agg, i64 nc, DCsr<double> &C,
                       cudaStream_t s);
 
+// Fused residual restriction of an aggregation level: C = [R | -R A], nc x 2n,
+// so that R (b - A x) = C [b; x] is one SpMM (columns < n gather b, columns
+// >= n gather x).  Row I: its members (value 1, ascending), then the entries
+// of R A (column n + j), each the sum of the members' a_mj in ascending member
+// order.
+void gpu_restrict_residual_matrix(const DCsr<double> &A, const i32 *agg, const i64 *mrp,
+                                  const i32 *members, i64 nc, DCsr<double> &C, cudaStream_t s);
+
 // Member CSR of an aggregation (R): fine vertices grouped by aggregate id,
 // ascending inside each aggregate.
 void gpu_members(const i32 *agg, i64 n, i64 nc, DBuf<i64> &mrp, DBuf<i32> &members,

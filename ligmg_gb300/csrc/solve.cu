@@ -145,6 +145,7 @@ void spmm(const MatView<T> &A, const T *X, int k, Epi epi, const EpiArgs &a, cud
     case Epi::ChebB: return dispatch_k<T, Epi::ChebB>(A, X, k, a, s);
     case Epi::ElimInterp: return dispatch_k<T, Epi::ElimInterp>(A, X, k, a, s);
     case Epi::Jacobi: return dispatch_k<T, Epi::Jacobi>(A, X, k, a, s);
+    case Epi::Split: return dispatch_k<T, Epi::Split>(A, X, k, a, s);
   }
 }
 template void spmm<float>(const MatView<float> &, const float *, int, Epi, const EpiArgs &,

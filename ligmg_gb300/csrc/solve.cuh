@@ -24,6 +24,9 @@ struct MatView {
   T *partial = nullptr;        // nchunks x K
   int lanes_per_row = 32;      // 4, 8, 16 or 32 (single-RHS layout)
   int tb = 256;                // threads per block of the launch (64, 128 or 256)
+  // Epi::Split only: the second gathered operand and the first column taken from it
+  const T *x2 = nullptr;
+  i64 xsplit = 0;
 };
 
 // Hub-row schedule owned by a level (built once at setup).
@@ -56,6 +59,7 @@ enum class Epi {
   ChebB,       // r' = r - A d; d' = c1 d + c2 invd r'; xo = xi + d'
   ElimInterp,  // y = A x + q .* b   (A = P, x = xc)
   Jacobi,      // y = xi + w invd (b - A x)   (weighted Jacobi sweep, w = c1)
+  Split,       // y = A [X; x2]: columns < xsplit gather X, the others x2 (row j - xsplit)
 };
 
 struct EpiArgs {

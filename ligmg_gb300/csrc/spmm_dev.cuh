@@ -78,7 +78,7 @@ __device__ __forceinline__ void xload(const T *p, T (&o)[VW]) {
 template <typename T, int K, int VW, Epi E>
 __device__ __forceinline__ void epilogue(const EpiArgs &a, i64 r, int c0, T (&acc)[VW]) {
   const i64 off = r * K + c0;
-  if constexpr (E == Epi::Store) {
+  if constexpr (E == Epi::Store || E == Epi::Split) {
     vstore<T, VW>((T *)a.y + off, acc);
   } else if constexpr (E == Epi::Resid) {
     T b[VW];
@@ -135,9 +135,21 @@ __device__ __forceinline__ void epilogue(const EpiArgs &a, i64 r, int c0, T (&ac
   }
 }
 
+// Row j of the gathered operand: X, or with SPLIT (Epi::Split) X for j <
+// xsplit and x2 row j - xsplit otherwise.
+template <typename T, int K, bool SPLIT>
+__device__ __forceinline__ const T *xsrc(const MatView<T> &A, const T *X, i32 j) {
+  if constexpr (SPLIT) {
+    const bool lo = j < A.xsplit;
+    return (lo ? X : A.x2) + (lo ? (i64)j : (i64)j - A.xsplit) * K;
+  } else {
+    return X + (i64)j * K;
+  }
+}
+
 // GX: matrix and X in global memory (read-only cache loads); otherwise they
 // may be staged in shared memory and are read with generic loads.
-template <typename T, int K, int VW, int E, bool GX = true>
+template <typename T, int K, int VW, int E, bool GX = true, bool SPLIT = false>
 __device__ __forceinline__ void row_accumulate(const MatView<T> &A, const T *__restrict__ X, i64 k,
                                                i64 e, int ch, T (&acc)[VW]) {
   const T *__restrict__ av = A.v;
@@ -148,10 +160,10 @@ __device__ __forceinline__ void row_accumulate(const MatView<T> &A, const T *__r
     i32 j0 = mld<GX>(ac + k), j1 = mld<GX>(ac + k + E), j2 = mld<GX>(ac + k + 2 * E),
         j3 = mld<GX>(ac + k + 3 * E);
     T x0[VW], x1[VW], x2[VW], x3[VW];
-    xload<T, VW, GX>(X + (i64)j0 * K + ch * VW, x0);
-    xload<T, VW, GX>(X + (i64)j1 * K + ch * VW, x1);
-    xload<T, VW, GX>(X + (i64)j2 * K + ch * VW, x2);
-    xload<T, VW, GX>(X + (i64)j3 * K + ch * VW, x3);
+    xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j0) + ch * VW, x0);
+    xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j1) + ch * VW, x1);
+    xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j2) + ch * VW, x2);
+    xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j3) + ch * VW, x3);
 #pragma unroll
     for (int q = 0; q < VW; q++) acc[q] += a0 * x0[q];
 #pragma unroll
@@ -165,7 +177,7 @@ __device__ __forceinline__ void row_accumulate(const MatView<T> &A, const T *__r
     T a0 = mld<GX>(av + k);
     i32 j0 = mld<GX>(ac + k);
     T x0[VW];
-    xload<T, VW, GX>(X + (i64)j0 * K + ch * VW, x0);
+    xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j0) + ch * VW, x0);
 #pragma unroll
     for (int q = 0; q < VW; q++) acc[q] += a0 * x0[q];
   }
@@ -205,7 +217,7 @@ __device__ __forceinline__ void spmm_unit(const MatView<T> &A, const T *__restri
       e = A.rp[r + 1];
       if (A.hub_thresh > 0 && e - b > A.hub_thresh) act = false;
     }
-    if (act) row_accumulate<T, K, VW, E, GX>(A, X, b + slot, e, ch, acc);
+    if (act) row_accumulate<T, K, VW, E, GX, EP == Epi::Split>(A, X, b + slot, e, ch, acc);
     reduce_slots<T, VW, L, G>(acc);
     if (act && slot == 0) epilogue<T, K, VW, EP>(a, r, ch * VW, acc);
     return;
@@ -213,7 +225,7 @@ __device__ __forceinline__ void spmm_unit(const MatView<T> &A, const T *__restri
   if constexpr (G == 32) {
     const i64 c = warp - nregw;
     if (c >= A.nchunks) return;
-    row_accumulate<T, K, VW, E, GX>(A, X, A.ch_beg[c] + slot, A.ch_end[c], ch, acc);
+    row_accumulate<T, K, VW, E, GX, EP == Epi::Split>(A, X, A.ch_beg[c] + slot, A.ch_end[c], ch, acc);
     reduce_slots<T, VW, L, G>(acc);
     if (slot == 0) vstore<T, VW>(A.partial + c * K + ch * VW, acc);
     __threadfence();

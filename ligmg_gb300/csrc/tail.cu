@@ -82,6 +82,7 @@ __device__ void run_spmm(const TOp<T> &op, i64 gwarp, i64 nwarps, int lane) {
     A.rp = res<SM>(A.rp);
     A.ci = res<SM>(A.ci);
     A.v = res<SM>(A.v);
+    A.x2 = res<SM>(A.x2);
     a.invd = res<SM>(a.invd);
     a.q = res<SM>(a.q);
     a.y = res<SM>(a.y);
@@ -105,6 +106,7 @@ __device__ void run_spmm(const TOp<T> &op, i64 gwarp, i64 nwarps, int lane) {
     LG_TAIL_EPI(Epi::ChebB)
     LG_TAIL_EPI(Epi::ElimInterp)
     LG_TAIL_EPI(Epi::Jacobi)
+    LG_TAIL_EPI(Epi::Split)
 #undef LG_TAIL_EPI
   }
 }
