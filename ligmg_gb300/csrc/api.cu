@@ -95,6 +95,12 @@ double tridiag_lmax(const std::vector<double> &d, const std::vector<double> &e) 
   return hi;
 }
 
+__global__ void k_ad_values(i64 nnz, const i32 *ci, const double *v, const double *invd,
+                            double *ad) {
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nnz) ad[t] = v[t] * invd[ci[t]];
+}
+
 __global__ void k_invdiag(const i64 *rp, const i32 *ci, const double *v, i64 n, double *invd) {
   i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -182,6 +188,10 @@ struct Level {
   // restriction in one SpMM: bc = C [b; x]
   DCsr<double> Cr;
   DBuf<float> Cr32;
+  // A D^-1 values (a_ij / a_jj): the first Chebyshev step from a zero guess
+  // gathers b itself (A d0 = A D^-1 b / theta)
+  DBuf<double> ADv;
+  DBuf<float> AD32;
   // hub-row plans: hubA64 (FP64, k = 1) is built at setup; the others are
   // built on first use per (precision, k) from the cached host row pointers
   HubPlan<double> hubA64;
@@ -384,6 +394,14 @@ MatView<T> viewA(const Level &L, int k, cudaStream_t s) {
   return m;
 }
 template <typename T>
+MatView<T> viewAD(const Level &L, int k, cudaStream_t s) {
+  MatView<T> m = bare_view<T>(L, MAT_A);
+  plan_for<T>(L, MAT_A, k, s).fill(m);
+  if constexpr (sizeof(T) == 8) m.v = (const T *)L.ADv.p;
+  else m.v = (const T *)L.AD32.p;
+  return m;
+}
+template <typename T>
 MatView<T> viewR(const Level &L, int k, cudaStream_t s) {
   MatView<T> m = bare_view<T>(L, MAT_R);
   plan_for<T>(L, MAT_R, k, s).fill(m);
@@ -423,7 +441,8 @@ const T *pinvT(const Level &L) {
 }
 
 // per-level scalar slots (k doubles each)
-enum Slot { S_SUM = 0, S_ZQ, S_BETA, S_ETA0, S_ETA1, S_RHO, S_ALPHA, S_PQR, S_NSLOT };
+// S_F32: float copies of mu, beta and alpha (3 k floats) for FP32 levels
+enum Slot { S_SUM = 0, S_ZQ, S_BETA, S_ETA0, S_ETA1, S_RHO, S_ALPHA, S_PQR, S_F32, S_NSLOT };
 
 template <typename T>
 struct LevelWork {
@@ -669,6 +688,10 @@ void ensure_fp32(Handle &H) {
       L.Cr32.alloc(L.Cr.nnz, s);
       convert<double, float>(L.Cr.nnz, L.Cr.v.p, L.Cr32.p, s);
     }
+    if (L.ADv.n) {
+      L.AD32.alloc(L.ADv.n, s);
+      convert<double, float>(L.ADv.n, L.ADv.p, L.AD32.p, s);
+    }
     L.has32 = true;
   }
   LG_CUDA(cudaStreamSynchronize(s));
@@ -756,6 +779,7 @@ struct TailBuilder {
     }
     op.x0 = X;
     op.a = a;
+    op.a.mirror();
     ops.push_back(op);
   }
   void elem(TOpKind kind, i64 n, const T *x0, const T *x1, T *y0, double f = 1) {
@@ -778,7 +802,7 @@ struct TailBuilder {
     if (o().smoother_type == LIGMG_SMOOTHER_JACOBI) {
       const double omega = 2.0 / 3.0;
       if (x_zero) {
-        elem(TOpKind::Cheb0, n, b, invd, x, 1.0 / omega);
+        elem(TOpKind::Cheb0, n, b, invd, x, omega);
         return;
       }
       EpiArgs a;
@@ -792,17 +816,29 @@ struct TailBuilder {
     const T *x_cur;
     T *d_cur;
     T *d_other = w.d1.p;
+    int first = 1;
+    if (x_zero && iters == 1) {
+      elem(TOpKind::Cheb0, n, b, invd, x, 1.0 / L.theta);
+      return;
+    }
     if (x_zero) {
-      T *d0 = iters == 1 ? x : w.d0.p;
-      elem(TOpKind::Cheb0, n, b, invd, d0, L.theta);
-      if (iters == 1) return;
-      d_cur = w.d0.p;
-      x_cur = w.d0.p;
-      r_cur = b;
+      const bool last = iters == 2;
+      EpiArgs a;
+      a.b = b; a.invd = invd; a.ith = 1.0 / L.theta; a.c1 = L.c1[0]; a.c2 = L.c2[0];
+      a.rout = last ? nullptr : w.r.p;
+      a.dout = last ? nullptr : w.d1.p;
+      a.xout = last ? x : w.xt.p;
+      spmm(viewAD<T>(L, k, s), b, Epi::ChebZ, a);
+      if (last) return;
+      r_cur = w.r.p;
+      d_cur = w.d1.p;
+      d_other = w.d0.p;
+      x_cur = w.xt.p;
+      first = 2;
     } else {
       EpiArgs a;
       a.b = b; a.invd = invd; a.xin = x; a.rout = w.r.p; a.dout = w.d0.p; a.xout = w.xt.p;
-      a.theta = L.theta;
+      a.ith = 1.0 / L.theta;
       spmm(A, x, Epi::ChebA, a);
       d_cur = w.d0.p;
       x_cur = w.xt.p;
@@ -812,7 +848,7 @@ struct TailBuilder {
         return;
       }
     }
-    for (int it = 1; it < iters; it++) {
+    for (int it = first; it < iters; it++) {
       bool last = it == iters - 1;
       EpiArgs a;
       a.invd = invd;
@@ -1005,6 +1041,8 @@ bool tail_record(Handle &H, Work<T> &W, size_t start, int smem_avail, int kl,
       add(L.agg.mrp.p, 8 * ((size_t)L.nc + 1));
       add(L.agg.members.p, 4 * n);
       add(valsR<T>(L), sv * n);
+      if constexpr (sizeof(T) == 8) add(L.ADv.p, sv * (size_t)L.A.nnz);
+      else add(L.AD32.p, sv * (size_t)L.A.nnz);
       add(L.Cr.rp.p, 8 * ((size_t)L.Cr.n + 1));
       add(L.Cr.ci.p, 4 * (size_t)L.Cr.nnz);
       add(valsC<T>(L), sv * (size_t)L.Cr.nnz);
@@ -1313,7 +1351,7 @@ struct Engine {
       const double omega = 2.0 / 3.0;
       if (x_zero) {
         timed(H, (int)l, LIGMG_KERNEL_VECTOR, k, sizeof(T) == 8, (2.0 * n * k + n) * sizeof(T),
-              [&] { cheb_init_zero<T>(n, k, b, invd, 1.0 / omega, x, s); });
+              [&] { cheb_init_zero<T>(n, k, b, invd, omega, x, s); });
         return;
       }
       EpiArgs a;
@@ -1331,18 +1369,33 @@ struct Engine {
     const T *x_cur;
     T *d_cur;
     T *d_other = w.d1.p;
-    if (x_zero) {
-      T *d0 = iters == 1 ? x : w.d0.p;
+    int first = 1;  // next Chebyshev step of the loop below
+    if (x_zero && iters == 1) {
       timed(H, (int)l, LIGMG_KERNEL_VECTOR, k, sizeof(T) == 8, (2.0 * n * k + n) * sizeof(T),
-            [&] { cheb_init_zero<T>(n, k, b, invd, L.theta, d0, s); });
-      if (iters == 1) return;
-      d_cur = w.d0.p;
-      x_cur = w.d0.p;  // x1 = d0
-      r_cur = b;       // r0 = b
+            [&] { cheb_init_zero<T>(n, k, b, invd, 1.0 / L.theta, x, s); });
+      return;
+    }
+    if (x_zero) {
+      // steps 0 and 1 in one SpMM gathering b with the A D^-1 values
+      const bool last = iters == 2;
+      EpiArgs a;
+      a.b = b; a.invd = invd; a.ith = 1.0 / L.theta; a.c1 = L.c1[0]; a.c2 = L.c2[0];
+      a.rout = last ? nullptr : w.r.p;
+      a.dout = last ? nullptr : w.d1.p;
+      a.xout = last ? x : w.xt.p;
+      timed(H, (int)l, LIGMG_KERNEL_CHEB_B, k, sizeof(T) == 8,
+            core_bytes(n, L.A.nnz, n, k, sizeof(T)) + ((last ? 1.0 : 3.0) * n * k + n) * sizeof(T),
+            [&] { spmm<T>(viewAD<T>(L, k, s), b, k, Epi::ChebZ, a, s); });
+      if (last) return;
+      r_cur = w.r.p;
+      d_cur = w.d1.p;
+      d_other = w.d0.p;
+      x_cur = w.xt.p;
+      first = 2;
     } else {
       EpiArgs a;
       a.b = b; a.invd = invd; a.xin = x; a.rout = w.r.p; a.dout = w.d0.p; a.xout = w.xt.p;
-      a.theta = L.theta;
+      a.ith = 1.0 / L.theta;
       timed(H, (int)l, LIGMG_KERNEL_CHEB_A, k, sizeof(T) == 8,
             core_bytes(n, L.A.nnz, n, k, sizeof(T)) + (5.0 * n * k + n) * sizeof(T),
             [&] { spmm<T>(A, x, k, Epi::ChebA, a, s); });
@@ -1356,7 +1409,7 @@ struct Engine {
         return;
       }
     }
-    for (int it = 1; it < iters; it++) {
+    for (int it = first; it < iters; it++) {
       bool last = it == iters - 1;
       EpiArgs a;
       a.invd = invd;
@@ -1482,6 +1535,12 @@ struct Engine {
     const bool seg = S.nseg > 0;
     FcgScalars sc{w.slot(S_SUM, k), w.slot(S_BETA, k), w.slot(S_ETA0, k), w.slot(S_ETA1, k),
                   w.slot(S_ALPHA, k), nullptr};
+    if constexpr (sizeof(T) == 4) {
+      float *f = reinterpret_cast<float *>(w.slot(S_F32, k));
+      sc.mu_f = f;
+      sc.beta_f = f + k;
+      sc.alpha_f = f + 2 * k;
+    }
     if (seg)  // one set of Krylov scalars per graph of the batch
       sc = FcgScalars{w.sslot(S_SUM), w.sslot(S_BETA), w.sslot(S_ETA0), w.sslot(S_ETA1),
                       w.sslot(S_ALPHA), nullptr};
@@ -1509,7 +1568,7 @@ struct Engine {
                 seg_fcg_update<T>(S, n, x, r, p, q, sc.alpha, it + 1 < iters, s);
               } else {
                 fcg_alpha<T>(n, k, p, q, r, sc, w.fscratch.p, s);
-                fcg_update<T>(n, k, x, r, p, q, sc.alpha, it + 1 < iters, s);
+                fcg_update<T>(n, k, x, r, p, q, sc.alpha, it + 1 < iters, s, sc.alpha_f);
               }
             });
       std::swap(p, pp);
@@ -1607,6 +1666,10 @@ void finish_level(Handle &H, Level &L) {
     L.lanesP = lanes_for(L.elim.P.nnz, L.elim.P.n);
   }
   if (L.type == LIGMG_LEVEL_AGG) {
+    L.ADv.alloc(L.A.nnz, s);
+    k_ad_values<<<grid_for(L.A.nnz, 256), 256, 0, s>>>(L.A.nnz, L.A.ci.p, L.A.v.p, L.invd.p,
+                                                       L.ADv.p);
+    LG_LAUNCH();
     gpu_restrict_residual_matrix(L.A, L.agg.agg.p, L.agg.mrp.p, L.agg.members.p, L.nc, L.Cr, s);
     L.crp_host = L.Cr.rp.to_host();
     L.lanesC = lanes_for(L.Cr.nnz, L.Cr.n);
@@ -1802,7 +1865,7 @@ void apply_prec_body(Handle &H, int k, size_t base, const double *r, double *z, 
   const SegInfo S = L.seginfo();
   timed(H, (int)base, LIGMG_KERNEL_OUTER, k, 1, 24.0 * n * k, [&] {
     if (S.nseg > 0) {  // one constant per graph of the batch
-      seg_sum<double>(S, z, sum, H.s);
+      seg_mean<double>(S, z, sum, H.s);
       seg_sub_mean<double>(S, n, z, sum, H.s);
       return;
     }
@@ -1914,6 +1977,9 @@ void apply_prec(Handle &H, int k, size_t base, const double *r, double *z, doubl
       g.exec = off;
       g.kernels = k_off;
     }
+    // this application's result from the path that is kept, like every later one
+    LG_CUDA(cudaGraphLaunch(g.exec, H.s));
+    add_launches(g.kernels);
   }
   g.r = r;
   g.z = z;
@@ -2373,7 +2439,7 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
   // remove the constant from b first (the reference expects a mean-free b
   // from its caller, main.cpp:138-139; R 1 is not constant)
   if (seg) {
-    seg_sum<double>(SF, w.Bfull.p, segbuf.p, s);
+    seg_mean<double>(SF, w.Bfull.p, segbuf.p, s);
     seg_sub_mean<double>(SF, n0, w.Bfull.p, segbuf.p, s);
   } else {
     col_reduce<double>(n0, k, Red::Sum, w.Bfull.p, nullptr, w.slot(S_SUM), w.scratch.p,

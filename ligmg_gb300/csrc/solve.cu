@@ -137,7 +137,9 @@ void dispatch_k(const MatView<T> &A, const T *X, int k, const EpiArgs &a, cudaSt
 }  // namespace
 
 template <typename T>
-void spmm(const MatView<T> &A, const T *X, int k, Epi epi, const EpiArgs &a, cudaStream_t s) {
+void spmm(const MatView<T> &A, const T *X, int k, Epi epi, const EpiArgs &args, cudaStream_t s) {
+  EpiArgs a = args;
+  a.mirror();
   switch (epi) {
     case Epi::Store: return dispatch_k<T, Epi::Store>(A, X, k, a, s);
     case Epi::Resid: return dispatch_k<T, Epi::Resid>(A, X, k, a, s);
@@ -146,6 +148,7 @@ void spmm(const MatView<T> &A, const T *X, int k, Epi epi, const EpiArgs &a, cud
     case Epi::ElimInterp: return dispatch_k<T, Epi::ElimInterp>(A, X, k, a, s);
     case Epi::Jacobi: return dispatch_k<T, Epi::Jacobi>(A, X, k, a, s);
     case Epi::Split: return dispatch_k<T, Epi::Split>(A, X, k, a, s);
+    case Epi::ChebZ: return dispatch_k<T, Epi::ChebZ>(A, X, k, a, s);
   }
 }
 template void spmm<float>(const MatView<float> &, const float *, int, Epi, const EpiArgs &,
@@ -157,9 +160,9 @@ template void spmm<double>(const MatView<double> &, const double *, int, Epi, co
 namespace {
 
 template <typename T>
-__global__ void k_cheb_init_zero(i64 n, int k, const T *b, const T *invd, T theta, T *d) {
+__global__ void k_cheb_init_zero(i64 n, int k, const T *b, const T *invd, T scale, T *d) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n * k) d[t] = invd[t / k] * b[t] / theta;
+  if (t < n * k) d[t] = (invd[t / k] * scale) * b[t];
 }
 
 template <typename T>
@@ -280,10 +283,10 @@ int colred_blocks(i64 n, int k) {
 }
 
 template <typename T>
-__global__ void k_sub_mean(i64 n, int k, T *x, const double *colsum) {
+__global__ void k_sub_mean(i64 n, int k, T *x, const double *colsum, double inv_n) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
-  double mu = colsum[t % k] / (double)n;
+  double mu = colsum[t % k] * inv_n;  // a product: an FP64 division per element is slow here
   x[t] = (T)((double)x[t] - mu);
 }
 
@@ -303,12 +306,22 @@ __global__ void k_fcg_direction(i64 n, int k, T *p, const T *z, const T *pp, con
   else p[t] = z[t];
 }
 
+// column scalar c in the data's type: the float copy when there is one (no
+// per-element FP64 conversion), else the FP64 value
+template <typename T>
+__device__ __forceinline__ T col_scalar(const double *d, const float *f, int c) {
+  if constexpr (sizeof(T) == 4) {
+    if (f) return f[c];
+  }
+  return (T)d[c];
+}
+
 template <typename T>
 __global__ void k_fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, const double *alpha,
-                             int upd_r) {
+                             const float *alpha_f, int upd_r) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
-  T a = (T)alpha[t % k];
+  const T a = col_scalar<T>(alpha, alpha_f, (int)(t % k));
   x[t] = x[t] + a * p[t];
   if (upd_r) r[t] = r[t] - a * q[t];
 }
@@ -336,6 +349,33 @@ __global__ void k_scal_beta(int k, const double *zq, const double *eta_prev, dou
 }
 
 // ---- fused reductions ------------------------------------------------------
+// FP32 data: the four rows of a group are combined in FP32 (a sum of four
+// values or products, fixed order) and only the group's partial is widened
+// and added in FP64: one FP64 add per four elements instead of up to five
+// FP64-pipe operations (two widenings and three adds) per element, which
+// bound these reductions on GB300.  Rows past the end contribute zeros.
+template <int OP, int NV>
+__device__ __forceinline__ void group4_add(const float (&x)[4], const float (&y)[4],
+                                           const float (&w)[4], bool use_y, double (&a)[NV]) {
+  if constexpr (OP == 0) {
+    a[0] += (double)dev::sum4(x);
+  } else if constexpr (OP == 1) {
+    a[0] += (double)dev::dot4(x, y);
+  } else if constexpr (OP == 2) {
+    a[0] += (double)dev::sum4(x);
+    if (use_y) {
+      a[1] += (double)dev::dot4(x, y);
+      a[2] += (double)dev::sum4(y);
+    }
+  } else {
+    a[0] += (double)dev::dot4(x, y);
+    a[1] += (double)dev::dot4(x, w);
+  }
+}
+template <int OP, int NV>
+__device__ __forceinline__ void group4_add(const double (&)[4], const double (&)[4],
+                                           const double (&)[4], bool, double (&)[NV]) {}
+
 // OP 0: [sum x]            OP 1: [sum x.y]
 // OP 2: [sum x, sum x.y, sum y]   (FCG beta)     OP 3: [sum x.y, sum x.w]  (alpha)
 template <typename T, int OP, int BS>
@@ -365,25 +405,29 @@ __global__ void __launch_bounds__(BS)
       const i64 o = rr * k + c;
       xv[u] = ok ? x[o] : (T)0;
       yv[u] = (ok && use_y) ? y[o] : (T)0;
-      if constexpr (HAS_W) wv[u] = ok ? w[o] : (T)0;
+      wv[u] = (HAS_W && ok) ? w[o] : (T)0;
     }
+    if constexpr (sizeof(T) == 4) {
+      group4_add<OP>(xv, yv, wv, use_y, a);
+    } else {
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const double xd = (double)xv[u];
-      if constexpr (OP == 0) {
-        a[0] += xd;
-      } else if constexpr (OP == 1) {
-        a[0] += xd * (double)yv[u];
-      } else if constexpr (OP == 2) {
-        a[0] += xd;
-        if (use_y) {
-          const double yd = (double)yv[u];
-          a[1] += xd * yd;
-          a[2] += yd;
+      for (int u = 0; u < 4; u++) {
+        const double xd = (double)xv[u];
+        if constexpr (OP == 0) {
+          a[0] += xd;
+        } else if constexpr (OP == 1) {
+          a[0] += xd * (double)yv[u];
+        } else if constexpr (OP == 2) {
+          a[0] += xd;
+          if (use_y) {
+            const double yd = (double)yv[u];
+            a[1] += xd * yd;
+            a[2] += yd;
+          }
+        } else {
+          a[0] += xd * (double)yv[u];
+          a[1] += xd * (double)wv[u];
         }
-      } else {
-        a[0] += xd * (double)yv[u];
-        a[1] += xd * (double)wv[u];
       }
     }
   }
@@ -438,18 +482,24 @@ __global__ void __launch_bounds__(BS)
       out[tid] = tot[0];
     } else if constexpr (OP == 2) {
       double mu = tot[0] / (double)n;
-      sc.mu[tid] = mu;
+      double beta = 0.0;
       if (y) {
         double e = sc.eta_prev[tid];
-        sc.beta[tid] = e == 0.0 ? 0.0 : (tot[1] - mu * tot[2]) / e;
-      } else {
-        sc.beta[tid] = 0.0;
+        beta = e == 0.0 ? 0.0 : (tot[1] - mu * tot[2]) / e;
+      }
+      sc.mu[tid] = mu;
+      sc.beta[tid] = beta;
+      if (sc.mu_f) {
+        sc.mu_f[tid] = (float)mu;
+        sc.beta_f[tid] = (float)beta;
       }
     } else {
       double eta = tot[0];
       sc.eta[tid] = eta;
       bool fz = sc.frozen && sc.frozen[tid];
-      sc.alpha[tid] = (fz || eta == 0.0) ? 0.0 : tot[1] / eta;
+      const double alpha = (fz || eta == 0.0) ? 0.0 : tot[1] / eta;
+      sc.alpha[tid] = alpha;
+      if (sc.alpha_f) sc.alpha_f[tid] = (float)alpha;
     }
   }
   if (tid == 0) *(unsigned *)scratch = 0u;
@@ -461,8 +511,8 @@ __global__ void k_fcg_dir(i64 n, int k, T *p, const T *z, const T *pp, FcgScalar
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
   int c = (int)(t % k);
-  T v = z[t] - (T)sc.mu[c];
-  if (pp) v = v - (T)sc.beta[c] * pp[t];
+  T v = z[t] - col_scalar<T>(sc.mu, sc.mu_f, c);
+  if (pp) v = v - col_scalar<T>(sc.beta, sc.beta_f, c) * pp[t];
   p[t] = v;
   if (pdf) {
     float h = (float)v;
@@ -678,7 +728,9 @@ __global__ void __launch_bounds__(256)
     __syncthreads();
   }
   if (threadIdx.x) return;
-  if constexpr (OP == 0 || OP == 1) {
+  if constexpr (OP == 0) {
+    out[sg] = sh[0][0] / (double)(r1 - r0);  // the segment's mean
+  } else if constexpr (OP == 1) {
     out[sg] = sh[0][0];
   } else if constexpr (OP == 2) {
     double mu = sh[0][0] / (double)(r1 - r0);
@@ -694,12 +746,10 @@ __global__ void __launch_bounds__(256)
 }
 
 template <typename T>
-__global__ void k_seg_sub_mean(SegInfo S, i64 n, T *x, const double *sums) {
+__global__ void k_seg_sub_mean(SegInfo S, i64 n, T *x, const double *means) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
-  i32 sg = S.rowseg[t];
-  double mu = sums[sg] / (double)(S.ptr[sg + 1] - S.ptr[sg]);
-  x[t] = (T)((double)x[t] - mu);
+  x[t] = (T)((double)x[t] - means[S.rowseg[t]]);
 }
 
 template <typename T>
@@ -754,14 +804,14 @@ void seg_dot(const SegInfo &S, const T *x, const T *y, double *out, cudaStream_t
   LG_LAUNCH();
 }
 template <typename T>
-void seg_sum(const SegInfo &S, const T *x, double *out, cudaStream_t s) {
+void seg_mean(const SegInfo &S, const T *x, double *out, cudaStream_t s) {
   FcgScalars none{};
   k_seg_red<T, 0><<<(unsigned)S.nseg, 256, 0, s>>>(S, x, nullptr, nullptr, none, out);
   LG_LAUNCH();
 }
 template <typename T>
-void seg_sub_mean(const SegInfo &S, i64 n, T *x, const double *sums, cudaStream_t s) {
-  k_seg_sub_mean<T><<<grid_for(n, 256), 256, 0, s>>>(S, n, x, sums);
+void seg_sub_mean(const SegInfo &S, i64 n, T *x, const double *means, cudaStream_t s) {
+  k_seg_sub_mean<T><<<grid_for(n, 256), 256, 0, s>>>(S, n, x, means);
   LG_LAUNCH();
 }
 template <typename T>
@@ -788,7 +838,7 @@ void seg_converge(i64 nseg, const double *rn2, const double *rn0sq, double tol, 
   template void seg_fcg_alpha<T>(const SegInfo &, const T *, const T *, const T *,          \
                                  FcgScalars, cudaStream_t);                                 \
   template void seg_dot<T>(const SegInfo &, const T *, const T *, double *, cudaStream_t);  \
-  template void seg_sum<T>(const SegInfo &, const T *, double *, cudaStream_t);             \
+  template void seg_mean<T>(const SegInfo &, const T *, double *, cudaStream_t);            \
   template void seg_sub_mean<T>(const SegInfo &, i64, T *, const double *, cudaStream_t);   \
   template void seg_fcg_dir<T>(const SegInfo &, i64, T *, const T *, const T *, FcgScalars, \
                                cudaStream_t, float2 *);                                     \
@@ -865,8 +915,8 @@ void col_dot1(i64 n, int k, const T *x, const T *y, double *out, double *scratch
 }
 
 template <typename T>
-void cheb_init_zero(i64 n, int k, const T *b, const T *invd, double theta, T *d, cudaStream_t s) {
-  k_cheb_init_zero<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, b, invd, (T)theta, d);
+void cheb_init_zero(i64 n, int k, const T *b, const T *invd, double scale, T *d, cudaStream_t s) {
+  k_cheb_init_zero<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, b, invd, (T)scale, d);
   LG_LAUNCH();
 }
 template <typename T>
@@ -930,7 +980,7 @@ void col_reduce(i64 n, int k, Red op, const T *x, const T *y, double *out, doubl
 
 template <typename T>
 void sub_mean(i64 n, int k, T *x, const double *colsum, cudaStream_t s) {
-  k_sub_mean<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, x, colsum);
+  k_sub_mean<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, x, colsum, 1.0 / (double)n);
   LG_LAUNCH();
 }
 template <typename T>
@@ -947,8 +997,9 @@ void fcg_direction(i64 n, int k, T *p, const T *z, const T *pprev, const double 
 }
 template <typename T>
 void fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, const double *alpha,
-                bool update_r, cudaStream_t s) {
-  k_fcg_update<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, x, r, p, q, alpha, update_r ? 1 : 0);
+                bool update_r, cudaStream_t s, const float *alpha_f) {
+  k_fcg_update<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, x, r, p, q, alpha, alpha_f,
+                                                       update_r ? 1 : 0);
   LG_LAUNCH();
 }
 template <typename T>
@@ -987,7 +1038,7 @@ void scal_beta(int k, const double *zq, const double *eta_prev, double *beta, cu
   template void fcg_direction<T>(i64, int, T *, const T *, const T *, const double *,        \
                                  cudaStream_t);                                                \
   template void fcg_update<T>(i64, int, T *, T *, const T *, const T *, const double *, bool, \
-                              cudaStream_t);                                                   \
+                              cudaStream_t, const float *);                                    \
   template void cg_direction<T>(i64, int, T *, const T *, const double *, cudaStream_t);
 LG_INST(float)
 LG_INST(double)

@@ -60,6 +60,9 @@ enum class Epi {
   ElimInterp,  // y = A x + q .* b   (A = P, x = xc)
   Jacobi,      // y = xi + w invd (b - A x)   (weighted Jacobi sweep, w = c1)
   Split,       // y = A [X; x2]: columns < xsplit gather X, the others x2 (row j - xsplit)
+  ChebZ,       // first two Chebyshev steps from x = 0 with A D^-1 values, X = b:
+               // d0 = invd b / theta; r = b - (A D^-1 b) / theta;
+               // d = c1 d0 + c2 invd r; xo = d0 + d
 };
 
 struct EpiArgs {
@@ -74,7 +77,14 @@ struct EpiArgs {
   const void *din = nullptr; // ChebB: d_k (own row)
   void *dout = nullptr;      // ChebA/ChebB (nullable in ChebB)
   const void *q = nullptr;   // ElimInterp diagonal
-  double theta = 1, c1 = 0, c2 = 0;
+  double ith = 1, c1 = 0, c2 = 0;  // ith = 1 / theta: a product, never an FP64 division
+  // float copies of ith, c1, c2 for FP32 epilogues (set by mirror())
+  float fith = 1, fc1 = 0, fc2 = 0;
+  void mirror() {
+    fith = (float)ith;
+    fc1 = (float)c1;
+    fc2 = (float)c2;
+  }
 };
 
 // y-epilogue SpMM over k columns (X and all vectors are n x k row-major).
@@ -92,8 +102,9 @@ void spmm_df(const MatView<double> &A, const float2 *vdf, const float2 *X, int k
 void split_df(i64 count, const double *v, float2 *out, cudaStream_t s);
 
 // elementwise / transfer kernels (n x k row-major)
+// d = scale D^-1 b: the first smoothing step from a zero guess
 template <typename T>
-void cheb_init_zero(i64 n, int k, const T *b, const T *invd, double theta, T *d, cudaStream_t s);
+void cheb_init_zero(i64 n, int k, const T *b, const T *invd, double scale, T *d, cudaStream_t s);
 template <typename T>
 void fill_value(i64 cnt, T *x, T v, cudaStream_t s);
 template <typename T>
@@ -124,7 +135,8 @@ void fcg_direction(i64 n, int k, T *p, const T *z, const T *pprev, const double 
                    cudaStream_t s);  // p = z - beta p_prev (pprev null: p = z)
 template <typename T>
 void fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, const double *alpha,
-                bool update_r, cudaStream_t s);  // x += a p; r -= a q
+                bool update_r, cudaStream_t s,
+                const float *alpha_f = nullptr);  // x += a p; r -= a q (a: alpha_f if set)
 template <typename T>
 void cg_direction(i64 n, int k, T *p, const T *z, const double *beta, cudaStream_t s);  // p = z + beta p
 
@@ -139,6 +151,10 @@ struct FcgScalars {
   double *eta_prev;  // k
   double *alpha;     // k
   const int *frozen; // k or null: alpha forced to 0
+  // float copies of mu, beta (written by fcg_beta) and alpha (fcg_alpha) for
+  // the elementwise kernels of an FP32 solve, which then convert no FP64
+  // scalar per element (GB300's FP64 pipe is narrow); null: none
+  float *mu_f = nullptr, *beta_f = nullptr, *alpha_f = nullptr;
 };
 i64 fused_scratch_len(i64 n, int k);
 // mu = sum(z)/n; beta = (z.qp - mu sum(qp)) / eta_prev (beta = 0 if qp null)
@@ -174,11 +190,12 @@ void seg_fcg_alpha(const SegInfo &S, const T *p, const T *q, const T *r, FcgScal
                    cudaStream_t s);
 template <typename T>
 void seg_dot(const SegInfo &S, const T *x, const T *y, double *out, cudaStream_t s);
+// out[g] = mean of x over graph g's rows
 template <typename T>
-void seg_sum(const SegInfo &S, const T *x, double *out, cudaStream_t s);
-// elementwise with per-row scalar lookup scalar[rowseg[i]]
+void seg_mean(const SegInfo &S, const T *x, double *out, cudaStream_t s);
+// x_i -= means[rowseg[i]]
 template <typename T>
-void seg_sub_mean(const SegInfo &S, i64 n, T *x, const double *sums, cudaStream_t s);
+void seg_sub_mean(const SegInfo &S, i64 n, T *x, const double *means, cudaStream_t s);
 template <typename T>
 void seg_fcg_dir(const SegInfo &S, i64 n, T *p, const T *z, const T *pp, FcgScalars sc,
                  cudaStream_t s, float2 *pdf = nullptr);

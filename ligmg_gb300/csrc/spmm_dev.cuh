@@ -63,6 +63,14 @@ __device__ __forceinline__ void vstore(T *p, const T (&o)[VW]) {
   }
 }
 
+// Four FP32 values (rows of one reduction group) combined in a fixed order.
+__device__ __forceinline__ float sum4(const float (&x)[4]) {
+  return (x[0] + x[1]) + (x[2] + x[3]);
+}
+__device__ __forceinline__ float dot4(const float (&x)[4], const float (&y)[4]) {
+  return __fmaf_rn(x[3], y[3], __fmaf_rn(x[2], y[2], __fmaf_rn(x[1], y[1], x[0] * y[0])));
+}
+
 // matrix arrays: read-only cache loads from global memory (GX) or generic loads
 template <bool GX, typename V>
 __device__ __forceinline__ V mld(const V *p) {
@@ -73,6 +81,14 @@ template <typename T, int VW, bool GX>
 __device__ __forceinline__ void xload(const T *p, T (&o)[VW]) {
   if constexpr (GX) vldg<T, VW>(p, o);
   else vload<T, VW>(p, o);
+}
+
+// an epilogue scalar in the data's type: FP32 epilogues take the float copy
+// (no FP64 conversion per thread)
+template <typename T>
+__device__ __forceinline__ T escal(double d, float f) {
+  if constexpr (sizeof(T) == 4) return f;
+  else return (T)d;
 }
 
 template <typename T, int K, int VW, Epi E>
@@ -90,12 +106,11 @@ __device__ __forceinline__ void epilogue(const EpiArgs &a, i64 r, int c0, T (&ac
     T b[VW], x[VW], d[VW];
     vload<T, VW>((const T *)a.b + off, b);
     vload<T, VW>((const T *)a.xin + off, x);
-    const T iv = ((const T *)a.invd)[r];
-    const T th = (T)a.theta;
+    const T ivt = ((const T *)a.invd)[r] * escal<T>(a.ith, a.fith);
 #pragma unroll
     for (int q = 0; q < VW; q++) {
       b[q] = b[q] - acc[q];
-      d[q] = iv * b[q] / th;
+      d[q] = ivt * b[q];
       x[q] = x[q] + d[q];
     }
     vstore<T, VW>((T *)a.rout + off, b);
@@ -107,7 +122,7 @@ __device__ __forceinline__ void epilogue(const EpiArgs &a, i64 r, int c0, T (&ac
     vload<T, VW>((const T *)a.din + off, d);
     vload<T, VW>((const T *)a.xin + off, x);
     const T iv = ((const T *)a.invd)[r];
-    const T c1 = (T)a.c1, c2 = (T)a.c2;
+    const T c1 = escal<T>(a.c1, a.fc1), c2 = escal<T>(a.c2, a.fc2);
 #pragma unroll
     for (int q = 0; q < VW; q++) {
       rr[q] = rr[q] - acc[q];
@@ -115,6 +130,22 @@ __device__ __forceinline__ void epilogue(const EpiArgs &a, i64 r, int c0, T (&ac
       x[q] = x[q] + d[q];
     }
     if (a.rout) vstore<T, VW>((T *)a.rout + off, rr);
+    if (a.dout) vstore<T, VW>((T *)a.dout + off, d);
+    vstore<T, VW>((T *)a.xout + off, x);
+  } else if constexpr (E == Epi::ChebZ) {
+    T b[VW], d0[VW], d[VW], x[VW];
+    vload<T, VW>((const T *)a.b + off, b);
+    const T iv = ((const T *)a.invd)[r];
+    const T ith = escal<T>(a.ith, a.fith), ivt = iv * ith;
+    const T c1 = escal<T>(a.c1, a.fc1), c2 = escal<T>(a.c2, a.fc2);
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      d0[q] = ivt * b[q];
+      b[q] = b[q] - acc[q] * ith;  // the residual after the first step
+      d[q] = c1 * d0[q] + c2 * (iv * b[q]);
+      x[q] = d0[q] + d[q];
+    }
+    if (a.rout) vstore<T, VW>((T *)a.rout + off, b);
     if (a.dout) vstore<T, VW>((T *)a.dout + off, d);
     vstore<T, VW>((T *)a.xout + off, x);
   } else if constexpr (E == Epi::ElimInterp) {
@@ -128,7 +159,7 @@ __device__ __forceinline__ void epilogue(const EpiArgs &a, i64 r, int c0, T (&ac
     T b[VW], x[VW];
     vload<T, VW>((const T *)a.b + off, b);
     vload<T, VW>((const T *)a.xin + off, x);
-    const T wi = (T)a.c1 * ((const T *)a.invd)[r];
+    const T wi = escal<T>(a.c1, a.fc1) * ((const T *)a.invd)[r];
 #pragma unroll
     for (int q = 0; q < VW; q++) x[q] = x[q] + wi * (b[q] - acc[q]);
     vstore<T, VW>((T *)a.y + off, x);

@@ -107,6 +107,7 @@ __device__ void run_spmm(const TOp<T> &op, i64 gwarp, i64 nwarps, int lane) {
     LG_TAIL_EPI(Epi::ElimInterp)
     LG_TAIL_EPI(Epi::Jacobi)
     LG_TAIL_EPI(Epi::Split)
+    LG_TAIL_EPI(Epi::ChebZ)
 #undef LG_TAIL_EPI
   }
 }
@@ -124,19 +125,46 @@ __device__ void block_partials(const T *x, const T *y, const T *w, bool use_y, i
   double a[NV];
 #pragma unroll
   for (int v = 0; v < NV; v++) a[v] = 0;
-  for (i64 r = r0 + rsub; r < r1; r += RS) {
-    const i64 o = r * K + c;
-    const double xv = (double)x[o];
-    if constexpr (NV == 3) {  // sum z, z.qp, sum qp
-      a[0] += xv;
-      if (use_y) {
-        const double yv = (double)y[o];
-        a[1] += xv * yv;
-        a[2] += yv;
+  if constexpr (sizeof(T) == 4) {
+    // four rows per step combined in FP32, one FP64 add per group (as in the
+    // launched reductions)
+    for (i64 r = r0 + rsub; r < r1; r += 4 * (i64)RS) {
+      float xv[4], yv[4], wv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const i64 rr = r + (i64)u * RS;
+        const bool ok = rr < r1;
+        const i64 o = rr * K + c;
+        xv[u] = ok ? x[o] : 0.f;
+        yv[u] = (ok && use_y) ? y[o] : 0.f;
+        wv[u] = (NV == 2 && ok) ? w[o] : 0.f;
       }
-    } else {  // p.q, p.r
-      a[0] += xv * (double)y[o];
-      a[1] += xv * (double)w[o];
+      if constexpr (NV == 3) {
+        a[0] += (double)sum4(xv);
+        if (use_y) {
+          a[1] += (double)dot4(xv, yv);
+          a[2] += (double)sum4(yv);
+        }
+      } else {
+        a[0] += (double)dot4(xv, yv);
+        a[1] += (double)dot4(xv, wv);
+      }
+    }
+  } else {
+    for (i64 r = r0 + rsub; r < r1; r += RS) {
+      const i64 o = r * K + c;
+      const double xv = (double)x[o];
+      if constexpr (NV == 3) {  // sum z, z.qp, sum qp
+        a[0] += xv;
+        if (use_y) {
+          const double yv = (double)y[o];
+          a[1] += xv * yv;
+          a[2] += yv;
+        }
+      } else {  // p.q, p.r
+        a[0] += xv * (double)y[o];
+        a[1] += xv * (double)w[o];
+      }
     }
   }
 #pragma unroll
@@ -199,7 +227,7 @@ __global__ void __launch_bounds__(NT, 1)
            const uint4 *__restrict__ image, int image_vec, TailIO<T> io) {
   static_assert(NT % K == 0 && NT >= 64, "tail block size");
   __shared__ double sh[3][NT];
-  __shared__ double scal[2][64];
+  __shared__ T scal[2][64];  // column scalars in the data's type (converted once)
   __shared__ int sh_abort;
   // cooperating CTAs: all of them (grid mode) or this one (shared-memory mode)
   const int cta = SM ? 0 : (int)blockIdx.x;
@@ -240,8 +268,8 @@ __global__ void __launch_bounds__(NT, 1)
         run_spmm<T, K, SM>(op, gwarp, nwarps, lane);
         break;
       case TOpKind::Cheb0: {
-        const T th = (T)op.f;
-        for (i64 t = gthr; t < nk; t += nthr) y0[t] = x1[t / K] * x0[t] / th;
+        const T f = (T)op.f;
+        for (i64 t = gthr; t < nk; t += nthr) y0[t] = (x1[t / K] * f) * x0[t];
         break;
       }
       case TOpKind::Prolong:
@@ -283,8 +311,8 @@ __global__ void __launch_bounds__(NT, 1)
             const double e = sc.eta_prev[c];
             beta = e == 0.0 ? 0.0 : (sh[1][c] - mu * sh[2][c]) / e;
           }
-          scal[0][c] = mu;
-          scal[1][c] = beta;
+          scal[0][c] = (T)mu;
+          scal[1][c] = (T)beta;
           if (cta == 0) {
             sc.mu[c] = mu;
             sc.beta[c] = beta;
@@ -293,8 +321,8 @@ __global__ void __launch_bounds__(NT, 1)
         __syncthreads();
         for (i64 t = gthr; t < nk; t += nthr) {
           const int c = (int)(t % K);
-          T v = x0[t] - (T)scal[0][c];
-          if (op.flag) v = v - (T)scal[1][c] * x1[t];
+          T v = x0[t] - scal[0][c];
+          if (op.flag) v = v - scal[1][c] * x1[t];
           y0[t] = v;
         }
         break;
@@ -305,7 +333,7 @@ __global__ void __launch_bounds__(NT, 1)
           const int c = threadIdx.x;
           const double eta = sh[0][c];
           const double alpha = eta == 0.0 ? 0.0 : sh[1][c] / eta;
-          scal[0][c] = alpha;
+          scal[0][c] = (T)alpha;
           if (cta == 0) {
             sc.eta[c] = eta;
             sc.alpha[c] = alpha;
@@ -313,7 +341,7 @@ __global__ void __launch_bounds__(NT, 1)
         }
         __syncthreads();
         for (i64 t = gthr; t < nk; t += nthr) {
-          const T a = (T)scal[0][(int)(t % K)];
+          const T a = scal[0][(int)(t % K)];
           y0[t] = y0[t] + a * x0[t];
           if (op.flag) y1[t] = y1[t] - a * x1[t];
         }

@@ -16,7 +16,7 @@ namespace lg {
 
 enum class TOpKind : int {
   Spmm,      // y = A X with epilogue `epi` (hub chunks included)
-  Cheb0,     // d = D^-1 b / theta                       (first Chebyshev step)
+  Cheb0,     // d = f D^-1 b (f = 1/theta; omega for Jacobi) (first smoothing step)
   Prolong,   // x += xc[agg]
   Coarse,    // x = pinv b (dense)
   Scale,     // x *= f
@@ -43,7 +43,7 @@ struct TOp {
   T *y0 = nullptr;          // Cheb0 d; Prolong/Coarse/Scale/Zero x; Copy dst; Dir p; Update x
   T *y1 = nullptr;          // Update r
   const i32 *idx = nullptr; // Prolong agg
-  double f = 1;             // Cheb0 theta; Scale factor
+  double f = 1;             // Cheb0 and Scale factor
   FcgScalars sc{};          // Dir/Update
 };
 
