@@ -89,7 +89,7 @@ namespace {
 using namespace dev;
 
 template <typename T, int K, int G, Epi EP>
-__global__ void __launch_bounds__(256) k_spmm(const MatView<T> A, const T *__restrict__ X,
+__global__ void __launch_bounds__(256, 6) k_spmm(const MatView<T> A, const T *__restrict__ X,
                                               const EpiArgs a) {
   const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   dev::spmm_unit<T, K, G, EP>(A, X, a, warp, threadIdx.x & 31);

@@ -180,37 +180,92 @@ __device__ __forceinline__ const T *xsrc(const MatView<T> &A, const T *X, i32 j)
 
 // GX: matrix and X in global memory (read-only cache loads); otherwise they
 // may be staged in shared memory and are read with generic loads.
+//
+// A lane takes entries k, k + E, k + 2E, ... of [k, e), four per step, and
+// loads the column indices of the next step before gathering this step's X
+// rows, so a step waits for one dependent latency (the gather) instead of two
+// (index, then gather).  Products are added in entry order.
+//   GX (global memory): full steps are branch-free; the last entries (fewer
+//     than four) go one at a time.
+//   otherwise (shared memory, coarse levels with short rows): the last step
+//     is masked (no gather, zero product past e), so no row pays a second
+//     loop.
 template <typename T, int K, int VW, int E, bool GX = true, bool SPLIT = false>
 __device__ __forceinline__ void row_accumulate(const MatView<T> &A, const T *__restrict__ X, i64 k,
                                                i64 e, int ch, T (&acc)[VW]) {
   const T *__restrict__ av = A.v;
   const i32 *__restrict__ ac = A.ci;
-  for (; k + 3 * E < e; k += 4 * E) {
-    T a0 = mld<GX>(av + k), a1 = mld<GX>(av + k + E), a2 = mld<GX>(av + k + 2 * E),
-      a3 = mld<GX>(av + k + 3 * E);
-    i32 j0 = mld<GX>(ac + k), j1 = mld<GX>(ac + k + E), j2 = mld<GX>(ac + k + 2 * E),
-        j3 = mld<GX>(ac + k + 3 * E);
-    T x0[VW], x1[VW], x2[VW], x3[VW];
-    xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j0) + ch * VW, x0);
-    xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j1) + ch * VW, x1);
-    xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j2) + ch * VW, x2);
-    xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j3) + ch * VW, x3);
+  if constexpr (GX) {
+    if (k + 3 * E < e) {
+      i32 jn[4];
 #pragma unroll
-    for (int q = 0; q < VW; q++) acc[q] += a0 * x0[q];
+      for (int u = 0; u < 4; u++) jn[u] = mld<GX>(ac + k + u * E);
+      while (true) {
+        i32 j[4];
 #pragma unroll
-    for (int q = 0; q < VW; q++) acc[q] += a1 * x1[q];
+        for (int u = 0; u < 4; u++) j[u] = jn[u];
+        const i64 kn = k + 4 * E;
+        const bool more = kn + 3 * E < e;
+        if (more) {
 #pragma unroll
-    for (int q = 0; q < VW; q++) acc[q] += a2 * x2[q];
+          for (int u = 0; u < 4; u++) jn[u] = mld<GX>(ac + kn + u * E);
+        }
+        T a[4], x[4][VW];
 #pragma unroll
-    for (int q = 0; q < VW; q++) acc[q] += a3 * x3[q];
-  }
-  for (; k < e; k += E) {
-    T a0 = mld<GX>(av + k);
-    i32 j0 = mld<GX>(ac + k);
-    T x0[VW];
-    xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j0) + ch * VW, x0);
+        for (int u = 0; u < 4; u++) {
+          a[u] = mld<GX>(av + k + u * E);
+          xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j[u]) + ch * VW, x[u]);
+        }
 #pragma unroll
-    for (int q = 0; q < VW; q++) acc[q] += a0 * x0[q];
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+          for (int q = 0; q < VW; q++) acc[q] += a[u] * x[u][q];
+        k = kn;
+        if (!more) break;
+      }
+    }
+    for (; k < e; k += E) {
+      T a0 = mld<GX>(av + k);
+      i32 j0 = mld<GX>(ac + k);
+      T x0[VW];
+      xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j0) + ch * VW, x0);
+#pragma unroll
+      for (int q = 0; q < VW; q++) acc[q] += a0 * x0[q];
+    }
+  } else {
+    if (k >= e) return;
+    i32 jn[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) jn[u] = (k + u * E < e) ? mld<GX>(ac + k + u * E) : -1;
+    while (true) {
+      i32 j[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) j[u] = jn[u];
+      const i64 kn = k + 4 * E;
+      const bool more = kn < e;
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) jn[u] = (kn + u * E < e) ? mld<GX>(ac + kn + u * E) : -1;
+      }
+      T a[4], x[4][VW];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (j[u] >= 0) {
+          a[u] = mld<GX>(av + k + u * E);
+          xload<T, VW, GX>(xsrc<T, K, SPLIT>(A, X, j[u]) + ch * VW, x[u]);
+        } else {
+          a[u] = (T)0;
+#pragma unroll
+          for (int q = 0; q < VW; q++) x[u][q] = (T)0;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int q = 0; q < VW; q++) acc[q] += a[u] * x[u][q];
+      if (!more) break;
+      k = kn;
+    }
   }
 }
 
