@@ -286,14 +286,18 @@ MatView<T> bare_view(const Level &L, int which) {
 // k), every candidate shape is timed on this level's own matrix (y = A x,
 // x = 0, one warm-up and three timed launches on the handle's stream) and the
 // fastest is kept with the plan:
-//   hub chunk size   split unit x {1, 2, 4}: long rows stay whole longer on
-//                    levels with many rows, are cut finer on small levels
+//   chunk size       split unit U x {8, 16, 32, 64, 128} entries (rows over
+//                    twice that are cut): long rows stay whole on levels
+//                    with many rows; on levels of at most 2^17 rows, where a
+//                    launch has too few warps to hide the gather latency,
+//                    rows of a few dozen entries are cut into several
+//                    warps' chunks (8 U and 16 U are tried there only)
 //   threads/block    {64, 128, 256}: small blocks free their slot as soon as
 //                    their rows finish (rows differ widely in length)
 //   lanes per row    {4, 8, 16, 32} for k = 1 on levels without hub rows
 // The choice only changes launch shapes and, on hub rows, how a row's sum is
 // split into chunk partials (its rounding); autotune = 0 uses the defaults
-// (factor 1, 64 threads for k > 1, 256 for k = 1, the level's lanes).
+// (chunks of 32 U, 64 threads for k > 1, 256 for k = 1, the level's lanes).
 template <typename T>
 void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotune,
                 cudaStream_t s) {
@@ -303,7 +307,7 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   LG_CUDA(cudaStreamIsCapturing(s, &cs));
   if (!autotune || cs != cudaStreamCaptureStatusNone || n <= 0) {
-    best.build(rp.data(), n, unit, k, s);
+    best.build(rp.data(), n, 32 * (i64)unit, k, s);
     best.tb = k > 1 ? 64 : 256;
     return;
   }
@@ -318,10 +322,12 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
   float best_ms = 1e30f;
   bool have = false;
   bool chunks_seen = true;
-  for (int f : {1, 2, 4}) {
-    if (!chunks_seen) break;  // no hub rows at a smaller unit: none at larger ones
+  for (int f : {8, 16, 32, 64, 128}) {
+    if (!chunks_seen) break;  // no long rows at a smaller split: none at larger ones
+    // the finer cuts only pay where a launch has few warps for its rows
+    if (f < 32 && n > (i64)131072) continue;
     HubPlan<T> cand;
-    cand.build(rp.data(), n, unit * f, k, s);
+    cand.build(rp.data(), n, (i64)unit * f, k, s);
     chunks_seen = cand.nchunks > 0;
     std::vector<int> lane_opts{0};
     if (k == 1 && cand.nchunks == 0) lane_opts = {4, 8, 16, 32};
@@ -352,7 +358,6 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
       best = std::move(cand);
       best.tb = cand_tb;
       best.lanes = cand_lanes;
-      best.factor = f;
       best_ms = cand_ms;
       have = true;
     }
@@ -1659,7 +1664,7 @@ void finish_level(Handle &H, Level &L) {
   L.lanesA = lanes_for(L.A.nnz, L.A.n);
   L.autotune = H.opts.autotune != 0;
   L.rp_host = L.A.rp.to_host();
-  L.hubA64.build(L.rp_host.data(), L.A.n, split_unit(8, 1), 1, s);
+  L.hubA64.build(L.rp_host.data(), L.A.n, 32 * (i64)split_unit(8, 1), 1, s);
   if (L.type == LIGMG_LEVEL_ELIM) {
     L.rrp_host = L.elim.R.rp.to_host();
     L.lanesR = lanes_for(L.elim.R.nnz, L.elim.R.n);

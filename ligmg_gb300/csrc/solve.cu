@@ -21,10 +21,11 @@ int split_unit(int value_bytes, int k) {
 }
 
 template <typename T>
-void HubPlan<T>::build(const i64 *rp_host, i64 n, int E, int kmax, cudaStream_t s) {
+void HubPlan<T>::build(const i64 *rp_host, i64 n, i64 split_len, int kmax, cudaStream_t s) {
   built = true;
   kcap = kmax;
-  thresh = 64 * (i64)E;
+  split = split_len;
+  thresh = 2 * split_len;
   i64 thr = thresh;
   std::vector<i64> row, beg, end;
   std::vector<i32> hub, first, cnt;
@@ -32,7 +33,7 @@ void HubPlan<T>::build(const i64 *rp_host, i64 n, int E, int kmax, cudaStream_t 
   for (i64 r = 0; r < n; r++) {
     i64 len = rp_host[r + 1] - rp_host[r];
     if (len <= thr) continue;
-    i64 want = std::min<i64>(std::max<i64>(cdiv(len, 32 * (i64)E), 2), 256);
+    i64 want = std::min<i64>(std::max<i64>(cdiv(len, split_len), 2), 256);
     i64 chunk = cdiv(len, want);
     i32 nc = (i32)cdiv(len, chunk);
     i32 f = (i32)row.size();
@@ -551,27 +552,41 @@ __device__ __forceinline__ void df_ldg(const float2 *p, float (&h)[VW], float (&
   }
 }
 
+// Entries k, k + E, ... of [k, e), four per step; the next step's column
+// indices load before this step's gathers (one dependent latency per step),
+// the last entries go one at a time.
 template <int K, int VW, int E>
 __device__ __forceinline__ void df_row(const MatView<double> &A, const float2 *__restrict__ vdf,
                                        const float2 *__restrict__ X, i64 k, i64 e, int ch,
                                        float (&sh)[VW], float (&sl)[VW]) {
   const i32 *__restrict__ ac = A.ci;
-  for (; k + 3 * E < e; k += 4 * E) {
-    float2 a0 = __ldg(vdf + k), a1 = __ldg(vdf + k + E), a2 = __ldg(vdf + k + 2 * E),
-           a3 = __ldg(vdf + k + 3 * E);
-    i32 j0 = __ldg(ac + k), j1 = __ldg(ac + k + E), j2 = __ldg(ac + k + 2 * E),
-        j3 = __ldg(ac + k + 3 * E);
-    float h0[VW], l0[VW], h1[VW], l1[VW], h2[VW], l2[VW], h3[VW], l3[VW];
-    df_ldg<VW>(X + (i64)j0 * K + ch * VW, h0, l0);
-    df_ldg<VW>(X + (i64)j1 * K + ch * VW, h1, l1);
-    df_ldg<VW>(X + (i64)j2 * K + ch * VW, h2, l2);
-    df_ldg<VW>(X + (i64)j3 * K + ch * VW, h3, l3);
+  if (k + 3 * E < e) {
+    i32 jn[4];
 #pragma unroll
-    for (int q = 0; q < VW; q++) {
-      df_fma(a0.x, a0.y, h0[q], l0[q], sh[q], sl[q]);
-      df_fma(a1.x, a1.y, h1[q], l1[q], sh[q], sl[q]);
-      df_fma(a2.x, a2.y, h2[q], l2[q], sh[q], sl[q]);
-      df_fma(a3.x, a3.y, h3[q], l3[q], sh[q], sl[q]);
+    for (int u = 0; u < 4; u++) jn[u] = __ldg(ac + k + u * E);
+    while (true) {
+      i32 j[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) j[u] = jn[u];
+      const i64 kn = k + 4 * E;
+      const bool more = kn + 3 * E < e;
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) jn[u] = __ldg(ac + kn + u * E);
+      }
+      float2 a[4];
+      float h[4][VW], l[4][VW];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        a[u] = __ldg(vdf + k + u * E);
+        df_ldg<VW>(X + (i64)j[u] * K + ch * VW, h[u], l[u]);
+      }
+#pragma unroll
+      for (int q = 0; q < VW; q++)
+#pragma unroll
+        for (int u = 0; u < 4; u++) df_fma(a[u].x, a[u].y, h[u][q], l[u][q], sh[q], sl[q]);
+      k = kn;
+      if (!more) break;
     }
   }
   for (; k < e; k += E) {

@@ -44,12 +44,14 @@ struct HubPlan {
   // launch shape kept with the plan (picked by the autotuner or defaults)
   int tb = 256;    // threads per block
   int lanes = 0;   // lanes per row for k = 1 (0: the level's default)
-  int factor = 1;  // split unit multiplier the chunks were built with
-  void build(const i64 *rp_host, i64 n, int unit, int kmax, cudaStream_t s);
+  i64 split = 0;   // target entries per chunk: rows longer than 2 x split are
+                   // cut into chunks of about split entries (at most 256 chunks)
+  void build(const i64 *rp_host, i64 n, i64 split_len, int kmax, cudaStream_t s);
   void fill(MatView<T> &m) const;
 };
 // Hub split unit U for k right-hand sides: the nonzeros a 32-lane group
-// advances per step (E = 32 / (k / VW) entry slots).
+// advances per step (E = 32 / (k / VW) entry slots).  The default chunk is
+// 32 U entries (eight unrolled steps of four).
 int split_unit(int value_bytes, int k);
 
 enum class Epi {
