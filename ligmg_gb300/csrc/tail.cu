@@ -94,9 +94,25 @@ __device__ void run_spmm(const TOp<T> &op, i64 gwarp, i64 nwarps, int lane) {
     a.din = res<SM>(a.din);
     a.dout = res<SM>(a.dout);
   }
+  // Shared-memory mode (whole rows, no chunks): when a row averages at most
+  // two unrolled steps of an 8-lane group, 8 lanes take each row and a warp
+  // works on four rows at once; a warp of 32 lanes would walk the level's
+  // short rows one by one, each ending in a five-level shuffle reduction.
+  constexpr int VW = (K % VT<T>::W == 0) ? VT<T>::W : 1;
+  constexpr int L = K / VW;
+  bool narrow = false;
+  if constexpr (SM && L <= 8) narrow = (A.rp[A.n] - A.rp[0]) * L <= (i64)64 * A.n;
+  const i64 units8 = (A.n + 3) / 4;
   switch (op.epi) {
 #define LG_TAIL_EPI(E)                                                        \
   case E:                                                                     \
+    if constexpr (SM && L <= 8) {                                             \
+      if (narrow) {                                                           \
+        for (i64 u = gwarp; u < units8; u += nwarps)                          \
+          spmm_unit<T, K, 8, E, !SM>(A, X, a, u, lane);                       \
+        break;                                                                \
+      }                                                                       \
+    }                                                                         \
     for (i64 u = gwarp; u < units; u += nwarps)                               \
       spmm_unit<T, K, 32, E, !SM>(A, X, a, u, lane);                          \
     break;
