@@ -101,6 +101,16 @@ __global__ void k_ad_values(i64 nnz, const i32 *ci, const double *v, const doubl
   if (t < nnz) ad[t] = v[t] * invd[ci[t]];
 }
 
+// rs_i = sum of row i's stored values (in column order, accumulated in FP64)
+template <typename V>
+__global__ void k_rowsum(const i64 *rp, const V *v, i64 n, V *rs) {
+  i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double t = 0;
+  for (i64 k = rp[i]; k < rp[i + 1]; k++) t += (double)v[k];
+  rs[i] = (V)t;
+}
+
 __global__ void k_invdiag(const i64 *rp, const i32 *ci, const double *v, i64 n, double *invd) {
   i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -192,6 +202,10 @@ struct Level {
   // gathers b itself (A d0 = A D^-1 b / theta)
   DBuf<double> ADv;
   DBuf<float> AD32;
+  // row sums of A's stored values (zero up to rounding for a Laplacian): the
+  // fused FCG direction product uses A (z - mu 1) = A z - mu rs
+  DBuf<double> rs64;
+  DBuf<float> rs32;
   // hub-row plans: hubA64 (FP64, k = 1) is built at setup; the others are
   // built on first use per (precision, k) from the cached host row pointers
   HubPlan<double> hubA64;
@@ -435,6 +449,11 @@ const T *invdT(const Level &L) {
   else return (const T *)L.invd32.p;
 }
 template <typename T>
+const T *rowsumT(const Level &L) {
+  if constexpr (sizeof(T) == 8) return (const T *)L.rs64.p;
+  else return (const T *)L.rs32.p;
+}
+template <typename T>
 const T *QT(const Level &L) {
   if constexpr (sizeof(T) == 8) return (const T *)L.elim.Q.p;
   else return (const T *)L.Q32.p;
@@ -673,6 +692,9 @@ void ensure_fp32(Handle &H) {
     if (L.has32) continue;
     L.Av32.alloc(L.A.nnz, s);
     convert<double, float>(L.A.nnz, L.A.v.p, L.Av32.p, s);
+    L.rs32.alloc(L.A.n, s);
+    k_rowsum<float><<<grid_for(L.A.n, 256), 256, 0, s>>>(L.A.rp.p, L.Av32.p, L.A.n, L.rs32.p);
+    LG_LAUNCH();
     if (L.invd.n) {
       L.invd32.alloc(L.invd.n, s);
       convert<double, float>(L.invd.n, L.invd.p, L.invd32.p, s);
@@ -1524,9 +1546,12 @@ struct Engine {
   }
 
   // K-cycle inner FCG with a fixed number of iterations, x0 = 0; r = b is
-  // updated in place (b is the level's restriction buffer).  Five launches
-  // per iteration: cycle, beta (fused reduction), direction, SpMM, alpha
-  // (fused reduction), update.
+  // updated in place (b is the level's restriction buffer).  Four launches
+  // per iteration besides the cycle: beta (fused reduction), direction and
+  // its product in one SpMM (Epi::FcgDir), alpha (fused reduction), update.
+  // The product of the direction p = (z - mu) - beta pp is formed as
+  // A z - mu rowsum(A) - beta qp: equal to A p up to rounding, since qp is
+  // the previous direction's product (batch mode: direction, then SpMM).
   void fcg_fixed(size_t l, T *b, T *x, int iters) {
     Level &L = *H.h[l];
     LevelWork<T> &w = W.lw[l];
@@ -1552,20 +1577,40 @@ struct Engine {
     for (int it = 0; it < iters; it++) {
       cycle(l, r, w.fz.p);
       const double nk = (double)n * k * sizeof(T);
-      timed(H, (int)l, LIGMG_KERNEL_KRYLOV, k, sizeof(T) == 8, (it > 0 ? 5.0 : 3.0) * nk, [&] {
-        if (seg) {
+      if (seg) {  // per-graph scalars: direction, then its product
+        timed(H, (int)l, LIGMG_KERNEL_KRYLOV, k, sizeof(T) == 8, (it > 0 ? 5.0 : 3.0) * nk, [&] {
           seg_fcg_beta<T>(S, w.fz.p, it > 0 ? qp : nullptr, sc, s);
           seg_fcg_dir<T>(S, n, p, w.fz.p, it > 0 ? pp : nullptr, sc, s);
+        });
+        EpiArgs a;
+        a.y = q;
+        timed(H, (int)l, LIGMG_KERNEL_SPMV, k, sizeof(T) == 8,
+              core_bytes(n, L.A.nnz, n, k, sizeof(T)) + 1.0 * n * k * sizeof(T),
+              [&] { spmm<T>(A, p, k, Epi::Store, a, s); });
+      } else {
+        // beta (reduction), then p and q = A p in one SpMM gathering z
+        timed(H, (int)l, LIGMG_KERNEL_KRYLOV, k, sizeof(T) == 8, (it > 0 ? 2.0 : 1.0) * nk,
+              [&] { fcg_beta<T>(n, k, w.fz.p, it > 0 ? qp : nullptr, sc, w.fscratch.p, s); });
+        EpiArgs a;
+        a.xin = w.fz.p;
+        a.q = rowsumT<T>(L);
+        if constexpr (sizeof(T) == 4) {
+          a.cmu = sc.mu_f;
+          a.cbeta = sc.beta_f;
         } else {
-          fcg_beta<T>(n, k, w.fz.p, it > 0 ? qp : nullptr, sc, w.fscratch.p, s);
-          fcg_dir<T>(n, k, p, w.fz.p, it > 0 ? pp : nullptr, sc, s);
+          a.cmu = sc.mu;
+          a.cbeta = sc.beta;
         }
-      });
-      EpiArgs a;
-      a.y = q;
-      timed(H, (int)l, LIGMG_KERNEL_SPMV, k, sizeof(T) == 8,
-            core_bytes(n, L.A.nnz, n, k, sizeof(T)) + 1.0 * n * k * sizeof(T),
-            [&] { spmm<T>(A, p, k, Epi::Store, a, s); });
+        if (it > 0) {
+          a.din = pp;
+          a.rin = qp;
+        }
+        a.dout = p;
+        a.y = q;
+        timed(H, (int)l, LIGMG_KERNEL_SPMV, k, sizeof(T) == 8,
+              core_bytes(n, L.A.nnz, n, k, sizeof(T)) + (it > 0 ? 5.0 : 3.0) * nk + n * sizeof(T),
+              [&] { spmm<T>(A, w.fz.p, k, Epi::FcgDir, a, s); });
+      }
       timed(H, (int)l, LIGMG_KERNEL_KRYLOV, k, sizeof(T) == 8, (it + 1 < iters ? 9.0 : 6.0) * nk,
             [&] {
               if (seg) {
@@ -1660,6 +1705,9 @@ void finish_level(Handle &H, Level &L) {
   cudaStream_t s = H.s;
   L.invd.alloc(L.A.n, s);
   k_invdiag<<<grid_for(L.A.n, 256), 256, 0, s>>>(L.A.rp.p, L.A.ci.p, L.A.v.p, L.A.n, L.invd.p);
+  LG_LAUNCH();
+  L.rs64.alloc(L.A.n, s);
+  k_rowsum<double><<<grid_for(L.A.n, 256), 256, 0, s>>>(L.A.rp.p, L.A.v.p, L.A.n, L.rs64.p);
   LG_LAUNCH();
   L.lanesA = lanes_for(L.A.nnz, L.A.n);
   L.autotune = H.opts.autotune != 0;

@@ -150,6 +150,7 @@ void spmm(const MatView<T> &A, const T *X, int k, Epi epi, const EpiArgs &args, 
     case Epi::Jacobi: return dispatch_k<T, Epi::Jacobi>(A, X, k, a, s);
     case Epi::Split: return dispatch_k<T, Epi::Split>(A, X, k, a, s);
     case Epi::ChebZ: return dispatch_k<T, Epi::ChebZ>(A, X, k, a, s);
+    case Epi::FcgDir: return dispatch_k<T, Epi::FcgDir>(A, X, k, a, s);
   }
 }
 template void spmm<float>(const MatView<float> &, const float *, int, Epi, const EpiArgs &,

@@ -65,6 +65,9 @@ enum class Epi {
   ChebZ,       // first two Chebyshev steps from x = 0 with A D^-1 values, X = b:
                // d0 = invd b / theta; r = b - (A D^-1 b) / theta;
                // d = c1 d0 + c2 invd r; xo = d0 + d
+  FcgDir,      // FCG direction and its product in one pass, X = z:
+               // p = (z - mu) - beta pp;  y = A z - mu rowsum(A) - beta qp
+               // (= A p, as qp = A pp); pp, qp null on the first iteration
 };
 
 struct EpiArgs {
@@ -78,7 +81,8 @@ struct EpiArgs {
   void *rout = nullptr;      // ChebA/ChebB (nullable in ChebB)
   const void *din = nullptr; // ChebB: d_k (own row)
   void *dout = nullptr;      // ChebA/ChebB (nullable in ChebB)
-  const void *q = nullptr;   // ElimInterp diagonal
+  const void *q = nullptr;   // ElimInterp diagonal; FcgDir row sums of A
+  const void *cmu = nullptr, *cbeta = nullptr;  // FcgDir: per-column mu, beta (k values)
   double ith = 1, c1 = 0, c2 = 0;  // ith = 1 / theta: a product, never an FP64 division
   // float copies of ith, c1, c2 for FP32 epilogues (set by mirror())
   float fith = 1, fc1 = 0, fc2 = 0;

@@ -148,6 +148,29 @@ __device__ __forceinline__ void epilogue(const EpiArgs &a, i64 r, int c0, T (&ac
     if (a.rout) vstore<T, VW>((T *)a.rout + off, b);
     if (a.dout) vstore<T, VW>((T *)a.dout + off, d);
     vstore<T, VW>((T *)a.xout + off, x);
+  } else if constexpr (E == Epi::FcgDir) {
+    T z[VW], mu[VW], pv[VW], qv[VW];
+    vload<T, VW>((const T *)a.xin + off, z);
+    vload<T, VW>((const T *)a.cmu + c0, mu);
+    const T rs = ((const T *)a.q)[r];
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      pv[q] = z[q] - mu[q];
+      qv[q] = acc[q] - mu[q] * rs;
+    }
+    if (a.din) {
+      T be[VW], pp[VW], qp[VW];
+      vload<T, VW>((const T *)a.cbeta + c0, be);
+      vload<T, VW>((const T *)a.din + off, pp);
+      vload<T, VW>((const T *)a.rin + off, qp);
+#pragma unroll
+      for (int q = 0; q < VW; q++) {
+        pv[q] = pv[q] - be[q] * pp[q];
+        qv[q] = qv[q] - be[q] * qp[q];
+      }
+    }
+    vstore<T, VW>((T *)a.dout + off, pv);
+    vstore<T, VW>((T *)a.y + off, qv);
   } else if constexpr (E == Epi::ElimInterp) {
     T b[VW];
     vload<T, VW>((const T *)a.b + off, b);

@@ -125,6 +125,8 @@ __device__ void run_spmm(const TOp<T> &op, i64 gwarp, i64 nwarps, int lane) {
     LG_TAIL_EPI(Epi::Split)
     LG_TAIL_EPI(Epi::ChebZ)
 #undef LG_TAIL_EPI
+    default:  // Epi::FcgDir: the tail program keeps direction and product apart
+      break;
   }
 }
 
