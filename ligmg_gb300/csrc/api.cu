@@ -473,6 +473,8 @@ struct LevelWork {
   i64 n = 0;
   DBuf<T> in, out, r, d0, d1, xt;           // cycle buffers
   DBuf<T> fz, fp0, fp1, fq0, fq1;           // K-cycle FCG buffers (fr = in, fx = out)
+  DBuf<T> gV, gZ, gW;                       // K-cycle FGMRES: basis, preconditioned basis, A z
+  DBuf<double> gH;                          // K-cycle FGMRES scalars
   DBuf<double> sc, scratch, fscratch;
   DBuf<double> segsc;  // batch mode: S_NSLOT x nseg scalars
   i64 scratch_len = 0, nseg = 0;
@@ -1189,6 +1191,7 @@ void tail_plan(Handle &H, Work<T> &W) {
   ts.start = 0;
   const i64 lim = H.opts.tail_rows;
   if (lim < 0 || H.h.size() < 2) return;
+  if (H.opts.kcycle && H.opts.kcycle_ksp_type != LIGMG_KSP_FCG) return;  // programs record FCG
   if (H.h[0]->seginfo().nseg > 0) return;  // batch mode keeps per-graph kernels
   if (lim > 0) {
     if (tail_max_ctas<T>(W.k) <= 0) return;
@@ -1513,7 +1516,71 @@ struct Engine {
       cycle(l + 1, bc, xc);
       return;
     }
-    fcg_fixed(l + 1, bc, xc, o().kcycle_iters);
+    if (o().kcycle_ksp_type == LIGMG_KSP_FGMRES) fgmres_fixed(l + 1, bc, xc, o().kcycle_iters);
+    else fcg_fixed(l + 1, bc, xc, o().kcycle_iters);
+  }
+
+  // K-cycle inner FGMRES (kcycle_ksp_type = fgmres, parse_options.hpp:399-400):
+  // exactly m Arnoldi steps from x = 0 (PETSc's restart length, 30, exceeds the
+  // K-cycle's iteration count), the outer FGMRES's arithmetic otherwise: b's
+  // constant projected out, right preconditioning with the cycle of level l
+  // (its constant projected out), classical Gram-Schmidt, Givens rotations and
+  // back substitution.  The Hessenberg least squares runs on the device (one
+  // thread per column), so the inner solve stays inside the preconditioner's
+  // CUDA graph; b (the level's restriction buffer) is overwritten.
+  void fgmres_fixed(size_t l, T *b, T *x, int m) {
+    Level &L = *H.h[l];
+    LevelWork<T> &w = W.lw[l];
+    const i64 n = L.A.n, nk = n * k;
+    if (w.gW.n != nk || w.gV.n != (i64)(m + 1) * nk) {
+      w.gV.alloc((i64)(m + 1) * nk, s);
+      w.gZ.alloc((i64)m * nk, s);
+      w.gW.alloc(nk, s);
+      w.gH.alloc((i64)((m + 1) * m + m + 3) * k, s);
+    }
+    auto V = [&](int i) { return w.gV.p + (i64)i * nk; };
+    auto Z = [&](int i) { return w.gZ.p + (i64)i * nk; };
+    double *Hb = w.gH.p;  // H(i, j) at Hb[(i m + j) k + c]
+    auto Hs = [&](int i, int j) { return Hb + ((i64)i * m + j) * k; };
+    double *b2 = Hb + (i64)(m + 1) * m * k, *rcp = b2 + k, *sum = rcp + k, *y = sum + k;
+    const bool f64 = sizeof(T) == 8;
+    const double vb = (double)nk * sizeof(T);
+    MatView<T> A = viewA<T>(L, k, s);
+    auto project = [&](T *v) {  // v -= mean(v), per column
+      col_reduce<T>(n, k, Red::Sum, v, nullptr, sum, w.scratch.p, w.scratch_len, s);
+      sub_mean<T>(n, k, v, sum, s);
+    };
+    timed(H, (int)l, LIGMG_KERNEL_KRYLOV, k, f64, 5.0 * vb, [&] {
+      project(b);
+      col_reduce<T>(n, k, Red::Dot, b, b, b2, w.scratch.p, w.scratch_len, s);
+      rsqrt_cols(k, b2, rcp, s);
+      scale_cols<T>(n, k, V(0), b, rcp, s);
+    });
+    for (int j = 0; j < m; j++) {
+      cycle(l, V(j), Z(j));
+      timed(H, (int)l, LIGMG_KERNEL_KRYLOV, k, f64, 3.0 * vb, [&] { project(Z(j)); });
+      EpiArgs a;
+      a.y = w.gW.p;
+      timed(H, (int)l, LIGMG_KERNEL_SPMV, k, f64,
+            core_bytes(n, L.A.nnz, n, k, sizeof(T)) + vb,
+            [&] { spmm<T>(A, Z(j), k, Epi::Store, a, s); });
+      timed(H, (int)l, LIGMG_KERNEL_KRYLOV, k, f64, (5.0 * (j + 1) + 3) * vb, [&] {
+        for (int i = 0; i <= j; i++)
+          col_reduce<T>(n, k, Red::Dot, V(i), w.gW.p, Hs(i, j), w.scratch.p, w.scratch_len, s);
+        for (int i = 0; i <= j; i++) axpby_cols<T>(n, k, w.gW.p, V(i), Hs(i, j), -1.0, 1.0, s);
+        col_reduce<T>(n, k, Red::Dot, w.gW.p, w.gW.p, Hs(j + 1, j), w.scratch.p, w.scratch_len,
+                      s);
+        if (j + 1 < m) {
+          rsqrt_cols(k, Hs(j + 1, j), rcp, s);
+          scale_cols<T>(n, k, V(j + 1), w.gW.p, rcp, s);
+        }
+      });
+    }
+    timed(H, (int)l, LIGMG_KERNEL_KRYLOV, k, f64, (2.0 * m + 1) * vb, [&] {
+      gmres_small(k, m, Hb, b2, y, s);
+      LG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * nk, s));
+      for (int i = 0; i < m; i++) axpby_cols<T>(n, k, x, Z(i), y + (i64)i * k, 1.0, 1.0, s);
+    });
   }
 
   // The levels from `start` down as one persistent launch when that level
@@ -2690,7 +2757,10 @@ ligmg_status ligmg_create(int64_t n, const int64_t *rowptr, const int32_t *col,
     if (o.outer_ksp_type == LIGMG_KSP_FGMRES && o.gmres_restart < 1)
       return LIGMG_ERR_INVALID_ARGUMENT;
     if (o.smoother_type > LIGMG_SMOOTHER_CHEBYSHEV || o.outer_ksp_type > LIGMG_KSP_FGMRES ||
-        o.kcycle_ksp_type != LIGMG_KSP_FCG || o.elim_iters > 1 || o.aff_scaling < LIGMG_AFF_NONE || o.aff_scaling > LIGMG_AFF_MAX)
+        (o.kcycle_ksp_type != LIGMG_KSP_FCG && o.kcycle_ksp_type != LIGMG_KSP_FGMRES) ||
+        o.elim_iters > 1 || o.aff_scaling < LIGMG_AFF_NONE || o.aff_scaling > LIGMG_AFF_MAX)
+      return LIGMG_ERR_UNSUPPORTED;
+    if (o.kcycle_ksp_type == LIGMG_KSP_FGMRES && o.kcycle_iters > kGmresInnerMax)
       return LIGMG_ERR_UNSUPPORTED;
     H->device = o.device;
     LG_CUDA(cudaSetDevice(H->device));

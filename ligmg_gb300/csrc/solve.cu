@@ -301,6 +301,55 @@ __global__ void k_axpby(i64 n, int k, T *y, const T *x, const double *alpha, dou
 }
 
 template <typename T>
+__global__ void k_scale_cols(i64 n, int k, T *y, const T *x, const double *coef) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  y[t] = (T)((double)x[t] * coef[t % k]);
+}
+
+__global__ void k_rsqrt_cols(int k, const double *sq, double *out) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k) return;
+  const double v = sq[c];
+  out[c] = v > 0 ? 1.0 / sqrt(v) : 0.0;
+}
+
+// One thread per column: Givens rotations of the (m + 1) x m Hessenberg
+// matrix column by column, then back substitution of the rotated triangle
+// (the arithmetic of the outer FGMRES, all steps at once).
+__global__ void k_gmres_small(int k, int m, const double *Hb, const double *b2, double *y) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k) return;
+  double R[kGmresInnerMax + 1][kGmresInnerMax], cs[kGmresInnerMax], sn[kGmresInnerMax],
+      g[kGmresInnerMax + 1], yv[kGmresInnerMax];
+  for (int i = 0; i <= m; i++) g[i] = 0.0;
+  g[0] = sqrt(fmax(b2[c], 0.0));
+  for (int j = 0; j < m; j++) {
+    for (int i = 0; i <= j; i++) R[i][j] = Hb[((i64)i * m + j) * k + c];
+    R[j + 1][j] = sqrt(fmax(Hb[((i64)(j + 1) * m + j) * k + c], 0.0));
+    for (int i = 0; i < j; i++) {
+      const double a = R[i][j], b = R[i + 1][j];
+      R[i][j] = cs[i] * a + sn[i] * b;
+      R[i + 1][j] = -sn[i] * a + cs[i] * b;
+    }
+    const double a = R[j][j], b = R[j + 1][j];
+    const double rho = sqrt(a * a + b * b);
+    cs[j] = rho > 0 ? a / rho : 1.0;
+    sn[j] = rho > 0 ? b / rho : 0.0;
+    R[j][j] = rho;
+    R[j + 1][j] = 0.0;
+    g[j + 1] = -sn[j] * g[j];
+    g[j] = cs[j] * g[j];
+  }
+  for (int i = m - 1; i >= 0; i--) {
+    double t = g[i];
+    for (int l = i + 1; l < m; l++) t -= R[i][l] * yv[l];
+    yv[i] = R[i][i] != 0 ? t / R[i][i] : 0.0;
+  }
+  for (int i = 0; i < m; i++) y[(i64)i * k + c] = yv[i];
+}
+
+template <typename T>
 __global__ void k_fcg_direction(i64 n, int k, T *p, const T *z, const T *pp, const double *beta) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
@@ -1006,6 +1055,20 @@ void axpby_cols(i64 n, int k, T *y, const T *x, const double *alpha, double sa, 
   LG_LAUNCH();
 }
 template <typename T>
+void scale_cols(i64 n, int k, T *y, const T *x, const double *coef, cudaStream_t s) {
+  k_scale_cols<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, y, x, coef);
+  LG_LAUNCH();
+}
+void rsqrt_cols(int k, const double *sq, double *out, cudaStream_t s) {
+  k_rsqrt_cols<<<1, 64 * cdiv(k, 64), 0, s>>>(k, sq, out);
+  LG_LAUNCH();
+}
+void gmres_small(int k, int m, const double *Hb, const double *b2, double *y, cudaStream_t s) {
+  if (m < 1 || m > kGmresInnerMax) throw Error(LIGMG_ERR_INVALID_ARGUMENT, "inner FGMRES steps");
+  k_gmres_small<<<1, 64 * cdiv(k, 64), 0, s>>>(k, m, Hb, b2, y);
+  LG_LAUNCH();
+}
+template <typename T>
 void fcg_direction(i64 n, int k, T *p, const T *z, const T *pprev, const double *beta,
                    cudaStream_t s) {
   k_fcg_direction<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, p, z, pprev, beta);
@@ -1055,7 +1118,8 @@ void scal_beta(int k, const double *zq, const double *eta_prev, double *beta, cu
                                  cudaStream_t);                                                \
   template void fcg_update<T>(i64, int, T *, T *, const T *, const T *, const double *, bool, \
                               cudaStream_t, const float *);                                    \
-  template void cg_direction<T>(i64, int, T *, const T *, const double *, cudaStream_t);
+  template void cg_direction<T>(i64, int, T *, const T *, const double *, cudaStream_t);    \
+  template void scale_cols<T>(i64, int, T *, const T *, const double *, cudaStream_t);
 LG_INST(float)
 LG_INST(double)
 template void convert<double, float>(i64, const double *, float *, cudaStream_t);

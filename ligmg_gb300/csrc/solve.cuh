@@ -136,6 +136,16 @@ void sub_mean(i64 n, int k, T *x, const double *colsum, cudaStream_t s);   // x 
 template <typename T>
 void axpby_cols(i64 n, int k, T *y, const T *x, const double *alpha, double sa, double sb,
                 cudaStream_t s);  // y = sb*y + sa*alpha[c]*x
+// y = coef[c] x (y and x may not overlap)
+template <typename T>
+void scale_cols(i64 n, int k, T *y, const T *x, const double *coef, cudaStream_t s);
+// out[c] = 1 / sqrt(sq[c]), 0 where sq[c] <= 0 (k <= 64 per launch block)
+void rsqrt_cols(int k, const double *sq, double *out, cudaStream_t s);
+// Inner FGMRES least squares for k columns: H(i, j) at Hb[(i m + j) k + c]
+// (i <= j: Arnoldi dot products; i = j + 1: the squared norm), b2 = |b|^2;
+// y (m x k) minimises |b| e1 - H y.  m <= kGmresInnerMax.
+constexpr int kGmresInnerMax = 16;
+void gmres_small(int k, int m, const double *Hb, const double *b2, double *y, cudaStream_t s);
 template <typename T>
 void fcg_direction(i64 n, int k, T *p, const T *z, const T *pprev, const double *beta,
                    cudaStream_t s);  // p = z - beta p_prev (pprev null: p = z)

@@ -926,7 +926,71 @@ struct orc_hier {
       return;
     }
     // petsc_fcg with kcycle_iters iterations on h[l+1], x0 = 0 (:115-126)
-    krylov_fixed(l + 1, xc, bc, opts.kcycle_iters);
+    if (opts.kcycle_ksp_type == LIGMG_KSP_FGMRES) fgmres_fixed(l + 1, xc, bc, opts.kcycle_iters);
+    else krylov_fixed(l + 1, xc, bc, opts.kcycle_iters);
+  }
+
+  // fixed-iteration FGMRES (K-cycle inner solve with kcycle_ksp_type fgmres,
+  // parse_options.hpp:399-400): exactly m Arnoldi steps from x = 0 (PETSc's
+  // restart length, 30, exceeds the K-cycle's iteration count), the outer
+  // FGMRES's arithmetic otherwise: b's constant projected out, right
+  // preconditioning with kcycle(l) (constant projected out), classical
+  // Gram-Schmidt, Givens rotations, back substitution; normalisations multiply
+  // by the reciprocal norm.
+  void fgmres_fixed(size_t l, std::vector<double> &x, const std::vector<double> &b0, int m) {
+    const Csr &A = h[l].A;
+    const i64 n = A.n;
+    x.assign(n, 0.0);
+    std::vector<double> b = b0;
+    remove_mean(b);
+    const double b2 = dot(b, b);
+    auto rsq = [](double v) { return v > 0 ? 1.0 / std::sqrt(v) : 0.0; };
+    std::vector<std::vector<double>> V(m + 1, std::vector<double>(n)), Z(m);
+    std::vector<double> w, H2((size_t)(m + 1) * m, 0.0);  // dots; (j + 1, j): squared norm
+    auto Hij = [&](int i, int j) -> double & { return H2[(size_t)i * m + j]; };
+    const double r0 = rsq(b2);
+    for (i64 t = 0; t < n; t++) V[0][t] = b[t] * r0;
+    for (int j = 0; j < m; j++) {
+      cycle(l, Z[j], V[j]);
+      remove_mean(Z[j]);
+      spmv(A, Z[j], w);
+      for (int i = 0; i <= j; i++) Hij(i, j) = dot(V[i], w);
+      for (int i = 0; i <= j; i++)
+        for (i64 t = 0; t < n; t++) w[t] -= Hij(i, j) * V[i][t];
+      Hij(j + 1, j) = dot(w, w);
+      if (j + 1 < m) {
+        const double rj = rsq(Hij(j + 1, j));
+        for (i64 t = 0; t < n; t++) V[j + 1][t] = w[t] * rj;
+      }
+    }
+    // Hessenberg least squares: Givens column by column, then the triangle
+    std::vector<double> R((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0), y(m);
+    auto Rij = [&](int i, int j) -> double & { return R[(size_t)i * m + j]; };
+    g[0] = std::sqrt(std::max(b2, 0.0));
+    for (int j = 0; j < m; j++) {
+      for (int i = 0; i <= j; i++) Rij(i, j) = Hij(i, j);
+      Rij(j + 1, j) = std::sqrt(std::max(Hij(j + 1, j), 0.0));
+      for (int i = 0; i < j; i++) {
+        const double a = Rij(i, j), c = Rij(i + 1, j);
+        Rij(i, j) = cs[i] * a + sn[i] * c;
+        Rij(i + 1, j) = -sn[i] * a + cs[i] * c;
+      }
+      const double a = Rij(j, j), c = Rij(j + 1, j);
+      const double rho = std::sqrt(a * a + c * c);
+      cs[j] = rho > 0 ? a / rho : 1.0;
+      sn[j] = rho > 0 ? c / rho : 0.0;
+      Rij(j, j) = rho;
+      Rij(j + 1, j) = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+    }
+    for (int i = m - 1; i >= 0; i--) {
+      double t = g[i];
+      for (int q = i + 1; q < m; q++) t -= Rij(i, q) * y[q];
+      y[i] = Rij(i, i) != 0 ? t / Rij(i, i) : 0.0;
+    }
+    for (int i = 0; i < m; i++)
+      for (i64 t = 0; t < n; t++) x[t] += y[i] * Z[i][t];
   }
 
   // fixed-iteration FCG (K-cycle inner solve), preconditioner = kcycle(l)

@@ -333,6 +333,40 @@ def test_pcg_jacobi_baseline():
     assert mg.iters() < info.iters()  # multigrid needs far fewer iterations
 
 
+@pytest.mark.parametrize("name", ["grid48_logn", "rmat12"])
+def test_kcycle_fgmres_cycle_matches_oracle(name):
+    # K-cycle inner solves by FGMRES (--kcycle-ksp-type fgmres): the FP64 cycle
+    # of every level against the oracle
+    L = GRAPHS[name]()
+    kw = dict(kcycle=1, kcycle_ksp_type="fgmres")
+    S, R = Solver(L, **kw), O.OracleSolver(L, **kw)
+    rng = np.random.default_rng(8)
+    for level in range(R.num_levels):
+        b = _proj(rng.standard_normal(R.level_info(level)["n"]))
+        xg, xr = S.cycle(level, b), R.cycle(level, b)
+        assert _relerr(xg, xr) <= 1e-12, (level, _relerr(xg, xr))
+
+
+@pytest.mark.parametrize("prec,k", [("fp64", 1), ("fp32", 8)])
+def test_kcycle_fgmres_solve_matches_oracle(prec, k):
+    L = GRAPHS["rmat12"]()
+    kw = dict(kcycle=1, kcycle_ksp_type="fgmres", outer_ksp_type="fcg")
+    S = Solver(L, precision=prec, **kw)
+    R = O.OracleSolver(L, **kw)
+    B = G.rhs(L.n, k=k, seed=13)
+    if k == 1:
+        B = B.reshape(L.n, 1)
+    info = S.solve_batched(B)
+    assert info.converged and (info.col_true_rel_residual <= 2e-8).all()
+    S2 = S.solve_batched(B)  # replayed from the captured graphs: identical
+    assert np.array_equal(info.solution, S2.solution)
+    for c in (0, k - 1):
+        xr, ir = R.solve(B[:, c].copy())
+        assert ir["status"] == 0
+        assert abs(int(info.col_iters[c]) - ir["iters"]) <= 1
+        assert _relerr(info.solution[:, c], xr) <= 1e-6
+
+
 @pytest.mark.parametrize("prec,k,restart", [("fp64", 1, 30), ("fp32", 8, 30), ("fp64", 1, 3)])
 def test_fgmres_outer_matches_oracle(prec, k, restart):
     # FGMRES(m) outer iterations (the reference's --outer-ksp-type fgmres)

@@ -219,6 +219,24 @@ def test_prepare_graph_tie_takes_smaller_label():
     assert list(orig) == [0, 2, 4] and len(rp) == 4 and len(ci) == 4
 
 
+@pytest.mark.parametrize("iters", [2, 3])
+def test_oracle_kcycle_fgmres_matches_dense_solution(iters):
+    # K-cycle inner solves by FGMRES (the reference's --kcycle-ksp-type fgmres)
+    L = G.grid2d(24, weights="lognormal", seed=4)
+    b = G.rhs(L.n, seed=6)
+    S = O.OracleSolver(L, kcycle=1, kcycle_ksp_type="fgmres", kcycle_iters=iters,
+                       outer_ksp_type="fcg")
+    x, info = S.solve(b)
+    assert info["status"] == 0 and info["true_rel_residual"] <= 1e-8
+    xd = np.linalg.lstsq(L.to_scipy().toarray(), b, rcond=None)[0]
+    xd -= xd.mean()
+    x = x - x.mean()
+    assert np.linalg.norm(x - xd) <= 1e-6 * np.linalg.norm(xd)
+    F = O.OracleSolver(L, kcycle=1, kcycle_iters=iters, outer_ksp_type="fcg")
+    _, fi = F.solve(b)
+    assert abs(info["iters"] - fi["iters"]) <= 3  # same K-cycle, another inner Krylov method
+
+
 @pytest.mark.parametrize("restart", [30, 3])
 def test_oracle_fgmres_matches_dense_solution(restart):
     L = G.grid2d(24, weights="lognormal", seed=4)
