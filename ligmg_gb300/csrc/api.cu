@@ -1624,12 +1624,13 @@ struct Engine {
     LevelWork<T> &w = W.lw[l];
     i64 n = L.A.n;
     MatView<T> A = viewA<T>(L, k, s);
-    timed(H, (int)l, LIGMG_KERNEL_VECTOR, k, sizeof(T) == 8, 1.0 * n * k * sizeof(T),
-          [&] { LG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * n * k, s)); });
     T *r = b;
     T *p = w.fp0.p, *pp = w.fp1.p, *q = w.fq0.p, *qp = w.fq1.p;
     const SegInfo S = L.seginfo();
     const bool seg = S.nseg > 0;
+    if (seg)  // x = 0 (otherwise the first update writes x = alpha p)
+      timed(H, (int)l, LIGMG_KERNEL_VECTOR, k, sizeof(T) == 8, 1.0 * n * k * sizeof(T),
+            [&] { LG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * n * k, s)); });
     FcgScalars sc{w.slot(S_SUM, k), w.slot(S_BETA, k), w.slot(S_ETA0, k), w.slot(S_ETA1, k),
                   w.slot(S_ALPHA, k), nullptr};
     if constexpr (sizeof(T) == 4) {
@@ -1685,7 +1686,7 @@ struct Engine {
                 seg_fcg_update<T>(S, n, x, r, p, q, sc.alpha, it + 1 < iters, s);
               } else {
                 fcg_alpha<T>(n, k, p, q, r, sc, w.fscratch.p, s);
-                fcg_update<T>(n, k, x, r, p, q, sc.alpha, it + 1 < iters, s, sc.alpha_f);
+                fcg_update<T>(n, k, x, r, p, q, sc.alpha, it + 1 < iters, s, sc.alpha_f, it == 0);
               }
             });
       std::swap(p, pp);

@@ -369,11 +369,11 @@ __device__ __forceinline__ T col_scalar(const double *d, const float *f, int c) 
 
 template <typename T>
 __global__ void k_fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, const double *alpha,
-                             const float *alpha_f, int upd_r) {
+                             const float *alpha_f, int upd_r, int x_zero) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
   const T a = col_scalar<T>(alpha, alpha_f, (int)(t % k));
-  x[t] = x[t] + a * p[t];
+  x[t] = x_zero ? a * p[t] : x[t] + a * p[t];
   if (upd_r) r[t] = r[t] - a * q[t];
 }
 
@@ -1076,9 +1076,9 @@ void fcg_direction(i64 n, int k, T *p, const T *z, const T *pprev, const double 
 }
 template <typename T>
 void fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, const double *alpha,
-                bool update_r, cudaStream_t s, const float *alpha_f) {
+                bool update_r, cudaStream_t s, const float *alpha_f, bool x_zero) {
   k_fcg_update<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, x, r, p, q, alpha, alpha_f,
-                                                       update_r ? 1 : 0);
+                                                       update_r ? 1 : 0, x_zero ? 1 : 0);
   LG_LAUNCH();
 }
 template <typename T>
@@ -1117,7 +1117,7 @@ void scal_beta(int k, const double *zq, const double *eta_prev, double *beta, cu
   template void fcg_direction<T>(i64, int, T *, const T *, const T *, const double *,        \
                                  cudaStream_t);                                                \
   template void fcg_update<T>(i64, int, T *, T *, const T *, const T *, const double *, bool, \
-                              cudaStream_t, const float *);                                    \
+                              cudaStream_t, const float *, bool);                              \
   template void cg_direction<T>(i64, int, T *, const T *, const double *, cudaStream_t);    \
   template void scale_cols<T>(i64, int, T *, const T *, const double *, cudaStream_t);
 LG_INST(float)

@@ -151,8 +151,8 @@ void fcg_direction(i64 n, int k, T *p, const T *z, const T *pprev, const double 
                    cudaStream_t s);  // p = z - beta p_prev (pprev null: p = z)
 template <typename T>
 void fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, const double *alpha,
-                bool update_r, cudaStream_t s,
-                const float *alpha_f = nullptr);  // x += a p; r -= a q (a: alpha_f if set)
+                bool update_r, cudaStream_t s, const float *alpha_f = nullptr,
+                bool x_zero = false);  // x += a p (x_zero: x = a p); r -= a q (a: alpha_f if set)
 template <typename T>
 void cg_direction(i64 n, int k, T *p, const T *z, const double *beta, cudaStream_t s);  // p = z + beta p
 
