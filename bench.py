@@ -90,6 +90,16 @@ def dist_info():
     return ws, rank, local
 
 
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum from one
+# single-pass ncu capture of every ChebZ and ChebB SpMM launch of one timed step
+# of the default workload: R-MAT scale 20, k = 32, FP32 hierarchy), averaged per
+# level over that level's launches of both kernels; the profile's `cheb_b` entries
+# group exactly those launches.  Used for roofline.traffic when the dominant
+# entry is one of them.
+CHEB_DRAM_BYTES_RMAT20_K32 = {1: 477.93e6, 2: 294.15e6, 3: 149.99e6, 4: 61.67e6,
+                              6: 12.86e6, 8: 1.62e6}
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -379,8 +389,14 @@ def run_ours(args):
         per_launch_bytes = top["bytes"] / top["launches"]
         per_launch_s = top["seconds"] / top["launches"]
         ach = per_launch_bytes / per_launch_s / 1e9
+        traffic, traffic_src = None, None
+        if (args.workload == "rmat20" and args.scale == 20 and k == 32 and not top["fp64"]
+                and top["kind"] == "cheb_b" and top["level"] in CHEB_DRAM_BYTES_RMAT20_K32):
+            traffic = CHEB_DRAM_BYTES_RMAT20_K32[top["level"]]
+            traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
+                           "mean over the level's ChebZ and ChebB launches of one step")
         roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "traffic": None, "peak_source": peak_kind,
+                "traffic": traffic, "traffic_source": traffic_src, "peak_source": peak_kind,
                 "kernel": f"spmm_{top['kind']} level {top['level']} k={top['k']} "
                           f"{'fp64' if top['fp64'] else 'fp32'}",
                 "bytes_per_launch": per_launch_bytes, "us_per_launch": per_launch_s * 1e6,
