@@ -206,11 +206,12 @@ __global__ void k_convert(i64 cnt, const S *src, D *dst) {
 
 // column reductions.  Thread t of a BS-thread block takes column t % k and
 // rows t / k, t / k + BS / k, ... (four rows per pass, loads issued first).
-// Large inputs (>= 2^20 elements): one 1024-thread block per SM at most, so
-// few block partials remain for the final pass; smaller inputs: 256-thread
-// blocks (shorter trees, more blocks).
+// Inputs of 2^17 elements or more: one 1024-thread block per SM at most, so
+// few block partials remain for the ticketed last block (with 256-thread
+// blocks a 561k-element reduction left it 34 partials per thread); smaller
+// inputs: 256-thread blocks (shorter trees, more blocks).
 constexpr int kRedBS = 1024;
-constexpr i64 kRedBig = i64(1) << 20;
+constexpr i64 kRedBig = i64(1) << 17;
 template <typename T, int OP, int BS>
 __global__ void __launch_bounds__(BS) k_colred(i64 n, int k, const T *x, const T *y,
                                                 i64 rows_per_block, double *part) {
