@@ -7,8 +7,9 @@ solved as one n x k row-major block through the C ABI
 solve of k RHS to rtol 1e-8.  `e2e` repeats the measurement through the host
 entry point ligmg_solve_batched (pinned host buffers; H2D of B and D2H of X
 inside the timed region).  The plain FP64 single-RHS GPU solve is measured
-next to it (spec comparison) and the CPU oracle (the restated reference
-algorithm, all host cores) gives cpu_baseline.
+next to it (the per-RHS comparison of the FP32 batched solve against plain
+FP64) and the CPU oracle (the restated reference algorithm, all host cores)
+gives cpu_baseline.
 
 --impl reference: the reference (CombBLAS/PETSc/MPI) cannot be built on this
 image, so this arm times the CPU restatement of its algorithm (oracle/),
@@ -331,7 +332,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
     log(f"e2e {e2e_ms:.2f} ms")
-    # ---- plain FP64 single-RHS GPU solve (spec comparison) ------------------
+    # ---- plain FP64 single-RHS GPU solve (per-RHS comparison) ----------------------
     fp64 = {}
     if not args.no_fp64:
         t0 = time.perf_counter()
@@ -482,7 +483,7 @@ def _timed_solves(S, stream, Bd, k, steps, warmup):
 
 
 def run_grid3d(args):
-    """configs[2]: k right-hand sides as an n x k block, k in {1, 8, 32, 64}."""
+    """3-D grid Laplacian: k right-hand sides as an n x k block, k in {1, 8, 32, 64}."""
     import torch
     from ligmg_gb300 import Solver
     from ligmg_gb300 import build as Bld
@@ -518,7 +519,7 @@ def run_grid3d(args):
 
 
 def run_rgg_batch(args):
-    """configs[3]: 256 random geometric graphs (n log-uniform in [1e4, 2e5])
+    """Batch of 256 random geometric graphs (n log-uniform in [1e4, 2e5])
     solved together from one captured CUDA graph."""
     from ligmg_gb300 import BatchSolver, Solver
     from ligmg_gb300 import build as Bld

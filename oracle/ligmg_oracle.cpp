@@ -2,7 +2,8 @@
 // (setup + solve) at single-rank semantics.
 //
 // TEST INFRASTRUCTURE ONLY.  tests/, __graft_entry__.smoke() and bench.py's
-// CPU-baseline leg use it as the checker; the product library never does.
+// CPU-baseline leg use it to check or time against; the product library never
+// does.
 //
 // Parity status: UNPINNED against the reference.  The reference (ligmg,
 // header-only C++ over CombBLAS + PETSc + MPI) cannot be built here: MPI,

@@ -3,8 +3,8 @@
  *
  * The oracle is a plain C++ restatement of LigMG's hot path at single-rank
  * semantics.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline leg load it, and only as the checker.  The product library
- * (ligmg_gb300/) never links or calls it.
+ * baseline leg load it, and only to check or time against.  The product
+ * library (ligmg_gb300/) never links or calls it.
  */
 #ifndef LIGMG_ORACLE_H
 #define LIGMG_ORACLE_H

@@ -290,7 +290,7 @@ def test_unsupported_k_rejected():
 
 @pytest.mark.parametrize("name", ["my_matrix", "rmat12"])
 def test_cycle_on_imported_oracle_hierarchy(name, tmp_path):
-    """The spec check on an exported hierarchy: import the oracle's
+    """Parity on an exported hierarchy: import the oracle's
     hierarchy (written to PETSc binary and read back) and compare one FP64
     cycle and a full solve with the oracle's."""
     from ligmg_gb300 import petsc_io
