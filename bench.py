@@ -332,6 +332,27 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
     log(f"e2e {e2e_ms:.2f} ms")
+    # ---- FP32-hierarchy single-RHS solve on the same handle (one zero-mean RHS,
+    # the unbatched form of the same solve) -------------------------------------------
+    fp32s = {}
+    if not args.no_fp64:
+        b1 = torch.from_numpy(G.rhs(n, k=1, seed=rng_seed)).to(dev).reshape(n, 1).contiguous()
+        x1 = torch.empty((n, 1), dtype=torch.float64, device=dev)
+        for _ in range(max(args.warmup, 1)):  # the first k = 1 solve also tunes its plans
+            S.solve_batched_device(b1.data_ptr(), 1, x1.data_ptr())
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        nrep = 3
+        it32 = []
+        for _ in range(nrep):
+            inf = S.solve_batched_device(b1.data_ptr(), 1, x1.data_ptr())
+            it32.append(inf.iters())
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fp32s = {"ms_per_rhs": f0.elapsed_time(f1) / nrep, "iters": it32,
+                 "true_rel_residual": inf.true_rel_residual}
+        log(f"fp32 single {fp32s['ms_per_rhs']:.2f} ms/RHS")
     # ---- plain FP64 single-RHS GPU solve (per-RHS comparison) ----------------------
     fp64 = {}
     if not args.no_fp64:
@@ -430,6 +451,9 @@ def run_ours(args):
             "l2": "hierarchy (>= 300 MB FP32+FP64 matrices) larger than the 129 MB L2",
             "fp64_single_rhs": fp64,
             "speedup_vs_fp64_single": (fp64.get("ms_per_rhs", 0) / value) if fp64 else None,
+            "fp32_single_rhs": fp32s,
+            "speedup_fp32_single_vs_fp64_single": (fp64["ms_per_rhs"] / fp32s["ms_per_rhs"])
+            if (fp64 and fp32s) else None,
             "top_kernels": [{**r, "gbs": r["bytes"] / r["seconds"] / 1e9}
                             for r in sorted(stats, key=lambda r: -r["seconds"])[:8]],
             "profile_ms_per_step_by_level": by_key(stats, "level", args.steps),
