@@ -19,7 +19,7 @@
  *   ligmg_spmv             <- SpMV_inplace (MatShell MATOP_MULT)  util.hpp:451-476
  *   ligmg_status_string    <- PETSC_CHECK_ERROR message   util.hpp:653-660
  * The PETSc plugin PCCreate_LIGMG (petsc_shim.hpp:64-74) is a thin client of
- * ligmg_create / ligmg_solve; its source is shown in INTEGRATION.md.
+ * ligmg_create / ligmg_solve.
  *
  * Rules:
  *   - status 0 (LIGMG_OK) is success; LIGMG_NOT_CONVERGED is a soft status
@@ -345,10 +345,10 @@ ligmg_status ligmg_backward(ligmg_handle h, const double *g, double *dw,
 
 /* y = A x with the level's FP64 matrix, device pointers, allocating nothing.
  * This entry point has no counterpart in the reference.  It exists for
- * callers that cannot allocate device memory at the point of the call: code
- * recording a CUDA graph (an allocation during stream capture invalidates
- * the capture) and applications whose memory is owned by their own pool
- * allocator.  ligmg_spmv allocates temporary buffers on every call; this
+ * callers that cannot allocate device memory at the point of the call, such
+ * as applications whose device memory is owned by their own pool allocator
+ * or that run inside a region where a cudaMalloc would synchronise the
+ * device.  ligmg_spmv allocates temporary buffers on every call; this
  * variant reads dx[n] and writes dy[n] (caller-owned) and keeps the
  * split-row partial sums of power-law hub rows in a fixed static device
  * array: at most 65536 row chunks and 16384 split rows per level (512 KiB +

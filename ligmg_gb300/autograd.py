@@ -8,6 +8,10 @@ edges: (u, v) int arrays with u != v, each undirected edge once.  x is the
 mean-free solution; gradients flow to w (dloss/dw_e = -(x_u - x_v)(lam_u - lam_v))
 and to b (the mean-free adjoint solution).  The solve itself runs in
 libligmg_gb300 on the GPU; torch only carries the tensors.
+
+A forward or adjoint solve that stops at the iteration limit
+(LIGMG_NOT_CONVERGED) raises NotConvergedError: its x or its gradients would
+be wrong, so neither is returned.
 """
 import numpy as np
 
@@ -20,6 +24,10 @@ except ImportError:  # pragma: no cover
     torch = None
 
 
+class NotConvergedError(RuntimeError):
+    """A solve inside LaplacianSolve reached the iteration limit."""
+
+
 def edge_positions(L, u, v):
     """CSR position of entry (u[e], v[e]) for every edge."""
     rp, ci = L.rowptr, L.col
@@ -30,6 +38,15 @@ def edge_positions(L, u, v):
     return pos
 
 
+def require_converged(info, what):
+    """Raise NotConvergedError unless `info` (a ConvergenceInfo) converged."""
+    if not info.converged:
+        raise NotConvergedError(
+            f"{what} stopped after {info.iters()} iterations without reaching the tolerance "
+            f"(true relative residual {info.true_rel_residual:.3e})")
+    return info
+
+
 if torch is not None:
     class LaplacianSolve(torch.autograd.Function):
         @staticmethod
@@ -38,7 +55,7 @@ if torch is not None:
             n = b.shape[0]
             L = G.laplacian_from_edges(n, u, v, w.detach().cpu().numpy())
             S = Solver(L, options) if options is not None else Solver(L)
-            info = S.forward(b.detach().cpu().numpy())
+            info = require_converged(S.forward(b.detach().cpu().numpy()), "forward solve")
             x = info.solution - info.solution.mean()
             ctx.solver = S
             ctx.pos = edge_positions(L, np.asarray(u), np.asarray(v))
@@ -48,7 +65,8 @@ if torch is not None:
         def backward(ctx, gx):
             g = gx.detach().cpu().numpy().astype(np.float64)
             g = g - g.mean()  # x is mean-free: only the mean-free part of g matters
-            dw, db = ctx.solver.backward(g)
+            dw, db, info = ctx.solver.backward(g, with_info=True)
+            require_converged(info, "adjoint solve")
             gw = torch.from_numpy(dw[ctx.pos].copy()).to(gx.device)
             gb = torch.from_numpy(db).to(gx.device)
             return gw, gb, None, None

@@ -3345,7 +3345,8 @@ extern "C" ligmg_status ligmg_spmv_device_noalloc(ligmg_handle h, int32_t level,
     MatView<double> A = viewA<double>(L, 1, h->s);
     A.partial = (double *)base;
     A.hub_counter = (int *)(base + kNoallocCounterOffset);
-    // the counters must start at zero; the array keeps the previous call's state
+    // the split-row kernel resets each counter when a row completes; zeroing
+    // them here only guards against a previous call that stopped part-way
     if (L.hubA64.nhubs > 0)
       LG_CUDA(cudaMemsetAsync(A.hub_counter, 0, sizeof(int) * L.hubA64.nhubs, h->s));
     EpiArgs a;

@@ -282,17 +282,25 @@ class Solver:
                                info.work, x, info.true_rel_residual, st == 0, ci, ct,
                                info.cycle_complexity)
 
-    def backward(self, g):
+    def backward(self, g, with_info=False):
         """Adjoint of the kept forward solve (ligmg_backward): returns (dw, db)
         with dw per stored CSR entry of the input matrix (the edge-weight
-        derivative on off-diagonal entries, 0 on the diagonal) and db = dloss/db."""
+        derivative on off-diagonal entries, 0 on the diagonal) and db = dloss/db.
+        with_info=True also returns the adjoint solve's ConvergenceInfo (its
+        `converged` is False when the adjoint solve stopped at the iteration
+        limit, LIGMG_NOT_CONVERGED)."""
         g = np.ascontiguousarray(g, dtype=np.float64)
         dw = np.empty(len(self._ci))
         db = np.empty(self.n)
         info, hist, ci, ct = self._info(1)
-        check(lib().ligmg_backward(self._h, _p(g), _p(dw), _p(db), C.byref(info)),
-              "ligmg_backward")
-        return dw, db
+        st = check(lib().ligmg_backward(self._h, _p(g), _p(dw), _p(db), C.byref(info)),
+                   "ligmg_backward")
+        if not with_info:
+            return dw, db
+        return dw, db, ConvergenceInfo(hist[: info.history_len].copy(), info.iters,
+                                       info.solve_seconds, info.work, None,
+                                       info.true_rel_residual, st == 0, ci, ct,
+                                       info.cycle_complexity)
 
     # ---- measurement ---------------------------------------------------------
     def profile(self, enable=True):

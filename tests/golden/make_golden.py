@@ -10,7 +10,9 @@
    level's ids and matrix values).  It pins the oracle against itself across
    builds and hosts (x86_64 here, aarch64 on the GPU host).
 
-Run: python tests/golden/make_golden.py
+Run: python tests/golden/make_golden.py [path/to/reference/checkout]
+(the checkout defaults to $LIGMG_REFERENCE; the fixture is its
+examples/my_matrix.mtx)
 """
 import hashlib
 import os
@@ -21,7 +23,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-REF_MTX = "/root/reference/examples/my_matrix.mtx"
+REF_ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LIGMG_REFERENCE", "")
+REF_MTX = os.path.join(REF_ROOT, "examples", "my_matrix.mtx") if REF_ROOT else ""
 
 
 def digest(*arrays):
@@ -33,7 +36,7 @@ def digest(*arrays):
 
 def make_edges():
     out = os.path.join(HERE, "my_matrix_edges.npz")
-    if not os.path.exists(REF_MTX):
+    if not REF_MTX or not os.path.exists(REF_MTX):
         if os.path.exists(out):
             return
         raise SystemExit("reference fixture not available")

@@ -37,21 +37,25 @@ def _free_port():
     return p
 
 
+NGRAPHS, NBLOCKS = 5, 6
+
+
 def _worker(rank, world, port, out):
     import torch.distributed as dist
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     from ligmg_gb300 import graphs as G
-    from ligmg_gb300.replicas import block_range, lpt_partition, reduce_max, reduce_sum
+    from ligmg_gb300.replicas import lpt_partition, reduce_max, reduce_sum
     from oracle import oracle as O
     O.set_threads(1)
-    gs = [G.grid2d(12 + 3 * i, weights="lognormal", seed=i) for i in range(5)]
+    gs = [G.grid2d(12 + 3 * i, weights="lognormal", seed=i) for i in range(NGRAPHS)]
+    # graphs are the unit split across ranks; every rank solves all RHS
+    # blocks of the graphs it owns
     mine = lpt_partition([g.nnz for g in gs], world)[rank]
     res = {}
     for gi in mine:
         S = O.OracleSolver(gs[gi], kcycle=1, outer_ksp_type="fcg")
-        lo, hi = block_range(6, world, rank)  # RHS blocks of this rank
-        for c in range(lo, hi):
+        for c in range(NBLOCKS):
             x, info = S.solve(G.rhs(gs[gi].n, seed=100 * gi + c))
             res[(gi, c)] = (info["iters"], float(info["true_rel_residual"]))
     tmax = reduce_max([float(rank + 1)])
@@ -69,9 +73,11 @@ def test_two_rank_replicas_gloo():
     for r in range(world):
         res, tmax, cnt = out[r]
         assert tmax == 2.0  # max over ranks
+        assert not (set(res) & set(allres))  # no pair solved by two ranks
         allres.update(res)
-    # every (graph, rhs-block) pair of this rank's graphs was solved once
-    assert out[0][2] == out[1][2] == float(len(out[0][0]) + len(out[1][0]))
+    # every (graph, rhs-block) pair was solved, by exactly one rank
+    assert set(allres) == {(g, c) for g in range(NGRAPHS) for c in range(NBLOCKS)}
+    assert out[0][2] == out[1][2] == float(NGRAPHS * NBLOCKS)
     for (gi, c), (iters, tr) in allres.items():
         assert iters > 0 and tr < 1e-7
     # graphs were split between the two ranks

@@ -1,5 +1,6 @@
 """ligmg_spmv_device_noalloc: the level SpMV for callers that cannot allocate
-device memory at the call (stream capture, external pool allocators).
+device memory at the call (applications whose device memory belongs to their
+own pool allocator).
 
 It must give the same y = A x as the allocating entry point ligmg_spmv, on
 two calls in a row (the second call finds the shared scratch array holding
