@@ -144,6 +144,17 @@ typedef struct ligmg_options {
                                  has at most this many rows; < 0: every level
                                  launches its own kernels */
   int32_t gmres_restart;      /* FGMRES restart length (30, PETSc's default) */
+  int32_t spmv_tiles;         /* 1 (default): single right-hand-side products
+                                 of matrices averaging at least six entries
+                                 per row use the nonzero-balanced tile layout
+                                 (a warp per tile of whole rows, a lane per 16
+                                 consecutive entries); 0: one group of lanes
+                                 per row */
+  int64_t wait_spins;         /* polls of an incomplete barrier before a
+                                 device-side wait on other CTAs (the grid-mode
+                                 tail kernel's barriers) gives up; the kernel
+                                 then stops and the call returns
+                                 LIGMG_ERR_INTERNAL.  0: the default (2^23) */
 } ligmg_options;
 
 /* ConvergenceInfo (util.hpp:143-170) of one solve.  For a batched solve the

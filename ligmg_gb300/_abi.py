@@ -77,6 +77,8 @@ class Options(C.Structure):
         ("autotune", C.c_int32),
         ("tail_rows", C.c_int64),
         ("gmres_restart", C.c_int32),
+        ("spmv_tiles", C.c_int32),
+        ("wait_spins", C.c_int64),
     ]
 
 
@@ -143,6 +145,8 @@ def default_options(**overrides) -> Options:
     o.autotune = 1
     o.tail_rows = 0
     o.gmres_restart = 30
+    o.spmv_tiles = 1
+    o.wait_spins = 0
     for k, v in overrides.items():
         if k in ("smoother_type",) and isinstance(v, str):
             v = SMOOTHER[v]

@@ -781,6 +781,14 @@ Work<T> &work_for(Handle &H, int k) {
   return W;
 }
 
+// Zeroed barrier state carrying the handle's wait limit (options.wait_spins).
+inline void tail_sync_reset(Handle &H, DBuf<TailSync> &sync) {
+  TailSync z{};
+  z.limit = H.opts.wait_spins;
+  LG_CUDA(cudaMemcpyAsync(sync.p, &z, sizeof(TailSync), cudaMemcpyHostToDevice, H.s));
+  LG_CUDA(cudaStreamSynchronize(H.s));
+}
+
 // ---------------------------------------------------------------------------
 // Coarse-tail program: the operations Engine below issues for one visit of
 // the levels from `start` down, recorded (same order, buffers and scalars)
@@ -1002,8 +1010,12 @@ struct TailBuilder {
 inline size_t tail_start_level(const Handle &H) {
   const i64 lim = H.opts.tail_rows;
   if (lim <= 0 || H.h.size() < 2) return 0;
+  // a top elimination level is applied once outside the cycle
+  // (multigrid.hpp:322), so the cycle starts at level 1 and the tail is
+  // entered at level 2 at the earliest
+  const size_t first = (H.opts.top_elim && H.h[0]->type == LIGMG_LEVEL_ELIM) ? 2 : 1;
   size_t t = H.h.size();
-  while (t > 1 && H.h[t - 1]->A.n <= lim) t--;
+  while (t > first && H.h[t - 1]->A.n <= lim) t--;
   return t < H.h.size() ? t : 0;
 }
 
@@ -1263,7 +1275,7 @@ void tail_prepare(Handle &H, Work<T> &W) {
   DBuf<T> save(nin, s);
   LG_CUDA(cudaMemcpyAsync(save.p, top.in.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
   ts.sync.alloc(1, s);
-  ts.sync.zero();
+  tail_sync_reset(H, ts.sync);
   ts.bytes = 2.0 * H.h[start]->A.n * k * sizeof(T);
   for (size_t l = start; l < H.h.size(); l++)
     ts.bytes += 8.0 * (H.h[l]->A.n + 1) + (double)H.h[l]->A.nnz * (4 + sizeof(T));
@@ -1331,30 +1343,29 @@ void tail_prepare(Handle &H, Work<T> &W) {
   cudaEventDestroy(e1);
   LG_CUDA(cudaMemcpyAsync(top.in.p, save.p, sizeof(T) * nin, cudaMemcpyDeviceToDevice, s));
   LG_CUDA(cudaStreamSynchronize(s));
-  // a barrier that gave up during the timing runs (never expected) turns the
-  // tail off rather than failing the solve
+  // a barrier wait that ran out during the timing runs fails the call like
+  // one in a solve (the tail stays off; the state is reset for a retry)
   TailSync h{};
   LG_CUDA(cudaMemcpy(&h, ts.sync.p, sizeof(TailSync), cudaMemcpyDeviceToHost));
   if (h.err) {
-    ts.sync.zero();
-    LG_CUDA(cudaStreamSynchronize(s));
-    return;
+    tail_sync_reset(H, ts.sync);
+    ts.tried = false;
+    throw Error(LIGMG_ERR_INTERNAL, "coarse-tail kernel: a grid barrier wait ran out");
   }
   ts.on = true;
 }
 
 // Error raised by a persistent tail launch (a grid barrier that gave up).
 template <typename T>
-void tail_check(Work<T> &W, cudaStream_t s) {
+void tail_check(Handle &H, Work<T> &W, cudaStream_t s) {
   if (!W.tail.on) return;
   TailSync h{};
   LG_CUDA(cudaMemcpyAsync(&h, W.tail.sync.p, sizeof(TailSync), cudaMemcpyDeviceToHost, s));
   LG_CUDA(cudaStreamSynchronize(s));
   if (h.err) {
     // an abandoned barrier leaves the arrival counter mid-way: start clean
-    W.tail.sync.zero();
-    LG_CUDA(cudaStreamSynchronize(s));
-    throw Error(LIGMG_ERR_INTERNAL, "coarse-tail kernel: grid barrier gave up");
+    tail_sync_reset(H, W.tail.sync);
+    throw Error(LIGMG_ERR_INTERNAL, "coarse-tail kernel: a grid barrier wait ran out");
   }
 }
 
@@ -2146,6 +2157,8 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
   int active = 0;
   for (int c = 0; c < k; c++) {
     rn0[c] = std::sqrt(h_rn2[c]);
+    if (!std::isfinite(rn0[c]))  // NaN or Inf in the right-hand side
+      throw Error(LIGMG_ERR_NONFINITE, "right-hand side holds a NaN or Inf");
     if (rn0[c] == 0) frozen[c] = 1; else active++;
   }
   res.hist0.push_back(rn0[0]);
@@ -2282,6 +2295,8 @@ SolveResult outer_solve_fgmres(Handle &H, size_t base, OuterWork &w, int k) {
   std::vector<char> done(k, 0);
   int active = 0;
   for (int c = 0; c < k; c++) {
+    if (!std::isfinite(rn0[c]))
+      throw Error(LIGMG_ERR_NONFINITE, "right-hand side holds a NaN or Inf");
     ttol[c] = std::max(o.tol * rn0[c], 1e-60);
     if (rn0[c] == 0) done[c] = 1;
     else active++;
@@ -2522,6 +2537,8 @@ SolveResult outer_solve_seg(Handle &H, size_t base, OuterWork &w) {
   res.col_iters = its;
   res.rel.assign(ns, 0.0);
   for (i64 g = 0; g < ns; g++) {
+    if (!std::isfinite(r0[g]))
+      throw Error(LIGMG_ERR_NONFINITE, "right-hand side holds a NaN or Inf");
     if (!std::isfinite(r2[g])) throw Error(LIGMG_ERR_BREAKDOWN, "non-finite residual");
     res.converged = res.converged && fz[g];
     res.iters = std::max(res.iters, its[g]);
@@ -2534,8 +2551,8 @@ SolveResult outer_solve_seg(Handle &H, size_t base, OuterWork &w) {
 // full solve: B (n0 x k) in w.Bfull -> w.Xfull; fills info
 // Raise the error of any persistent tail launch of this handle.
 void check_tails(Handle &H) {
-  for (auto &w : H.w32) tail_check<float>(*w.second, H.s);
-  for (auto &w : H.w64) tail_check<double>(*w.second, H.s);
+  for (auto &w : H.w32) tail_check<float>(H, *w.second, H.s);
+  for (auto &w : H.w64) tail_check<double>(H, *w.second, H.s);
 }
 
 ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *dX,
@@ -2720,6 +2737,8 @@ void ligmg_default_options(ligmg_options *o) {
   o->autotune = 1;
   o->tail_rows = 0;
   o->gmres_restart = 30;
+  o->spmv_tiles = 1;
+  o->wait_spins = 0;
 }
 
 const char *ligmg_status_string(ligmg_status s) {
@@ -2933,6 +2952,7 @@ ligmg_status ligmg_solve_pcg_jacobi(ligmg_handle h, const double *b, double *x,
            *alpha = sc.p + 5, *rn2 = sc.p + 6;
     col_dot1<double>(n, 1, R.p, R.p, rn2, red.p, s);
     double rn0 = std::sqrt(read_scalar(rn2, s));
+    if (!std::isfinite(rn0)) throw Error(LIGMG_ERR_NONFINITE, "right-hand side holds a NaN or Inf");
     std::vector<double> hist{rn0};
     int it = 0;
     bool conv = rn0 == 0;

@@ -27,7 +27,7 @@ namespace {
 
 using namespace dev;
 
-constexpr long long kBarrierSpins = 1ll << 23;  // ~0.3 s at 32 ns a spin
+constexpr long long kBarrierSpins = 1ll << 23;  // default limit: ~0.3 s at 32 ns a spin
 
 // Returns false when the barrier gave up (error recorded) or another CTA
 // reported an error: the caller leaves the kernel.
@@ -41,10 +41,11 @@ __device__ __forceinline__ bool grid_barrier(TailSync *gs, int *sh_abort, int nc
     volatile unsigned *av = &gs->arrive;
     volatile int *ev = &gs->err;
     long long spins = 0;
+    const long long limit = gs->limit > 0 ? gs->limit : kBarrierSpins;
     int abort = 0;
     while (((old ^ *av) & 0x80000000u) == 0) {
       if (*ev) { abort = 1; break; }
-      if (++spins > kBarrierSpins) {
+      if (++spins >= limit) {  // `limit` polls of an incomplete barrier
         atomicExch(&gs->err, 1);
         abort = 1;
         break;

@@ -47,15 +47,17 @@ struct TOp {
   FcgScalars sc{};          // Dir/Update
 };
 
-// Grid barrier state, zero-initialised.  Every completed barrier adds exactly
-// 2^31 to `arrive` (CTA 0 adds 2^31 - (G - 1), the others 1), so its low 31
-// bits are zero at each barrier's start and bit 31 flips exactly when the
-// last CTA arrives.  err != 0: a wait ran out of its iteration limit; every
-// CTA then leaves the kernel (the host resets the state).
+// Grid barrier state (arrive and err zero-initialised).  Every completed
+// barrier adds exactly 2^31 to `arrive` (CTA 0 adds 2^31 - (G - 1), the
+// others 1), so its low 31 bits are zero at each barrier's start and bit 31
+// flips exactly when the last CTA arrives.  err != 0: a wait ran out of its
+// iteration limit; every CTA then leaves the kernel (the host resets the
+// state).  limit: polls of an incomplete barrier before a CTA gives up
+// (<= 0: 2^23).
 struct TailSync {
   unsigned arrive;
   int err;
-  int pad[2];
+  long long limit;
 };
 
 constexpr int kTailThreads = 1024;      // grid mode

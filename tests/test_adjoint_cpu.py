@@ -50,3 +50,14 @@ def test_edge_and_rhs_gradients_match_central_differences():
         bm[i] -= h
         fd = (loss(n, u, v, w, bp, xt) - loss(n, u, v, w, bm, xt)) / (2 * h)
         assert abs(fd - lam[i]) <= 1e-5 * max(abs(fd), 1e-3 * np.abs(lam).max()), (i, fd, lam[i])
+
+
+def test_require_converged_raises_on_a_non_converged_solve():
+    import pytest
+    from ligmg_gb300.autograd import NotConvergedError, require_converged
+    from ligmg_gb300.solver import ConvergenceInfo
+    ok = ConvergenceInfo([1.0, 1e-9], 5, 0.0, 1.0, None, 1e-9, True)
+    assert require_converged(ok, "solve") is ok
+    bad = ConvergenceInfo([1.0, 0.5], 1, 0.0, 1.0, None, 0.5, False)
+    with pytest.raises(NotConvergedError):
+        require_converged(bad, "adjoint solve")
