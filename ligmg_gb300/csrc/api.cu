@@ -214,6 +214,7 @@ struct Level {
   std::vector<i64> rp_host, rrp_host, crp_host;
   int lanesA = 32, lanesR = 32, lanesP = 4, lanesC = 32;
   bool autotune = true;  // options.autotune at creation
+  bool tiles = true;     // options.spmv_tiles at creation
   // Chebyshev coefficients
   double theta = 1, delta = 1;
   std::vector<double> c1, c2;
@@ -318,10 +319,15 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
   const std::vector<i64> &rp = plan_rows(L, which);
   const i64 n = (i64)rp.size() - 1;
   const int unit = split_unit(sizeof(T), k);
+  // the single right-hand side tile layout, for matrices whose rows fill a
+  // lane's run of entries on average
+  const bool tile_ok = k == 1 && L.tiles && n > 0 &&
+                       (double)(rp[n] - rp[0]) >= kTileMinMeanRow * (double)n;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   LG_CUDA(cudaStreamIsCapturing(s, &cs));
   if (!autotune || cs != cudaStreamCaptureStatusNone || n <= 0) {
-    best.build(rp.data(), n, 32 * (i64)unit, k, s);
+    if (tile_ok) best.build_tiles(rp.data(), n, s);
+    else best.build(rp.data(), n, 32 * (i64)unit, k, s);
     best.tb = k > 1 ? 64 : 256;
     return;
   }
@@ -374,6 +380,29 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
       best.lanes = cand_lanes;
       best_ms = cand_ms;
       have = true;
+    }
+  }
+  if (tile_ok) {
+    HubPlan<T> cand;
+    cand.build_tiles(rp.data(), n, s);
+    if (cand.ntiles > 0) {
+      MatView<T> m = base;
+      cand.fill(m);
+      EpiArgs a;
+      a.y = Y.p;
+      spmm<T>(m, X.p, k, epi, a, s);
+      LG_CUDA(cudaEventRecord(e0, s));
+      for (int r = 0; r < 3; r++) spmm<T>(m, X.p, k, epi, a, s);
+      LG_CUDA(cudaEventRecord(e1, s));
+      LG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      LG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (!have || ms < best_ms) {
+        best = std::move(cand);
+        best.tb = 256;
+        best_ms = ms;
+        have = true;
+      }
     }
   }
   cudaEventDestroy(e0);
@@ -1790,8 +1819,12 @@ void finish_level(Handle &H, Level &L) {
   LG_LAUNCH();
   L.lanesA = lanes_for(L.A.nnz, L.A.n);
   L.autotune = H.opts.autotune != 0;
+  L.tiles = H.opts.spmv_tiles != 0;
   L.rp_host = L.A.rp.to_host();
-  L.hubA64.build(L.rp_host.data(), L.A.n, 32 * (i64)split_unit(8, 1), 1, s);
+  if (L.tiles && L.A.n > 0 && (double)L.A.nnz >= kTileMinMeanRow * (double)L.A.n)
+    L.hubA64.build_tiles(L.rp_host.data(), L.A.n, s);
+  else
+    L.hubA64.build(L.rp_host.data(), L.A.n, 32 * (i64)split_unit(8, 1), 1, s);
   if (L.type == LIGMG_LEVEL_ELIM) {
     L.rrp_host = L.elim.R.rp.to_host();
     L.lanesR = lanes_for(L.elim.R.nnz, L.elim.R.n);

@@ -67,6 +67,54 @@ void HubPlan<T>::build(const i64 *rp_host, i64 n, i64 split_len, int kmax, cudaS
 }
 
 template <typename T>
+void HubPlan<T>::build_tiles(const i64 *rp_host, i64 n, cudaStream_t s) {
+  // rows of up to kTilePos - 4 entries always fit a tile (after rounding the
+  // start down by at most three); longer ones become hub rows
+  build(rp_host, n, (kTilePos - 4) / 2, 1, s);
+  const i64 nnz = rp_host[n];
+  std::vector<int4> desc;
+  std::vector<u32> bits;
+  bool ok = nnz < ((i64)1 << 33);
+  i64 r = 0;
+  while (ok && r < n) {
+    const i64 len = rp_host[r + 1] - rp_host[r];
+    if (len <= 0) {  // empty rows are not supported by the tile layout
+      ok = false;
+      break;
+    }
+    if (thresh > 0 && len > thresh) {
+      r++;
+      continue;
+    }
+    const i64 r0 = r, ab = rp_host[r0] & ~(i64)3;
+    while (r < n && r - r0 < kTileRows) {
+      const i64 l = rp_host[r + 1] - rp_host[r];
+      if (l <= 0 || (thresh > 0 && l > thresh) || rp_host[r + 1] - ab > kTilePos) break;
+      r++;
+    }
+    if (r == r0) {  // cannot happen for rows of at most thresh entries
+      ok = false;
+      break;
+    }
+    desc.push_back(make_int4((int)r0, (int)(r - r0), (int)(rp_host[r] - ab), (int)(ab >> 2)));
+    u32 w[kTilePos / 32] = {0};
+    for (i64 q = r0; q < r; q++) {
+      const i64 rel = rp_host[q] - ab;
+      w[rel >> 5] |= 1u << (rel & 31);
+    }
+    bits.insert(bits.end(), w, w + kTilePos / 32);
+  }
+  ntiles = ok ? (i64)desc.size() : 0;
+  if (ntiles) {
+    tdesc.alloc(ntiles, s);
+    tdesc.upload(desc.data(), ntiles);
+    tbits.alloc((i64)bits.size(), s);
+    tbits.upload(bits.data(), (i64)bits.size());
+    LG_CUDA(cudaStreamSynchronize(s));
+  }
+}
+
+template <typename T>
 void HubPlan<T>::fill(MatView<T> &m) const {
   m.hub_thresh = thresh;
   m.nchunks = nchunks;
@@ -80,6 +128,9 @@ void HubPlan<T>::fill(MatView<T> &m) const {
   m.partial = partial.p;
   m.tb = tb;
   if (lanes > 0) m.lanes_per_row = lanes;
+  m.ntiles = ntiles;
+  m.tdesc = tdesc.p;
+  m.tbits = tbits.p;
 }
 template struct HubPlan<float>;
 template struct HubPlan<double>;
@@ -96,6 +147,185 @@ __global__ void __launch_bounds__(256, 6) k_spmm(const MatView<T> A, const T *__
   dev::spmm_unit<T, K, G, EP>(A, X, a, warp, threadIdx.x & 31);
 }
 
+// ---- single right-hand side, nonzero-balanced tiles -------------------------
+// GB300 issues about two FP64 lane operations per SM clock, so a warp-wide
+// FP64 instruction holds the SM's FP64 pipe for ~16 clocks whatever its
+// active mask; a warp per row spends a five-step shuffle reduction and a
+// lane-0 epilogue (a dozen such instructions) on every row.  Here a warp
+// takes a tile of whole rows (at most kTilePos entries), a lane 16
+// consecutive entries accumulated with one FMA each; rows crossing lanes are
+// combined by one segmented scan over the warp (five FP64 adds per tile),
+// complete row sums go to shared memory and the epilogue runs one row per
+// lane.  Every load of a tile (descriptor aside) is independent of the
+// others: one round trip brings the column indices, values and row-start
+// bits (16-byte vector loads that do not allocate in L1, so L1 keeps the
+// gathered vector), a second one all 16 gathers of a lane, and the
+// epilogue's inputs are prefetched into L1 before the gathers.  Summation
+// order: within a lane in entry order, across lanes by the scan's fixed tree.
+constexpr int kTileLane = kTilePos / 32;  // entries per lane
+constexpr int kTileWarps = 8;             // warps per block
+#ifndef LG_TILE_MIN_BLOCKS
+#define LG_TILE_MIN_BLOCKS 2  // resident blocks per SM the register budget is set for
+#endif
+
+__device__ __forceinline__ int4 ld_stream_i4(const i32 *p) {
+  int4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p));
+  return r;
+}
+__device__ __forceinline__ void ld_stream_v(const double *p, double (&o)[2]) {
+  asm volatile("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];"
+               : "=d"(o[0]), "=d"(o[1])
+               : "l"(p));
+}
+__device__ __forceinline__ void ld_stream_v(const float *p, float (&o)[4]) {
+  asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(o[0]), "=f"(o[1]), "=f"(o[2]), "=f"(o[3])
+               : "l"(p));
+}
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+// L1 prefetch of the vectors an epilogue reads for row r (1 right-hand side)
+template <typename T, Epi EP>
+__device__ __forceinline__ void epilogue_prefetch(const EpiArgs &a, i64 r) {
+  const T *b = (const T *)a.b, *xin = (const T *)a.xin, *rin = (const T *)a.rin,
+          *din = (const T *)a.din, *invd = (const T *)a.invd, *q = (const T *)a.q;
+  if constexpr (EP == Epi::Resid || EP == Epi::ElimInterp) prefetch_l1(b + r);
+  if constexpr (EP == Epi::ChebA || EP == Epi::Jacobi) {
+    prefetch_l1(b + r);
+    prefetch_l1(xin + r);
+    prefetch_l1(invd + r);
+  }
+  if constexpr (EP == Epi::ChebB) {
+    prefetch_l1(rin + r);
+    prefetch_l1(din + r);
+    prefetch_l1(xin + r);
+    prefetch_l1(invd + r);
+  }
+  if constexpr (EP == Epi::ChebZ) {
+    prefetch_l1(b + r);
+    prefetch_l1(invd + r);
+  }
+  if constexpr (EP == Epi::ElimInterp) prefetch_l1(q + r);
+  if constexpr (EP == Epi::FcgDir) {
+    prefetch_l1(xin + r);
+    prefetch_l1(q + r);
+    if (din) {
+      prefetch_l1(din + r);
+      prefetch_l1(rin + r);
+    }
+  }
+}
+
+template <typename T, Epi EP>
+__device__ __forceinline__ void tile_unit(const MatView<T> &A, const T *__restrict__ X,
+                                          const EpiArgs &a, i64 t, int lane, T *ssum) {
+  constexpr bool SPLIT = EP == Epi::Split;
+  constexpr int U = kTileLane, VWV = 16 / (int)sizeof(T);
+  const int4 d = __ldg(A.tdesc + t);
+  const int r0 = d.x, nr = d.y, e_rel = d.z;
+  const i64 ab = (i64)d.w << 2;
+  const int lb = lane * U;
+  // this lane's 16 row-start bits
+  const u32 word =
+      (__ldg(A.tbits + t * (kTilePos / 32) + (lane >> 1)) >> ((lane & 1) * 16)) & 0xffffu;
+  i32 c[U];
+  T v[U];
+#pragma unroll
+  for (int g = 0; g < U / 4; g++) {
+    const int rel = lb + 4 * g;
+    if (rel + 4 <= e_rel) {
+      const int4 cc = ld_stream_i4(A.ci + ab + rel);
+      c[4 * g] = cc.x;
+      c[4 * g + 1] = cc.y;
+      c[4 * g + 2] = cc.z;
+      c[4 * g + 3] = cc.w;
+#pragma unroll
+      for (int h = 0; h < 4 / VWV; h++) {
+        T tv[VWV];
+        ld_stream_v(A.v + ab + rel + h * VWV, tv);
+#pragma unroll
+        for (int q = 0; q < VWV; q++) v[4 * g + h * VWV + q] = tv[q];
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const bool in = rel + q < e_rel;
+        c[4 * g + q] = in ? __ldg(A.ci + ab + rel + q) : 0;
+        v[4 * g + q] = in ? __ldg(A.v + ab + rel + q) : (T)0;
+      }
+    }
+  }
+  for (int i = lane; i < nr; i += 32) epilogue_prefetch<T, EP>(a, (i64)r0 + i);
+  const int s_rel = __ffs(__shfl_sync(0xffffffffu, word, 0)) - 1;  // the tile's first entry
+  const int lo = max(s_rel - lb, 0), hi = min(e_rel - lb, U);
+  u32 okm = 0;  // this lane's entries of the tile
+  if (hi > lo) okm = ((1u << hi) - 1u) & ~((1u << lo) - 1u);
+  T xv[U];
+#pragma unroll
+  for (int j = 0; j < U; j++)
+    xv[j] = ((okm >> j) & 1u) ? __ldg(xsrc<T, 1, SPLIT>(A, X, c[j])) : (T)0;
+  // rows started before this lane: exclusive scan of the row-start counts
+  const int cnt = __popc(word);
+  int inc = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  const int pre = inc - cnt;
+  int ri = pre - 1;  // the row open at the lane's first entry
+  bool cont = true, brk = false;
+  T acc = (T)0, hs = (T)0;
+#pragma unroll
+  for (int j = 0; j < U; j++) {
+    const T vj = ((okm >> j) & 1u) ? v[j] : (T)0;
+    if ((word >> j) & 1u) {  // a row starts: close the open one
+      if (cont) hs = acc;
+      else ssum[ri] = acc;
+      cont = false;
+      brk = true;
+      ri++;
+      acc = (T)0;
+    }
+    acc = fma(vj, xv[j], acc);
+  }
+  // inclusive scan of the lanes' open sums, restarted at every lane where a
+  // row starts: S = the lane's last row summed up to the lane's end
+  T S = acc;
+  int f = brk;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T su = __shfl_up_sync(0xffffffffu, S, o);
+    const int fu = __shfl_up_sync(0xffffffffu, f, o);
+    if (lane >= o) {
+      if (!f) S += su;
+      f |= fu;
+    }
+  }
+  const T sprev = __shfl_up_sync(0xffffffffu, S, 1);
+  if (lane > 0 && brk) ssum[pre - 1] = sprev + hs;  // the row open at this lane's start ends here
+  if (lane == (e_rel - 1) / U) ssum[nr - 1] = S;     // the tile's last row
+  __syncwarp();
+  for (int i = lane; i < nr; i += 32) {
+    T r1[1] = {ssum[i]};
+    epilogue<T, 1, 1, EP>(a, (i64)r0 + i, 0, r1);
+  }
+}
+
+template <typename T, Epi EP>
+__global__ void __launch_bounds__(kTileWarps * 32, LG_TILE_MIN_BLOCKS)
+    k_spmv_tile(const MatView<T> A, const T *__restrict__ X, const EpiArgs a) {
+  __shared__ T ssum[kTileWarps][kTileRows];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const i64 warp = (i64)blockIdx.x * kTileWarps + w;
+  if (warp < A.ntiles) tile_unit<T, EP>(A, X, a, warp, lane, ssum[w]);
+  else dev::hub_unit<T, 1, EP>(A, X, a, warp - A.ntiles, lane);
+}
+
 template <typename T, int K, int G, Epi EP>
 void launch_spmm(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t s) {
   constexpr int RPW = 32 / G;
@@ -109,6 +339,13 @@ void launch_spmm(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t
 template <typename T, int K, Epi EP>
 void dispatch_g(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t s) {
   if constexpr (K == 1) {
+    // the tile layout reads 16-byte aligned column and value arrays
+    if (A.ntiles > 0 && (((uintptr_t)A.ci | (uintptr_t)A.v) & 15) == 0) {
+      k_spmv_tile<T, EP><<<grid_for(A.ntiles + A.nchunks, kTileWarps), kTileWarps * 32, 0, s>>>(
+          A, X, a);
+      LG_LAUNCH();
+      return;
+    }
     int g = A.nchunks > 0 ? 32 : A.lanes_per_row;
     switch (g) {
       case 4: return launch_spmm<T, 1, 4, EP>(A, X, a, s);

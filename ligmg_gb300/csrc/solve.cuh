@@ -24,6 +24,15 @@ struct MatView {
   T *partial = nullptr;        // nchunks x K
   int lanes_per_row = 32;      // 4, 8, 16 or 32 (single-RHS layout)
   int tb = 256;                // threads per block of the launch (64, 128 or 256)
+  // single right-hand side, tile layout (0 tiles: row layout).  Tile t:
+  // tdesc[t] = {first row, rows, e, abase / 4}: its entries are [abase + s,
+  // abase + e) with abase the first entry rounded down to a multiple of four,
+  // s < 4 and e <= kTilePos.  tbits[t * kTilePos / 32 + w] bit b: entry
+  // abase + 32 w + b starts a row of the tile.  Hub rows (longer than a
+  // tile holds) are never in a tile.
+  i64 ntiles = 0;
+  const int4 *tdesc = nullptr;
+  const u32 *tbits = nullptr;
   // Epi::Split only: the second gathered operand and the first column taken from it
   const T *x2 = nullptr;
   i64 xsplit = 0;
@@ -41,14 +50,28 @@ struct HubPlan {
   DBuf<T> partial;
   int kcap = 0;
   bool built = false;
+  // k = 1 tile layout (MatView::tdesc, tbits); ntiles = 0 when not built
+  DBuf<int4> tdesc;
+  DBuf<u32> tbits;
+  i64 ntiles = 0;
   // launch shape kept with the plan (picked by the autotuner or defaults)
   int tb = 256;    // threads per block
   int lanes = 0;   // lanes per row for k = 1 (0: the level's default)
   i64 split = 0;   // target entries per chunk: rows longer than 2 x split are
                    // cut into chunks of about split entries (at most 256 chunks)
   void build(const i64 *rp_host, i64 n, i64 split_len, int kmax, cudaStream_t s);
+  // k = 1 tile layout: rows longer than a tile holds are hub rows (the split
+  // is set so); the other rows are packed into tiles in order
+  void build_tiles(const i64 *rp_host, i64 n, cudaStream_t s);
   void fill(MatView<T> &m) const;
 };
+// Single right-hand side tile layout: at most kTilePos entries (counted from
+// the tile's first entry rounded down to a multiple of four) and kTileRows
+// rows per tile; a warp takes a tile, a lane 16 consecutive entries.
+constexpr int kTilePos = 512;
+constexpr int kTileRows = 64;
+// worthwhile from this many nonzeros per row on average
+constexpr double kTileMinMeanRow = 6.0;
 // Hub split unit U for k right-hand sides: the nonzeros a 32-lane group
 // advances per step (E = 32 / (k / VW) entry slots).  The default chunk is
 // 32 U entries (eight unrolled steps of four).

@@ -300,10 +300,52 @@ __device__ __forceinline__ void reduce_slots(T (&acc)[VW]) {
     for (int q = 0; q < VW; q++) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
 }
 
+// Hub chunk c of y = A X: the warp sums its chunk into a partial; the warp
+// that completes a hub row's last chunk sums the chunk partials in a fixed
+// order and runs the epilogue, so results do not depend on scheduling.
+template <typename T, int K, Epi EP, bool GX = true>
+__device__ __forceinline__ void hub_unit(const MatView<T> &A, const T *__restrict__ X,
+                                         const EpiArgs &a, i64 c, int lane) {
+  constexpr int G = 32;
+  constexpr int VW = (K % VT<T>::W == 0) ? VT<T>::W : 1;
+  constexpr int L = K / VW;
+  constexpr int E = G / L;
+  const int slot = lane / L, ch = lane % L;
+  if (c >= A.nchunks) return;
+  T acc[VW];
+#pragma unroll
+  for (int q = 0; q < VW; q++) acc[q] = (T)0;
+  row_accumulate<T, K, VW, E, GX, EP == Epi::Split>(A, X, A.ch_beg[c] + slot, A.ch_end[c], ch, acc);
+  reduce_slots<T, VW, L, G>(acc);
+  if (slot == 0) vstore<T, VW>(A.partial + c * K + ch * VW, acc);
+  __threadfence();
+  __syncwarp();
+  int last = 0;
+  if (lane == 0) last = atomicAdd(&A.hub_counter[A.ch_hub[c]], 1) == A.ch_cnt[c] - 1;
+  last = __shfl_sync(0xffffffffu, last, 0);
+  if (!last) return;
+  __threadfence();
+  {
+    // every slot sums a strided subset of the chunk partials; the slot
+    // partials are combined in a fixed shuffle tree (deterministic)
+    const i64 first = A.ch_first[c];
+    const int cnt = A.ch_cnt[c];
+    T s[VW];
+#pragma unroll
+    for (int q = 0; q < VW; q++) s[q] = (T)0;
+#pragma unroll 4
+    for (int t = slot; t < cnt; t += E) {
+#pragma unroll
+      for (int q = 0; q < VW; q++) s[q] += __ldcg(A.partial + (first + t) * K + ch * VW + q);
+    }
+    reduce_slots<T, VW, L, G>(s);
+    if (slot == 0) epilogue<T, K, VW, EP>(a, A.ch_row[c], ch * VW, s);
+  }
+  if (lane == 0) A.hub_counter[A.ch_hub[c]] = 0;
+}
+
 // One warp's share of y = A X with a fused epilogue: a regular row (or RPW
-// rows) for warp < ceil(n / RPW), else hub chunk warp - ceil(n / RPW); the
-// warp that completes a hub row's last chunk sums the chunk partials in a
-// fixed order and runs the epilogue.
+// rows) for warp < ceil(n / RPW), else hub chunk warp - ceil(n / RPW).
 template <typename T, int K, int G, Epi EP, bool GX = true>
 __device__ __forceinline__ void spmm_unit(const MatView<T> &A, const T *__restrict__ X,
                                           const EpiArgs &a, i64 warp, int lane) {
@@ -314,10 +356,10 @@ __device__ __forceinline__ void spmm_unit(const MatView<T> &A, const T *__restri
   constexpr int RPW = 32 / G;
   const int g = lane % G, slot = g / L, ch = g % L;
   const i64 nregw = (A.n + RPW - 1) / RPW;
-  T acc[VW];
-#pragma unroll
-  for (int q = 0; q < VW; q++) acc[q] = (T)0;
   if (warp < nregw) {
+    T acc[VW];
+#pragma unroll
+    for (int q = 0; q < VW; q++) acc[q] = (T)0;
     const i64 r = warp * RPW + lane / G;
     bool act = r < A.n;
     i64 b = 0, e = 0;
@@ -331,37 +373,7 @@ __device__ __forceinline__ void spmm_unit(const MatView<T> &A, const T *__restri
     if (act && slot == 0) epilogue<T, K, VW, EP>(a, r, ch * VW, acc);
     return;
   }
-  if constexpr (G == 32) {
-    const i64 c = warp - nregw;
-    if (c >= A.nchunks) return;
-    row_accumulate<T, K, VW, E, GX, EP == Epi::Split>(A, X, A.ch_beg[c] + slot, A.ch_end[c], ch, acc);
-    reduce_slots<T, VW, L, G>(acc);
-    if (slot == 0) vstore<T, VW>(A.partial + c * K + ch * VW, acc);
-    __threadfence();
-    __syncwarp();
-    int last = 0;
-    if (lane == 0) last = atomicAdd(&A.hub_counter[A.ch_hub[c]], 1) == A.ch_cnt[c] - 1;
-    last = __shfl_sync(0xffffffffu, last, 0);
-    if (!last) return;
-    __threadfence();
-    {
-      // every slot sums a strided subset of the chunk partials; the slot
-      // partials are combined in a fixed shuffle tree (deterministic)
-      const i64 first = A.ch_first[c];
-      const int cnt = A.ch_cnt[c];
-      T s[VW];
-#pragma unroll
-      for (int q = 0; q < VW; q++) s[q] = (T)0;
-#pragma unroll 4
-      for (int t = slot; t < cnt; t += E) {
-#pragma unroll
-        for (int q = 0; q < VW; q++) s[q] += __ldcg(A.partial + (first + t) * K + ch * VW + q);
-      }
-      reduce_slots<T, VW, L, G>(s);
-      if (slot == 0) epilogue<T, K, VW, EP>(a, A.ch_row[c], ch * VW, s);
-    }
-    if (lane == 0) A.hub_counter[A.ch_hub[c]] = 0;
-  }
+  if constexpr (G == 32) hub_unit<T, K, EP, GX>(A, X, a, warp - nregw, lane);
 }
 
 }  // namespace dev
