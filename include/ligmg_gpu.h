@@ -362,8 +362,8 @@ ligmg_status ligmg_backward(ligmg_handle h, const double *g, double *dw,
  * device.  ligmg_spmv allocates temporary buffers on every call; this
  * variant reads dx[n] and writes dy[n] (caller-owned) and keeps the
  * split-row partial sums of power-law hub rows in a fixed static device
- * array: at most 65536 row chunks and 16384 split rows per level (512 KiB +
- * 64 KiB, held by every GPU that loads the library until exit).  A level
+ * array: at most 262144 row chunks and 131072 split rows per level (2 MiB +
+ * 512 KiB, held by every GPU that loads the library until exit).  A level
  * beyond those limits returns LIGMG_ERR_UNSUPPORTED.  The work is queued on
  * the handle's stream and the call returns without synchronising.  The
  * first call on a device looks up the array's device address; make that

@@ -3361,8 +3361,8 @@ ligmg_status ligmg_kernel_stats(ligmg_handle h, ligmg_kernel_stat *out, int32_t 
 // scratch (split hub-row partial sums and their completion counters) lives in
 // this fixed device array instead of buffers owned by the handle.
 namespace {
-constexpr i64 kNoallocMaxChunks = 65536;
-constexpr i64 kNoallocMaxHubs = 16384;
+constexpr i64 kNoallocMaxChunks = 262144;
+constexpr i64 kNoallocMaxHubs = 131072;
 constexpr size_t kNoallocCounterOffset = sizeof(double) * kNoallocMaxChunks;
 static __device__ __align__(256) unsigned char
     g_spmv_scratch[sizeof(double) * kNoallocMaxChunks + sizeof(int) * kNoallocMaxHubs];

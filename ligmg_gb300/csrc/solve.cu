@@ -21,11 +21,12 @@ int split_unit(int value_bytes, int k) {
 }
 
 template <typename T>
-void HubPlan<T>::build(const i64 *rp_host, i64 n, i64 split_len, int kmax, cudaStream_t s) {
+void HubPlan<T>::build(const i64 *rp_host, i64 n, i64 split_len, int kmax, cudaStream_t s,
+                       i64 over) {
   built = true;
   kcap = kmax;
   split = split_len;
-  thresh = 2 * split_len;
+  thresh = over > 0 ? over : 2 * split_len;
   i64 thr = thresh;
   std::vector<i64> row, beg, end;
   std::vector<i32> hub, first, cnt;
@@ -69,8 +70,9 @@ void HubPlan<T>::build(const i64 *rp_host, i64 n, i64 split_len, int kmax, cudaS
 template <typename T>
 void HubPlan<T>::build_tiles(const i64 *rp_host, i64 n, cudaStream_t s) {
   // rows of up to kTilePos - 4 entries always fit a tile (after rounding the
-  // start down by at most three); longer ones become hub rows
-  build(rp_host, n, (kTilePos - 4) / 2, 1, s);
+  // start down by at most three); longer ones become hub rows, cut into
+  // chunks of about 1024 entries (at least two)
+  build(rp_host, n, 1024, 1, s, kTilePos - 4);
   const i64 nnz = rp_host[n];
   std::vector<int4> desc;
   std::vector<u32> bits;

@@ -59,7 +59,8 @@ struct HubPlan {
   int lanes = 0;   // lanes per row for k = 1 (0: the level's default)
   i64 split = 0;   // target entries per chunk: rows longer than 2 x split are
                    // cut into chunks of about split entries (at most 256 chunks)
-  void build(const i64 *rp_host, i64 n, i64 split_len, int kmax, cudaStream_t s);
+  // rows longer than `over` entries (default 2 x split_len) are split
+  void build(const i64 *rp_host, i64 n, i64 split_len, int kmax, cudaStream_t s, i64 over = 0);
   // k = 1 tile layout: rows longer than a tile holds are hub rows (the split
   // is set so); the other rows are packed into tiles in order
   void build_tiles(const i64 *rp_host, i64 n, cudaStream_t s);
