@@ -72,10 +72,13 @@ def parse():
     ap.add_argument("--scale", type=int, default=SCALE)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
-    ap.add_argument("--workload", default="rmat20", choices=["rmat20", "grid3d-ksweep", "rgg-batch"],
-                    help="rmat20: the headline line (default); grid3d-ksweep: 128^3 7-point grid, "
+    ap.add_argument("--workload", default="rmat20",
+                    choices=["rmat20", "grid2d", "grid3d-ksweep", "rgg-batch", "adjoint"],
+                    help="rmat20: the headline line (default); grid2d: 256^2 5-point grid, FP64 "
+                         "V-cycle with Chebyshev(2,2) in FCG; grid3d-ksweep: 128^3 7-point grid, "
                          "lognormal weights, k in 1,8,32,64; rgg-batch: 256 uneven random "
-                         "geometric graphs solved in one launch")
+                         "geometric graphs solved in one launch; adjoint: R-MAT 18 gradients "
+                         "against central differences and oracle-built gradients")
     ap.add_argument("--grid", type=int, default=128)
     ap.add_argument("--tail-rows", type=int, default=None,
                     help="levels with at most this many rows (from the first such level "
@@ -99,6 +102,13 @@ def dist_info():
 # entry is one of them.
 CHEB_DRAM_BYTES_RMAT20_K32 = {1: 477.93e6, 2: 294.15e6, 3: 149.99e6, 4: 61.67e6,
                               6: 12.86e6, 8: 1.62e6}
+
+
+# DRAM bytes per matrix entry of the FP64 single right-hand-side SpMV
+# (k_spmv_tile, y = A x), from an ncu capture of a smaller case of the same
+# kernel (see SPMV_TRAFFIC_SOURCE); scaled to a launch by its entries.
+SPMV_DRAM_BYTES_PER_NNZ = None
+SPMV_TRAFFIC_SOURCE = None
 
 
 def peaks():
@@ -179,7 +189,8 @@ class ClockSampler:
 
 def cpu_baseline_oracle(L, b, threads):
     """The oracle (CPU restatement of the reference algorithm), FP64 K-cycle,
-    one RHS; returns (ms per RHS, setup seconds, iterations)."""
+    one RHS; returns (ms per RHS, setup seconds, iterations, oracle solver,
+    its solution)."""
     from oracle import oracle as O
     O.set_threads(threads)
     t = time.perf_counter()
@@ -187,7 +198,89 @@ def cpu_baseline_oracle(L, b, threads):
     setup = time.perf_counter() - t
     t = time.perf_counter()
     x, info = S.solve(b)
-    return (time.perf_counter() - t) * 1e3, setup, info["iters"], S
+    return (time.perf_counter() - t) * 1e3, setup, info["iters"], S, x
+
+
+def _proj(x):
+    return x - x.mean()
+
+
+def hierarchy_parity(S, S64, R, b, x_oracle):
+    """The GPU hierarchy of the headline workload against the oracle's, on the
+    same graph: every level's type, sizes, CSR arrays and value bits and its
+    ids must be identical; one FP64 cycle from the first cycled level
+    (after the top elimination) must match to 1e-12 relative after
+    projecting out the constant; the FP64 GPU solve of b must match the
+    oracle's solution to 1e-6 relative."""
+    nl = R.num_levels
+    out = {"levels_gpu": S.num_levels, "levels_oracle": nl, "levels_equal": 0,
+           "first_mismatch": None}
+    for l in range(min(nl, S.num_levels)):
+        gi, ri = S.level_info(l), R.level_info(l)
+        eq = gi == ri
+        if eq:
+            grp, gci, gv = S.level_matrix(l)
+            rrp, rci, rv = R.level_matrix(l)
+            eq = (np.array_equal(grp, rrp) and np.array_equal(gci, rci)
+                  and np.array_equal(gv.view(np.int64), rv.view(np.int64)))
+            del grp, gci, gv, rrp, rci, rv
+        if eq and ri["type"] != "coarse":
+            eq = np.array_equal(S.level_ids(l), R.level_ids(l))
+        if eq:
+            out["levels_equal"] += 1
+        elif out["first_mismatch"] is None:
+            out["first_mismatch"] = l
+    base = 1 if R.level_info(0)["type"] == "elim" else 0
+    bb = _proj(np.random.default_rng(42).standard_normal(R.level_info(base)["n"]))
+    xg, xr = S64.cycle(base, bb), R.cycle(base, bb)
+    out["cycle_level"] = base
+    out["cycle_fp64_relerr"] = float(np.linalg.norm(_proj(xg) - _proj(xr)) /
+                                     np.linalg.norm(_proj(xr)))
+    xs = S64.solve(b).solution
+    out["solution_fp64_relerr_vs_oracle"] = float(np.linalg.norm(_proj(xs) - _proj(x_oracle)) /
+                                                  np.linalg.norm(_proj(x_oracle)))
+    out["bars"] = "levels bit-equal; cycle <= 1e-12; solution <= 1e-6"
+    out["ok"] = bool(out["levels_equal"] == nl == S.num_levels and out["cycle_fp64_relerr"] <= 1e-12
+                     and out["solution_fp64_relerr_vs_oracle"] <= 1e-6)
+    return out
+
+
+def spmv_roofline(S64, stream, peak, peak_kind, reps=20):
+    """The plain FP64 single right-hand-side SpMV y = A x (the reference's
+    SpMV_inplace, util.hpp:451-476) on the level with the most entries below
+    the top elimination, through the device-pointer entry point: CUDA events
+    on the handle's stream around `reps` launches; x (8n bytes) lies in L2,
+    the matrix (12 bytes per entry plus row pointers) does not."""
+    import ctypes as C
+    import torch
+    from ligmg_gb300._lib import check, lib
+    lv = max(range(1, S64.num_levels - 1), key=lambda l: S64.level_info(l)["nnz"])
+    inf = S64.level_info(lv)
+    n, nnz = inf["n"], inf["nnz"]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    x = torch.randn(n, dtype=torch.float64, device=dev)
+    y = torch.empty(n, dtype=torch.float64, device=dev)
+
+    def run():
+        check(lib().ligmg_spmv_device_noalloc(S64._h, lv, C.c_void_p(x.data_ptr()),
+                                              C.c_void_p(y.data_ptr())), "spmv")
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3 / reps
+    byt = 8.0 * (n + 1) + 12.0 * nnz + 16.0 * n
+    traffic = SPMV_DRAM_BYTES_PER_NNZ * nnz if SPMV_DRAM_BYTES_PER_NNZ else None
+    return {"bound": "hbm", "achieved": byt / sec / 1e9, "peak": peak, "unit": "GB/s",
+            "frac": byt / sec / 1e9 / peak, "peak_source": peak_kind,
+            "traffic": traffic, "traffic_source": SPMV_TRAFFIC_SOURCE if traffic else None,
+            "kernel": f"k_spmv_tile FP64 k=1 (y = A x), level {lv} n={n} nnz={nnz}",
+            "bytes_per_launch": byt, "us_per_launch": sec * 1e6, "launches_timed": reps}
 
 
 def run_reference(args):
@@ -355,6 +448,7 @@ def run_ours(args):
         log(f"fp32 single {fp32s['ms_per_rhs']:.2f} ms/RHS")
     # ---- plain FP64 single-RHS GPU solve (per-RHS comparison) ----------------------
     fp64 = {}
+    S64 = None
     if not args.no_fp64:
         t0 = time.perf_counter()
         S64 = Solver(L, **solver_kw("fp64"), device=local)
@@ -382,12 +476,7 @@ def run_ours(args):
         S64.solve_batched_device(b1.data_ptr(), 1, x1.data_ptr())
         st64 = S64.kernel_stats()
         S64.profile(False)
-        spmv = [r for r in st64 if r["kind"] == "spmv" and r["fp64"] and r["k"] == 1]
-        if spmv:
-            top = max(spmv, key=lambda r: r["bytes"] / max(r["launches"], 1))
-            fp64["spmv_gbs"] = top["bytes"] / top["seconds"] / 1e9
-            fp64["spmv_level"] = top["level"]
-        S64.close()
+        fp64["profile_ms_by_level"] = by_key(st64, "level", 1)
         log(f"fp64 single {fp64['ms_per_rhs']:.2f} ms/RHS")
     # ---- aggregate over ranks ----------------------------------------------------
     if ws > 1:
@@ -426,13 +515,32 @@ def run_ours(args):
                 "measured_over": f"profiled repeat of the {args.steps} timed steps "
                                  f"({profiled_ms / args.steps:.2f} ms/step with events)"}
     cpu = None
+    cpu1 = None
+    parity = None
     if not args.no_cpu_baseline and ws == 1:
+        from oracle import oracle as O
         threads = os.cpu_count() or 1
         b0 = Bd[0][:, 0].cpu().numpy().copy()
-        ms, osetup, oit, _ = cpu_baseline_oracle(L, b0, threads)
+        ms, osetup, oit, R, xo = cpu_baseline_oracle(L, b0, threads)
         cpu = {"value": ms, "unit": "ms/RHS", "cores": threads, "kind": "port",
                "sample": f"1 RHS (column 0 of the first block), FP64 K-cycle solve to rtol 1e-8 on "
                          f"the full graph, {oit} iterations; oracle setup {osetup:.1f}s untimed"}
+        O.set_threads(1)
+        t0 = time.perf_counter()
+        R.solve(b0)
+        cpu1 = {"value": (time.perf_counter() - t0) * 1e3, "unit": "ms/RHS", "cores": 1,
+                "kind": "port", "sample": "the same single-RHS solve on one core"}
+        O.set_threads(threads)
+        log(f"oracle {ms:.1f} ms/RHS on {threads} threads, {cpu1['value']:.1f} on one")
+        if S64 is not None:
+            t0 = time.perf_counter()
+            parity = hierarchy_parity(S, S64, R, b0, xo)
+            parity["seconds"] = time.perf_counter() - t0
+            log(f"parity {parity}")
+        del R
+    spmv_roof = spmv_roofline(S64, stream, *peaks()) if S64 is not None else None
+    if S64 is not None:
+        S64.close()
     levels = [S.level_info(l) for l in range(S.num_levels)]
     out = {
         "metric": METRIC, "value": value, "unit": "ms/RHS", "n_gpus": ws, "steps": args.steps,
@@ -450,6 +558,8 @@ def run_ours(args):
             "level_nnz": [l["nnz"] for l in levels],
             "l2": "hierarchy (>= 300 MB FP32+FP64 matrices) larger than the 129 MB L2",
             "fp64_single_rhs": fp64,
+            "parity": parity,
+            "cpu_baseline_1thread": cpu1,
             "speedup_vs_fp64_single": (fp64.get("ms_per_rhs", 0) / value) if fp64 else None,
             "fp32_single_rhs": fp32s,
             "speedup_fp32_single_vs_fp64_single": (fp64["ms_per_rhs"] / fp32s["ms_per_rhs"])
@@ -469,6 +579,7 @@ def run_ours(args):
                               for r in sorted(stats, key=lambda r: -r["seconds"])],
         },
         "roofline": roof,
+        "roofline_spmv": spmv_roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_ms / total_rhs, "unit": "ms/RHS",
                 "h2d_bytes_per_step": n * k * 8, "d2h_bytes_per_step": n * k * 8},
@@ -578,6 +689,183 @@ def run_rgg_batch(args):
     print(json.dumps(out), flush=True)
 
 
+def run_grid2d(args):
+    """2-D 5-point grid Laplacian 256 x 256, unit weights, one zero-mean RHS:
+    FP64 V-cycle with Chebyshev(2,2) smoothing preconditioning FCG to rtol
+    1e-8 (plain method), timed per RHS with device-resident b; the oracle
+    timed on one and on all host cores; the GPU hierarchy, one FP64 cycle and
+    the solution checked against the oracle's."""
+    import torch
+    from ligmg_gb300 import Solver
+    from ligmg_gb300 import build as Bld
+    from ligmg_gb300 import graphs as G
+    from oracle import oracle as O
+    Bld.build()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    L = G.grid2d(args.grid)
+    kw = dict(kcycle=0, outer_ksp_type="fcg", pre_smooth=2, post_smooth=2)
+    t0 = time.perf_counter()
+    S = Solver(L, **kw)
+    setup = time.perf_counter() - t0
+    S.set_stream(stream.cuda_stream)
+    b = G.rhs(L.n, seed=7)
+    Bd = [torch.from_numpy(b).to(dev).reshape(L.n, 1).contiguous()]
+    clk = ClockSampler(0)
+    clk.start()
+    ms, infos = _timed_solves(S, stream, Bd, 1, args.steps, args.warmup)
+    clocks = clk.stop()
+    # the same solve with the FP32 hierarchy (single and 32 RHS)
+    S32 = Solver(L, precision="fp32", **kw)
+    S32.set_stream(stream.cuda_stream)
+    ms32, inf32 = _timed_solves(S32, stream, Bd, 1, args.steps, args.warmup)
+    B32 = [torch.from_numpy(G.rhs(L.n, k=32, seed=8)).to(dev)]
+    ms32k, inf32k = _timed_solves(S32, stream, B32, 32, args.steps, args.warmup)
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    t0 = time.perf_counter()
+    R = O.OracleSolver(L, **kw)
+    osetup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    xo, io = R.solve(b)
+    cpu_all = (time.perf_counter() - t0) * 1e3
+    O.set_threads(1)
+    t0 = time.perf_counter()
+    R.solve(b)
+    cpu_one = (time.perf_counter() - t0) * 1e3
+    O.set_threads(threads)
+    parity = hierarchy_parity(S, S, R, b, xo)
+    value = ms / args.steps
+    peak, peak_kind = peaks()
+    out = {"metric": METRIC, "value": value, "unit": "ms/RHS", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+           "config": {"workload": f"grid2d {args.grid}x{args.grid} 5-point, unit weights, "
+                                  f"n={L.n} nnz={L.nnz}; FP64 V-cycle, Chebyshev(2,2), FCG "
+                                  f"rtol 1e-8; 1 RHS per step",
+                      "setup_s": setup, "iters": [i.iters() for i in infos],
+                      "max_true_rel_residual": max(i.true_rel_residual for i in infos),
+                      "levels": S.num_levels, "parity": parity,
+                      "fp32_hierarchy_single_ms_per_rhs": ms32 / args.steps,
+                      "fp32_hierarchy_k32_ms_per_rhs": ms32k / (32 * args.steps),
+                      "fp32_iters": [i.iters() for i in inf32],
+                      "oracle_setup_s": osetup, "oracle_iters": io["iters"],
+                      "cpu_1thread_ms_per_rhs": cpu_one,
+                      "l2": "the hierarchy (< 20 MB) fits in L2: a latency-bound workload"},
+           "roofline": spmv_roofline(S, stream, peak, peak_kind),
+           "cpu_baseline": {"value": cpu_all, "unit": "ms/RHS", "cores": threads, "kind": "port",
+                            "sample": "the same FP64 solve (1 RHS) by the oracle, all host cores; "
+                                      f"one core: {cpu_one:.1f} ms"},
+           "clocks": clocks}
+    print(json.dumps(out), flush=True)
+
+
+def run_adjoint(args):
+    """Differentiation through the solve on R-MAT 18: loss = 0.5 ||x - x_t||^2
+    with x = L(w)^+ b.  Gradients with respect to every edge weight and to b
+    from ligmg_forward / ligmg_backward (FP64, rtol 1e-12), checked on 64
+    random edges and 64 random entries of b against central differences
+    (relative step 1e-6, every perturbed system solved from a fresh setup to
+    rtol 1e-12) and on all edges against the gradient built from two oracle
+    solves (x and the adjoint lambda).  value: ms per forward + backward."""
+    import torch
+    from ligmg_gb300 import Solver
+    from ligmg_gb300 import build as Bld
+    from ligmg_gb300 import graphs as G
+    from oracle import oracle as O
+    Bld.build()
+    scale = 18 if args.scale == SCALE else args.scale
+    L0 = G.rmat(scale, edge_factor=EDGE_FACTOR, seed=GRAPH_SEED)
+    A = L0.to_scipy().tocoo()
+    m = A.row < A.col
+    u, v, w = A.row[m], A.col[m], -A.data[m]
+    n = L0.n
+    rng = np.random.default_rng(5)
+    b = G.rhs(n, seed=9)
+    xt = rng.standard_normal(n)
+    xt -= xt.mean()
+    kw = dict(kcycle=1, outer_ksp_type="fcg", tol=1e-12)
+    L = G.laplacian_from_edges(n, u, v, w)
+    S = Solver(L, **kw)
+    pos = np.empty(len(u), dtype=np.int64)  # CSR position of (u, v)
+    for e in range(len(u)):
+        lo = L.rowptr[u[e]]
+        pos[e] = lo + np.searchsorted(L.col[lo:L.rowptr[u[e] + 1]], v[e])
+
+    def fwd_bwd():
+        info = S.forward(b)
+        x = info.solution - info.solution.mean()
+        dw, db = S.backward(x - xt)
+        return x, dw[pos], db, info
+    for _ in range(args.warmup):
+        fwd_bwd()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        x, gw, gb, info = fwd_bwd()
+    value = (time.perf_counter() - t0) * 1e3 / args.steps
+
+    def loss_w(wv):
+        Sx = Solver(G.laplacian_from_edges(n, u, v, wv), **kw)
+        xs = Sx.solve(b).solution
+        Sx.close()
+        xs = xs - xs.mean()
+        return 0.5 * np.sum((xs - xt) ** 2)
+
+    def loss_b(bv):
+        xs = S.solve(bv).solution
+        xs = xs - xs.mean()
+        return 0.5 * np.sum((xs - xt) ** 2)
+    t0 = time.perf_counter()
+    ew = rng.choice(len(w), 64, replace=False)
+    fd_w = []
+    for e in ew:
+        h = 1e-6 * w[e]
+        wp, wm = w.copy(), w.copy()
+        wp[e] += h
+        wm[e] -= h
+        fd_w.append((loss_w(wp) - loss_w(wm)) / (2 * h))
+    ib = rng.choice(n, 64, replace=False)
+    fd_b = []
+    for i in ib:
+        bp, bm = b.copy(), b.copy()
+        bp[i] += 1e-6
+        bm[i] -= 1e-6
+        fd_b.append((loss_b(bp) - loss_b(bm)) / 2e-6)
+    fd_s = time.perf_counter() - t0
+    fd_w, fd_b = np.array(fd_w), np.array(fd_b)
+
+    def rel(fd, g):
+        return np.abs(fd - g) / np.maximum(np.abs(fd), 1e-300)
+    # the oracle's own solves: x, then lambda = L^+ (x - x_t)
+    O.set_threads(os.cpu_count() or 1)
+    R = O.OracleSolver(L, **kw)
+    xo, _ = R.solve(b)
+    xo -= xo.mean()
+    lam, _ = R.solve(xo - xt)
+    lam -= lam.mean()
+    gw_o = -(xo[u] - xo[v]) * (lam[u] - lam[v])
+    rw, rb = rel(fd_w, gw[ew]), rel(fd_b, gb[ib])
+    out = {"metric": "gradient of 0.5||x - x_t||^2 through the solve: ms per forward+backward",
+           "value": value, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
+           "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+           "config": {"workload": f"rmat{scale} (ef {EDGE_FACTOR}, w~U(0.5,2), LCC) n={n} "
+                                  f"edges={len(u)}; FP64 K-cycle FCG rtol 1e-12; "
+                                  "central differences with relative step 1e-6",
+                      "forward_iters": info.iters(),
+                      "edge_fd_rel_err_max": float(rw.max()),
+                      "edge_fd_rel_err_median": float(np.median(rw)),
+                      "edges_within_1e-5": int((rw <= 1e-5).sum()),
+                      "b_fd_rel_err_max": float(rb.max()),
+                      "b_within_1e-5": int((rb <= 1e-5).sum()),
+                      "checked": "64 random edges, 64 random entries of b",
+                      "vs_oracle_gradient_rel_err": float(np.linalg.norm(gw - gw_o) /
+                                                          np.linalg.norm(gw_o)),
+                      "vs_oracle_db_rel_err": float(np.linalg.norm(gb - lam) / np.linalg.norm(lam)),
+                      "fd_seconds": fd_s}}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     global TAIL_ROWS
     args = parse()
@@ -588,6 +876,12 @@ def main():
         run_grid3d(args)
     elif args.workload == "rgg-batch":
         run_rgg_batch(args)
+    elif args.workload == "grid2d":
+        if args.grid == 128:
+            args.grid = 256
+        run_grid2d(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_ours(args)
 
