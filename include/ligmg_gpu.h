@@ -74,6 +74,8 @@ typedef int ligmg_status;
 #define LIGMG_KSP_CG 0
 #define LIGMG_KSP_FCG 1
 #define LIGMG_KSP_FGMRES 2  /* flexible GMRES(gmres_restart), right preconditioned */
+#define LIGMG_KSP_PIPEFCG 3 /* the reference's pipelined FCG (parse_options.hpp:381-382):
+                               not built; ligmg_create returns LIGMG_ERR_UNSUPPORTED */
 #define LIGMG_PREC_FP64 0   /* hierarchy, smoothers and cycle in FP64 */
 #define LIGMG_PREC_FP32 1   /* FP32 hierarchy/cycle inside the FP64 outer Krylov */
 

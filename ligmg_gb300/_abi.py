@@ -28,7 +28,7 @@ STATUS_NAMES = {
 SMOOTHER = {"jacobi": 0, "chebyshev": 1}
 AFF_SCALING = {"none": 0, "row": 1, "column": 2, "rowcolumn": 3, "sym": 4, "max": 5}
 STRENGTH = {"affinity": 0, "algebraic-distance": 1, "none": 2}
-KSP = {"cg": 0, "fcg": 1, "fgmres": 2}
+KSP = {"cg": 0, "fcg": 1, "fgmres": 2, "pipefcg": 3}
 PRECISION = {"fp64": 0, "fp32": 1}
 LEVEL_TYPES = {0: "elim", 1: "agg", 2: "coarse"}
 

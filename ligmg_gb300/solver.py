@@ -337,11 +337,14 @@ class Solver:
                                info.work, None, info.true_rel_residual, st == 0, ci, ct,
                                info.cycle_complexity)
 
-    def dump_csv(self, f, info: ConvergenceInfo, graph="graph", setup_time=0.0, nnz=0):
-        """CSV row in the column order of print_csv (util.hpp:187-205)."""
-        f.write("graph,solver,iters,rel_error,cycle_complexity,wda,setup_time,solve_time,nnz,nodes\n")
-        f.write(f"{graph},ligmg,{info.iters()},{info.rel_residual()},{info.cycle_complexity()},"
-                f"{info.wda()},{setup_time},{info.time()},{nnz},1\n")
+    def dump_csv(self, f, info: ConvergenceInfo, graph="graph", setup_time=0.0, nnz=0,
+                 header=True):
+        """print_csv_header / print_csv (util.hpp:187-205): the options
+        columns, then graph, solver, iters, rel_error, cycle_complexity, wda,
+        setup_time, solve_time, nnz, nodes (csvout.py)."""
+        from . import csvout
+        csvout.write(f, self.options, info, graph=graph, setup_time=setup_time,
+                     nnz=nnz or len(self._ci), header=header)
 
 
 def prepare_graph(n, rowptr, col, val, lcc=True, laplacian=False, device=0):
