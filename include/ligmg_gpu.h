@@ -157,6 +157,14 @@ typedef struct ligmg_options {
                                  tail kernel's barriers) gives up; the kernel
                                  then stops and the call returns
                                  LIGMG_ERR_INTERNAL.  0: the default (2^23) */
+  int32_t batch_queue;        /* batch solves (ligmg_batch_solve): 1 (default):
+                                 every 16 outer iterations of all graphs run as
+                                 one persistent launch over a (graph,
+                                 operation, row block) work queue, each graph
+                                 advancing on its own and stopping when it
+                                 converges; 0: level-by-level kernels over the
+                                 union of the graphs replayed from a CUDA
+                                 graph */
 } ligmg_options;
 
 /* ConvergenceInfo (util.hpp:143-170) of one solve.  For a batched solve the

@@ -79,6 +79,7 @@ class Options(C.Structure):
         ("gmres_restart", C.c_int32),
         ("spmv_tiles", C.c_int32),
         ("wait_spins", C.c_int64),
+        ("batch_queue", C.c_int32),
     ]
 
 
@@ -147,6 +148,7 @@ def default_options(**overrides) -> Options:
     o.gmres_restart = 30
     o.spmv_tiles = 1
     o.wait_spins = 0
+    o.batch_queue = 1
     for k, v in overrides.items():
         if k in ("smoother_type",) and isinstance(v, str):
             v = SMOOTHER[v]

@@ -25,6 +25,7 @@ UNITS = {
     "solve.cu": [],
     "tail.cu": [],
     "prep.cu": [],
+    "queue.cu": [],
     "api.cu": [],
 }
 

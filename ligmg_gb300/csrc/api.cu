@@ -22,6 +22,7 @@
 #include "solve.cuh"
 #include "prep.cuh"
 #include "tail.cuh"
+#include "queue.cuh"
 
 namespace lg {
 namespace {
@@ -560,6 +561,28 @@ struct OuterWork {
   double *slot(int s) { return sc.p + (i64)s * k * 2; }
 };
 
+// Batch solves on the persistent work-queue kernel: the recorded programs
+// (outer iterations 0..15, and 16..31 for every later launch) and the state
+// of a launch.
+struct QueueProgram {
+  DBuf<QOp> ops;
+  DBuf<unsigned long long> items;
+  unsigned long long nitems = 0;
+  cudaGraphExec_t exec = nullptr;  // state reset + the launch, captured once
+  ~QueueProgram() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+struct QueueRun {
+  size_t base = 0;
+  int prec = -1;
+  QueueProgram first, more;
+  DBuf<const i64 *> segs;
+  DBuf<int> prog, blk;
+  DBuf<double> part;
+  DBuf<QueueState> st;
+};
+
 // per-kernel event timing (ligmg_profile_enable / ligmg_kernel_stats)
 struct ProfRec {
   int level, kind, k, fp64;
@@ -658,6 +681,7 @@ struct ligmg_handle_s {
   std::map<int, std::unique_ptr<lg::Work<float>>> w32;
   std::map<int, std::unique_ptr<lg::Work<double>>> w64;
   std::map<int, std::unique_ptr<lg::OuterWork>> ow;
+  std::unique_ptr<lg::QueueRun> queue;  // batch solves on the work-queue kernel
   ~ligmg_handle_s() {
     // Buffers keep the stream they were allocated on, which may be a stream
     // that is destroyed below or a caller's stream that no longer exists.
@@ -671,6 +695,7 @@ struct ligmg_handle_s {
     pgraphs.clear();
     if (batch_first) cudaGraphExecDestroy(batch_first);
     if (batch_more) cudaGraphExecDestroy(batch_more);
+    queue.reset();
     w32.clear();
     w64.clear();
     ow.clear();
@@ -2486,6 +2511,422 @@ void seg_outer_iteration(Handle &H, size_t base, OuterWork &w, SegOuter &so, int
   seg_converge(ns, so.rn2.p, so.rn0sq.p, H.opts.tol, it, so.frozen.p, so.iters.p, s);
 }
 
+// ---------------------------------------------------------------------------
+// Batch program for the persistent work-queue kernel (queue.cuh): the
+// operations of kQueueIters outer iterations, in the order the launched
+// segment path issues them (seg_outer_iteration, Engine in segment mode:
+// smooth / cycle / recurse / fcg_fixed), each tagged with the level whose
+// graph row ranges split it.  Matrices are read by whole rows.
+template <typename T>
+struct QueueBuilder {
+  Handle &H;
+  Work<T> &W;
+  OuterWork &w;
+  cudaStream_t s;
+  std::vector<QOp> ops;
+  static constexpr int DT = sizeof(T) == 8;
+  QueueBuilder(Handle &h, Work<T> &wk, OuterWork &ow) : H(h), W(wk), w(ow), s(h.s) {}
+  const ligmg_options &o() const { return H.opts; }
+
+  static int lanes_of(i64 nnz, i64 n) { return (n > 0 && nnz >= 32 * n) ? 32 : 8; }
+  template <typename V>
+  static MatView<V> whole(MatView<V> m) {
+    m.hub_thresh = 0;
+    m.nchunks = 0;
+    m.ntiles = 0;
+    return m;
+  }
+  void spmm(int lev, const MatView<T> &A, i64 nnz, const T *X, Epi e, const EpiArgs &a) {
+    QOp op;
+    op.kind = QKind::Spmm;
+    op.dbl = DT;
+    op.epi = e;
+    op.seglev = lev;
+    op.n = A.n;
+    op.lanes = lanes_of(nnz, A.n);
+    if constexpr (DT) op.Ad = whole(A);
+    else op.Af = whole(A);
+    op.x0 = X;
+    op.a = a;
+    op.a.mirror();
+    ops.push_back(op);
+  }
+  QOp &elem(QKind kind, int lev, i64 n, const void *x0, const void *x1, void *y0, double f = 1,
+            int dbl = DT) {
+    QOp op;
+    op.kind = kind;
+    op.dbl = dbl;
+    op.seglev = lev;
+    op.n = n;
+    op.x0 = x0;
+    op.x1 = x1;
+    op.y0 = y0;
+    op.f = f;
+    ops.push_back(op);
+    return ops.back();
+  }
+
+  void smooth(size_t l, T *x, const T *b, int iters, bool x_zero) {
+    Level &L = *H.h[l];
+    LevelWork<T> &lw = W.lw[l];
+    const int lv = (int)l;
+    i64 n = L.A.n;
+    MatView<T> A = viewA<T>(L, 1, s);
+    const T *invd = invdT<T>(L);
+    if (o().smoother_type == LIGMG_SMOOTHER_JACOBI) {
+      const double omega = 2.0 / 3.0;
+      if (x_zero) {
+        elem(QKind::Cheb0, lv, n, b, invd, x, omega);
+        return;
+      }
+      EpiArgs a;
+      a.b = b; a.invd = invd; a.xin = x; a.y = lw.xt.p; a.c1 = omega;
+      spmm(lv, A, L.A.nnz, x, Epi::Jacobi, a);
+      elem(QKind::Copy, lv, n, lw.xt.p, nullptr, x);
+      return;
+    }
+    if (iters <= 0) return;
+    const T *r_cur;
+    const T *x_cur;
+    T *d_cur;
+    T *d_other = lw.d1.p;
+    int first = 1;
+    if (x_zero && iters == 1) {
+      elem(QKind::Cheb0, lv, n, b, invd, x, 1.0 / L.theta);
+      return;
+    }
+    if (x_zero) {
+      const bool last = iters == 2;
+      EpiArgs a;
+      a.b = b; a.invd = invd; a.ith = 1.0 / L.theta; a.c1 = L.c1[0]; a.c2 = L.c2[0];
+      a.rout = last ? nullptr : lw.r.p;
+      a.dout = last ? nullptr : lw.d1.p;
+      a.xout = last ? x : lw.xt.p;
+      spmm(lv, viewAD<T>(L, 1, s), L.A.nnz, b, Epi::ChebZ, a);
+      if (last) return;
+      r_cur = lw.r.p;
+      d_cur = lw.d1.p;
+      d_other = lw.d0.p;
+      x_cur = lw.xt.p;
+      first = 2;
+    } else {
+      EpiArgs a;
+      a.b = b; a.invd = invd; a.xin = x; a.rout = lw.r.p; a.dout = lw.d0.p; a.xout = lw.xt.p;
+      a.ith = 1.0 / L.theta;
+      spmm(lv, A, L.A.nnz, x, Epi::ChebA, a);
+      d_cur = lw.d0.p;
+      x_cur = lw.xt.p;
+      r_cur = lw.r.p;
+      if (iters == 1) {
+        elem(QKind::Copy, lv, n, lw.xt.p, nullptr, x);
+        return;
+      }
+    }
+    for (int it = first; it < iters; it++) {
+      bool last = it == iters - 1;
+      EpiArgs a;
+      a.invd = invd;
+      a.rin = r_cur;
+      a.din = d_cur;
+      a.xin = x_cur;
+      a.c1 = L.c1[it - 1];
+      a.c2 = L.c2[it - 1];
+      a.rout = last ? nullptr : lw.r.p;
+      a.dout = last ? nullptr : d_other;
+      a.xout = last ? x : lw.xt.p;
+      spmm(lv, A, L.A.nnz, d_cur, Epi::ChebB, a);
+      if (!last) {
+        r_cur = lw.r.p;
+        std::swap(d_cur, d_other);
+        x_cur = lw.xt.p;
+      }
+    }
+  }
+
+  void cycle(size_t l, const T *b, T *x) {
+    Level &L = *H.h[l];
+    const int lv = (int)l;
+    i64 n = L.A.n;
+    if (L.type == LIGMG_LEVEL_COARSE) {
+      elem(QKind::Coarse, lv, n, b, pinvT<T>(L), x);
+      return;
+    }
+    LevelWork<T> &nw = W.lw[l + 1];
+    if (L.type == LIGMG_LEVEL_ELIM) {
+      EpiArgs a;
+      a.y = nw.in.p;
+      spmm(lv + 1, viewR<T>(L, 1, s), L.elim.R.nnz, b, Epi::Store, a);
+      recurse(l, nw.in.p, nw.out.p);
+      EpiArgs c;
+      c.y = x; c.b = b; c.q = QT<T>(L);
+      spmm(lv, viewP<T>(L), L.elim.P.nnz, nw.out.p, Epi::ElimInterp, c);
+      return;
+    }
+    smooth(l, x, b, o().pre_smooth, true);
+    EpiArgs rs;
+    rs.y = nw.in.p;
+    spmm(lv + 1, viewC<T>(L, 1, x, s), L.Cr.nnz, b, Epi::Split, rs);
+    recurse(l, nw.in.p, nw.out.p);
+    QOp &pr = elem(QKind::Prolong, lv, n, nw.out.p, nullptr, x);
+    pr.idx = L.agg.agg.p;
+    smooth(l, x, b, o().post_smooth, false);
+    if (o().constant_correction) elem(QKind::Scale, lv, n, nullptr, nullptr, x, 4.0 / 3.0);
+  }
+
+  void recurse(size_t l, T *bc, T *xc) {
+    const Level &N = *H.h[l + 1];
+    if (!o().kcycle || N.is_exact() || N.type == LIGMG_LEVEL_COARSE) {
+      cycle(l + 1, bc, xc);
+      return;
+    }
+    fcg_fixed(l + 1, bc, xc, o().kcycle_iters);
+  }
+
+  // K-cycle inner FCG in segment mode: per-graph scalars, x = 0 first
+  void fcg_fixed(size_t l, T *b, T *x, int iters) {
+    Level &L = *H.h[l];
+    LevelWork<T> &lw = W.lw[l];
+    const int lv = (int)l;
+    i64 n = L.A.n;
+    MatView<T> A = viewA<T>(L, 1, s);
+    elem(QKind::Zero, lv, n, nullptr, nullptr, x);
+    T *r = b;
+    T *p = lw.fp0.p, *pp = lw.fp1.p, *q = lw.fq0.p, *qp = lw.fq1.p;
+    FcgScalars sc{lw.sslot(S_SUM), lw.sslot(S_BETA), lw.sslot(S_ETA0), lw.sslot(S_ETA1),
+                  lw.sslot(S_ALPHA), nullptr};
+    for (int it = 0; it < iters; it++) {
+      cycle(l, r, lw.fz.p);
+      QOp &rb = elem(QKind::RedBeta, lv, n, lw.fz.p, it > 0 ? qp : nullptr, nullptr);
+      rb.flag = it > 0;
+      rb.sc = sc;
+      QOp &d = elem(QKind::Dir, lv, n, lw.fz.p, it > 0 ? pp : nullptr, p);
+      d.flag = it > 0;
+      d.sc = sc;
+      EpiArgs a;
+      a.y = q;
+      spmm(lv, A, L.A.nnz, p, Epi::Store, a);
+      QOp &ra = elem(QKind::RedAlpha, lv, n, p, q, nullptr);
+      ra.x2 = r;
+      ra.sc = sc;
+      QOp &u = elem(QKind::Update, lv, n, p, q, x);
+      u.y1 = r;
+      u.flag = it + 1 < iters;
+      u.sc = sc;
+      std::swap(p, pp);
+      std::swap(q, qp);
+      std::swap(sc.eta, sc.eta_prev);
+    }
+  }
+
+  // one outer FCG iteration (seg_outer_iteration with a native FP64 product)
+  void outer(size_t base, int it) {
+    Level &L = *H.h[base];
+    const int lv = (int)base;
+    const i64 n = L.A.n, ns = L.seginfo().nseg;
+    SegOuter &so = w.so;
+    auto slot = [&](int q) { return so.sc.p + (i64)q * ns; };
+    const bool odd = it & 1;
+    double *P = odd ? w.P1.p : w.P0.p, *PP = odd ? w.P0.p : w.P1.p;
+    double *Q = odd ? w.Q1.p : w.Q0.p, *QP = odd ? w.Q0.p : w.Q1.p;
+    double *eta = odd ? slot(S_ETA1) : slot(S_ETA0), *eta_prev = odd ? slot(S_ETA0) : slot(S_ETA1);
+    if constexpr (DT) {
+      cycle(base, w.R.p, w.Z.p);
+    } else {
+      LevelWork<T> &lw = W.lw[base];
+      elem(QKind::ToFloat, lv, n, w.R.p, nullptr, lw.in.p, 1, 0);
+      cycle(base, lw.in.p, lw.out.p);
+      elem(QKind::ToDouble, lv, n, lw.out.p, nullptr, w.Z.p, 1, 0);
+    }
+    QOp &rs = elem(QKind::RedSum, lv, n, w.Z.p, nullptr, nullptr, 1, 1);
+    rs.out = slot(S_SUM);
+    elem(QKind::SubMean, lv, n, nullptr, slot(S_SUM), w.Z.p, 1, 1);
+    FcgScalars sc{slot(S_ZQ), slot(S_BETA), eta, eta_prev, slot(S_ALPHA), so.frozen.p};
+    QOp &rb = elem(QKind::RedBeta, lv, n, w.Z.p, it > 0 ? QP : nullptr, nullptr, 1, 1);
+    rb.flag = it > 0;
+    rb.sc = sc;
+    QOp &d = elem(QKind::Dir, lv, n, w.Z.p, it > 0 ? PP : nullptr, P, 1, 1);
+    d.flag = it > 0;
+    d.sc = sc;
+    QOp sp;
+    sp.kind = QKind::Spmm;
+    sp.dbl = 1;
+    sp.epi = Epi::Store;
+    sp.seglev = lv;
+    sp.n = n;
+    sp.lanes = lanes_of(L.A.nnz, n);
+    sp.Ad = whole(viewA<double>(L, 1, s));
+    sp.x0 = P;
+    sp.a.y = Q;
+    ops.push_back(sp);
+    QOp &ra = elem(QKind::RedAlpha, lv, n, P, Q, nullptr, 1, 1);
+    ra.x2 = w.R.p;
+    ra.sc = sc;
+    QOp &u = elem(QKind::Update, lv, n, P, Q, w.X.p, 1, 1);
+    u.y1 = w.R.p;
+    u.flag = 1;
+    u.sc = sc;
+    QOp &rn = elem(QKind::RedNorm, lv, n, w.R.p, nullptr, nullptr, 1, 1);
+    rn.out = so.rn2.p;
+    rn.rn0sq = so.rn0sq.p;
+    rn.tol2 = H.opts.tol * H.opts.tol;
+    rn.frozen = so.frozen.p;
+    rn.iters = so.iters.p;
+    rn.it = it;
+  }
+};
+
+// Record kQueueIters outer iterations from it0 as a program: the operations
+// and their (graph, row block) items.
+template <typename T>
+void queue_record(Handle &H, Work<T> &W, OuterWork &w, size_t base, int it0, QueueProgram &P) {
+  QueueBuilder<T> B(H, W, w);
+  for (int it = it0; it < it0 + kQueueIters; it++) B.outer(base, it);
+  const i64 ns = H.h[base]->seginfo().nseg;
+  std::vector<unsigned long long> items;
+  for (size_t i = 0; i < B.ops.size(); i++) {
+    const std::vector<i64> &sg = H.h[B.ops[i].seglev]->seg_host;
+    for (i64 g = 0; g < ns; g++) {
+      const i64 rows = sg[g + 1] - sg[g];
+      const i64 nb = std::max<i64>(1, cdiv(rows, kQueueRows));
+      if (nb > kQueueMaxBlocks)
+        throw Error(LIGMG_ERR_UNSUPPORTED, "a graph of the batch is too large for the work queue");
+      for (i64 b = 0; b < nb; b++)
+        items.push_back(((unsigned long long)i << 40) | ((unsigned long long)g << 20) |
+                        (unsigned long long)b);
+    }
+  }
+  if (B.ops.size() >= ((size_t)1 << 23) || ns >= ((i64)1 << 20))
+    throw Error(LIGMG_ERR_UNSUPPORTED, "batch program too large for the work queue");
+  P.ops.alloc((i64)B.ops.size(), H.s);
+  P.ops.upload(B.ops.data(), (i64)B.ops.size());
+  P.items.alloc((i64)items.size(), H.s);
+  P.items.upload(items.data(), (i64)items.size());
+  P.nitems = items.size();
+  LG_CUDA(cudaStreamSynchronize(H.s));
+}
+
+// Batch outer solve on the work-queue kernel: one launch per kQueueIters
+// outer iterations of every graph (captured with its state reset in a CUDA
+// graph), relaunched until all graphs have converged or the limit is reached.
+template <typename T>
+SolveResult outer_solve_queue(Handle &H, size_t base, OuterWork &w) {
+  cudaStream_t s = H.s;
+  Level &L = *H.h[base];
+  const i64 n = L.A.n;
+  const SegInfo S = L.seginfo();
+  const i64 ns = S.nseg;
+  SegOuter &so = w.so;
+  if (so.frozen.n != ns) {
+    so.sc.alloc((i64)S_NSLOT * ns, s);
+    so.sc.zero();
+    so.rn2.alloc(ns, s);
+    so.rn0sq.alloc(ns, s);
+    so.frozen.alloc(ns, s);
+    so.iters.alloc(ns, s);
+  }
+  LG_CUDA(cudaMemsetAsync(w.X.p, 0, sizeof(double) * n, s));
+  LG_CUDA(cudaMemcpyAsync(w.R.p, w.B.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  LG_CUDA(cudaMemsetAsync(so.frozen.p, 0, sizeof(int) * ns, s));
+  seg_dot<double>(S, w.R.p, w.R.p, so.rn0sq.p, s);
+  seg_converge(ns, so.rn0sq.p, so.rn0sq.p, 0.0, -1, so.frozen.p, so.iters.p, s);  // b = 0
+  Work<T> &W = work_for<T>(H, 1);
+  const int prec = (int)sizeof(T);
+  if (!H.queue || H.queue->base != base || H.queue->prec != prec) {
+    H.queue.reset(new QueueRun());
+    QueueRun &Q = *H.queue;
+    Q.base = base;
+    Q.prec = prec;
+    std::vector<const i64 *> segs;
+    for (auto &lv : H.h) segs.push_back(lv->segptr.p);
+    Q.segs.alloc((i64)segs.size(), s);
+    Q.segs.upload(segs.data(), (i64)segs.size());
+    Q.prog.alloc(ns, s);
+    Q.blk.alloc(ns, s);
+    Q.part.alloc(ns * kQueueMaxBlocks * 3, s);
+    Q.st.alloc(1, s);
+    Q.st.zero();
+    queue_record<T>(H, W, w, base, 0, Q.first);
+    queue_record<T>(H, W, w, base, kQueueIters, Q.more);
+  }
+  QueueRun &Q = *H.queue;
+  auto args = [&](QueueProgram &P) {
+    QueueArgs a;
+    a.ops = P.ops.p;
+    a.items = P.items.p;
+    a.nitems = P.nitems;
+    a.segs = Q.segs.p;
+    a.nseg = (int)ns;
+    a.prog = Q.prog.p;
+    a.blk = Q.blk.p;
+    a.part = Q.part.p;
+    a.frozen = so.frozen.p;
+    a.st = Q.st.p;
+    a.wait_limit = H.opts.wait_spins > 0 ? H.opts.wait_spins : (1ll << 23);
+    return a;
+  };
+  // the launch and its state reset (ticket, error, progress counters) as one
+  // captured graph per program
+  auto graph_of = [&](QueueProgram &P) {
+    if (P.exec) return P.exec;
+    cudaGraph_t g = nullptr;
+    LG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      LG_CUDA(cudaMemsetAsync(Q.st.p, 0, offsetof(QueueState, it_offset), s));
+      LG_CUDA(cudaMemsetAsync(Q.prog.p, 0, sizeof(int) * ns, s));
+      LG_CUDA(cudaMemsetAsync(Q.blk.p, 0, sizeof(int) * ns, s));
+      launch_queue(args(P), s);
+    } catch (...) {
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    LG_CUDA(cudaStreamEndCapture(s, &g));
+    cudaError_t e = cudaGraphInstantiate(&P.exec, g, 0);
+    cudaGraphDestroy(g);
+    LG_CUDA(e);
+    add_launches(-1);  // the capture counted the launch; replays count it below
+    return P.exec;
+  };
+  SolveResult res;
+  std::vector<int> fz(ns), its(ns);
+  int done = 0;
+  for (int launch = 0; done < H.opts.iters; launch++) {
+    QueueProgram &P = launch == 0 ? Q.first : Q.more;
+    cudaGraphExec_t ex = graph_of(P);
+    const int offset = launch == 0 ? 0 : done - kQueueIters;
+    LG_CUDA(cudaMemcpyAsync(&Q.st.p->it_offset, &offset, sizeof(int), cudaMemcpyHostToDevice, s));
+    LG_CUDA(cudaGraphLaunch(ex, s));
+    add_launches(1);
+    done += kQueueIters;
+    QueueState hs{};
+    LG_CUDA(cudaMemcpyAsync(&hs, Q.st.p, sizeof(QueueState), cudaMemcpyDeviceToHost, s));
+    LG_CUDA(cudaMemcpyAsync(fz.data(), so.frozen.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, s));
+    LG_CUDA(cudaStreamSynchronize(s));
+    if (hs.err) throw Error(LIGMG_ERR_INTERNAL, "batch work queue: a wait ran out");
+    bool all = true;
+    for (int v : fz) all = all && v;
+    if (all) break;
+  }
+  std::vector<double> r2(ns), r0(ns);
+  LG_CUDA(cudaMemcpyAsync(its.data(), so.iters.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, s));
+  LG_CUDA(cudaMemcpyAsync(r2.data(), so.rn2.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
+  LG_CUDA(cudaMemcpyAsync(r0.data(), so.rn0sq.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
+  LG_CUDA(cudaStreamSynchronize(s));
+  res.converged = true;
+  res.col_iters = its;
+  res.rel.assign(ns, 0.0);
+  for (i64 g = 0; g < ns; g++) {
+    if (!std::isfinite(r0[g]))
+      throw Error(LIGMG_ERR_NONFINITE, "right-hand side holds a NaN or Inf");
+    if (!std::isfinite(r2[g]) && !fz[g]) throw Error(LIGMG_ERR_BREAKDOWN, "non-finite residual");
+    res.converged = res.converged && fz[g];
+    res.iters = std::max(res.iters, its[g]);
+    res.rel[g] = r0[g] > 0 ? std::sqrt(r2[g] / r0[g]) : 0.0;
+  }
+  res.hist0 = {std::sqrt(r0[0]), std::sqrt(r2[0])};
+  return res;
+}
+
 template <typename T>
 SolveResult outer_solve_seg(Handle &H, size_t base, OuterWork &w) {
   cudaStream_t s = H.s;
@@ -2630,8 +3071,12 @@ ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *
   if (seg && H.opts.outer_ksp_type == LIGMG_KSP_FGMRES)
     throw Error(LIGMG_ERR_UNSUPPORTED, "batch mode runs FCG or CG outer iterations");
   if (seg)
-    res = (H.opts.precision == LIGMG_PREC_FP32) ? outer_solve_seg<float>(H, base, w)
-                                                : outer_solve_seg<double>(H, base, w);
+    if (H.opts.batch_queue)
+      res = (H.opts.precision == LIGMG_PREC_FP32) ? outer_solve_queue<float>(H, base, w)
+                                                  : outer_solve_queue<double>(H, base, w);
+    else
+      res = (H.opts.precision == LIGMG_PREC_FP32) ? outer_solve_seg<float>(H, base, w)
+                                                  : outer_solve_seg<double>(H, base, w);
   else if (H.opts.outer_ksp_type == LIGMG_KSP_FGMRES)
     res = (H.opts.precision == LIGMG_PREC_FP32) ? outer_solve_fgmres<float>(H, base, w, k)
                                                 : outer_solve_fgmres<double>(H, base, w, k);
@@ -2772,6 +3217,7 @@ void ligmg_default_options(ligmg_options *o) {
   o->gmres_restart = 30;
   o->spmv_tiles = 1;
   o->wait_spins = 0;
+  o->batch_queue = 1;
 }
 
 const char *ligmg_status_string(ligmg_status s) {

@@ -60,3 +60,52 @@ def test_batch_rejects_off_block_entries():
     st = lib().ligmg_batch_create(2, p(bad), p(U.rowptr), p(U.col), p(U.val), C.byref(o),
                                   C.byref(h))
     assert st == 2
+
+
+@pytest.mark.parametrize("kw", [dict(precision="fp64", kcycle=1), dict(precision="fp32", kcycle=1),
+                                dict(precision="fp64", kcycle=0)])
+def test_work_queue_matches_union_graph_mode(kw):
+    # batch_queue = 1: one persistent launch over (graph, operation, row
+    # block) items per 16 outer iterations; 0: level kernels over the union.
+    # Same operations, reductions summed in a different fixed order.
+    gs = _graphs()
+    bs = [G.rhs(g.n, seed=30 + i) for i, g in enumerate(gs)]
+    bs[2] = np.zeros(gs[2].n)  # a graph with nothing to solve
+    xq, iq = BatchSolver(gs, batch_queue=1, **kw).solve(bs)
+    xu, iu = BatchSolver(gs, batch_queue=0, **kw).solve(bs)
+    assert iq.converged and iu.converged
+    assert iq.col_iters[2] == 0 and not np.any(xq[2])
+    assert (np.abs(iq.col_iters.astype(int) - iu.col_iters.astype(int)) <= 1).all(), \
+        (iq.col_iters, iu.col_iters)
+    for g, (a, b) in enumerate(zip(xq, xu)):
+        if g != 2:
+            assert _rel(a, b) <= 1e-6, g
+            assert iq.col_true_rel_residual[g] <= 2e-8, g
+
+
+def test_work_queue_relaunches_past_sixteen_iterations():
+    # a slow configuration (V-cycle, one Jacobi sweep, tight tolerance) needs
+    # more than one 16-iteration launch; iteration counts continue across
+    # launches and every graph still matches its single-graph solve
+    gs = _graphs()[:4]
+    kw = dict(kcycle=0, smoother_type="jacobi", tol=1e-10)
+    bs = [G.rhs(g.n, seed=40 + i) for i, g in enumerate(gs)]
+    xs, info = BatchSolver(gs, batch_queue=1, **kw).solve(bs)
+    assert info.converged and info.col_iters.max() > 16
+    for g, (L, b, x) in enumerate(zip(gs, bs, xs)):
+        single = Solver(L, outer_ksp_type="fcg", **kw).solve(b)
+        assert abs(int(info.col_iters[g]) - single.iters()) <= 1, (g, info.col_iters[g],
+                                                                     single.iters())
+        assert _rel(x, single.solution) <= 1e-6, g
+
+
+def test_work_queue_wait_limit_reports_internal_error():
+    from ligmg_gb300._lib import LigmgError
+    gs = _graphs()
+    bs = [G.rhs(g.n, seed=50 + i) for i, g in enumerate(gs)]
+    B = BatchSolver(gs, batch_queue=1, wait_spins=1, kcycle=1)
+    with pytest.raises(LigmgError) as e:  # a CTA gives up on its first poll
+        B.solve(bs)
+    assert e.value.status == 12
+    xs, info = BatchSolver(gs, batch_queue=1, kcycle=1).solve(bs)  # the context is intact
+    assert info.converged
