@@ -94,21 +94,31 @@ def dist_info():
     return ws, rank, local
 
 
-# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum from one
-# single-pass ncu capture of every ChebZ and ChebB SpMM launch of one timed step
-# of the default workload: R-MAT scale 20, k = 32, FP32 hierarchy), averaged per
-# level over that level's launches of both kernels; the profile's `cheb_b` entries
-# group exactly those launches.  Used for roofline.traffic when the dominant
-# entry is one of them.
-CHEB_DRAM_BYTES_RMAT20_K32 = {1: 477.93e6, 2: 294.15e6, 3: 149.99e6, 4: 61.67e6,
-                              6: 12.86e6, 8: 1.62e6}
+# DRAM bytes per matrix entry of the k = 32 FP32 SpMM with the fused
+# Chebyshev epilogue, from an ncu capture of a smaller case of the same kernel
+# (R-MAT 19 level 1, the ChebZ launch: 183.3 MB over 15,448,585 entries);
+# roofline.traffic scales it by the dominant launch's entries.  Levels whose
+# vectors stay in L2 move less, so this is an upper estimate there.
+SPMM_K32_DRAM_BYTES_PER_NNZ = 183.30e6 / 15448585
+SPMM_K32_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_spmm<float, 32, "
+                           "ChebZ> on R-MAT 19 level 1 (15,448,585 entries, 183.3 MB, 11.9 "
+                           "bytes per entry), scaled by the launch's entries")
+
+
+def level_nnz_of(S, level):
+    try:
+        return S.level_info(level)["nnz"]
+    except Exception:
+        return None
 
 
 # DRAM bytes per matrix entry of the FP64 single right-hand-side SpMV
 # (k_spmv_tile, y = A x), from an ncu capture of a smaller case of the same
 # kernel (see SPMV_TRAFFIC_SOURCE); scaled to a launch by its entries.
-SPMV_DRAM_BYTES_PER_NNZ = None
-SPMV_TRAFFIC_SOURCE = None
+SPMV_DRAM_BYTES_PER_NNZ = 194.58e6 / 15448585
+SPMV_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_spmv_tile (FP64, "
+                       "y = A x) on R-MAT 19 level 1 (15,448,585 entries): 194.58 MB per "
+                       "launch, 12.6 bytes per entry, scaled by this launch's entries")
 
 
 def peaks():
@@ -279,7 +289,8 @@ def spmv_roofline(S64, stream, peak, peak_kind, reps=20):
     return {"bound": "hbm", "achieved": byt / sec / 1e9, "peak": peak, "unit": "GB/s",
             "frac": byt / sec / 1e9 / peak, "peak_source": peak_kind,
             "traffic": traffic, "traffic_source": SPMV_TRAFFIC_SOURCE if traffic else None,
-            "kernel": f"k_spmv_tile FP64 k=1 (y = A x), level {lv} n={n} nnz={nnz}",
+            "kernel": f"FP64 k=1 SpMV y = A x (layout picked by the setup autotuner), "
+                      f"level {lv} n={n} nnz={nnz}",
             "bytes_per_launch": byt, "us_per_launch": sec * 1e6, "launches_timed": reps}
 
 
@@ -501,11 +512,12 @@ def run_ours(args):
         per_launch_s = top["seconds"] / top["launches"]
         ach = per_launch_bytes / per_launch_s / 1e9
         traffic, traffic_src = None, None
-        if (args.workload == "rmat20" and args.scale == 20 and k == 32 and not top["fp64"]
-                and top["kind"] == "cheb_b" and top["level"] in CHEB_DRAM_BYTES_RMAT20_K32):
-            traffic = CHEB_DRAM_BYTES_RMAT20_K32[top["level"]]
-            traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
-                           "mean over the level's ChebZ and ChebB launches of one step")
+        if not top["fp64"] and top["kind"] in ("cheb_b", "agg_restrict", "spmv"):
+            # DRAM bytes per entry of the k = 32 FP32 Chebyshev SpMM measured on a
+            # smaller case (profiles/spmm_k32_fp32_rmat19.md), scaled by entries
+            nnz_top = level_nnz_of(S, top["level"])
+            traffic = SPMM_K32_DRAM_BYTES_PER_NNZ * nnz_top if nnz_top else None
+            traffic_src = SPMM_K32_TRAFFIC_SOURCE
         roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "traffic": traffic, "traffic_source": traffic_src, "peak_source": peak_kind,
                 "kernel": f"spmm_{top['kind']} level {top['level']} k={top['k']} "

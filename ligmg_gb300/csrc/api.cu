@@ -1846,10 +1846,10 @@ void finish_level(Handle &H, Level &L) {
   L.autotune = H.opts.autotune != 0;
   L.tiles = H.opts.spmv_tiles != 0;
   L.rp_host = L.A.rp.to_host();
-  if (L.tiles && L.A.n > 0 && (double)L.A.nnz >= kTileMinMeanRow * (double)L.A.n)
-    L.hubA64.build_tiles(L.rp_host.data(), L.A.n, s);
-  else
-    L.hubA64.build(L.rp_host.data(), L.A.n, 32 * (i64)split_unit(8, 1), 1, s);
+  // the FP64 single right-hand-side plan of A is built (and, with autotune,
+  // its layout and launch shape timed) at setup: ligmg_spmv_device_noalloc
+  // and every FP64 solve use it without building anything later
+  build_plan<double>(L, MAT_A, 1, L.hubA64, L.autotune, s);
   if (L.type == LIGMG_LEVEL_ELIM) {
     L.rrp_host = L.elim.R.rp.to_host();
     L.lanesR = lanes_for(L.elim.R.nnz, L.elim.R.n);

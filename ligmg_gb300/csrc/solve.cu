@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(256, 6) k_spmm(const MatView<T> A, const T *__
 constexpr int kTileLane = kTilePos / 32;  // entries per lane
 constexpr int kTileWarps = 8;             // warps per block
 #ifndef LG_TILE_MIN_BLOCKS
-#define LG_TILE_MIN_BLOCKS 2  // resident blocks per SM the register budget is set for
+#define LG_TILE_MIN_BLOCKS 3  // resident blocks per SM the register budget is set for
 #endif
 
 __device__ __forceinline__ int4 ld_stream_i4(const i32 *p) {
