@@ -512,7 +512,7 @@ def run_ours(args):
         per_launch_s = top["seconds"] / top["launches"]
         ach = per_launch_bytes / per_launch_s / 1e9
         traffic, traffic_src = None, None
-        if not top["fp64"] and top["kind"] in ("cheb_b", "agg_restrict", "spmv"):
+        if not top["fp64"] and top["kind"] in ("cheb_b", "spmv"):
             # DRAM bytes per entry of the k = 32 FP32 Chebyshev SpMM measured on a
             # smaller case (profiles/spmm_k32_fp32_rmat19.md), scaled by entries
             nnz_top = level_nnz_of(S, top["level"])
