@@ -137,12 +137,15 @@ __global__ void k_edge_grad(const i64 *rp, const i32 *ci, i64 n, const double *x
   }
 }
 
-// segment offsets of the next level: the first new id inside each segment
-__global__ void k_gather_offsets(const i32 *scan, const i64 *seg_in, i64 nseg, i64 nc,
+// segment offsets of the next level: the first new id inside each segment.
+// A graph of the batch can vanish from a level (a lone vertex eliminated),
+// so trailing segments may be empty and start at n, past the scan's end:
+// they start at nc on the next level.
+__global__ void k_gather_offsets(const i32 *scan, const i64 *seg_in, i64 nseg, i64 n, i64 nc,
                                  i64 *seg_out) {
   i64 sg = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (sg > nseg) return;
-  seg_out[sg] = (sg == nseg) ? nc : (i64)scan[seg_in[sg]];
+  seg_out[sg] = (sg == nseg || seg_in[sg] >= n) ? nc : (i64)scan[seg_in[sg]];
 }
 
 __global__ void k_fill_rowseg(const i64 *segptr, i64 nseg, i64 n, i32 *rowseg) {
@@ -1905,7 +1908,8 @@ void make_hierarchy(Handle &H, i64 n, const i64 *rowptr, const i32 *col, const d
   auto next_offsets = [&](const Level &L, const i32 *scan, i64 nc) {
     if (!nseg) return;
     DBuf<i64> out(nseg + 1, s);
-    k_gather_offsets<<<grid_for(nseg + 1, 128), 128, 0, s>>>(scan, L.segptr.p, nseg, nc, out.p);
+    k_gather_offsets<<<grid_for(nseg + 1, 128), 128, 0, s>>>(scan, L.segptr.p, nseg, L.A.n, nc,
+                                                             out.p);
     LG_LAUNCH();
     cur_seg = out.to_host();
   };

@@ -112,3 +112,21 @@ def test_work_queue_wait_limit_reports_internal_error():
     assert e.value.status == 12
     xs, info = BatchSolver(gs, batch_queue=1, kcycle=1).solve(bs)  # the context is intact
     assert info.converged
+
+
+@pytest.mark.parametrize("queue", [1, 0])
+def test_batch_with_graphs_that_vanish_at_coarse_levels(queue):
+    # small graphs last: they shrink to nothing while the union is still
+    # coarsened, leaving empty trailing segments on the coarse levels
+    gs = [G.rgg(3000, seed=7), G.grid2d(24, weights="lognormal", seed=8), G.grid2d(5, seed=9),
+          G.rgg(60, seed=10)]
+    B = BatchSolver(gs, precision="fp32", kcycle=1, batch_queue=queue)
+    bs = [G.rhs(g.n, seed=60 + i) for i, g in enumerate(gs)]
+    xs, info = B.solve(bs)
+    assert info.converged
+    for g, (L, b, x) in enumerate(zip(gs, bs, xs)):
+        assert np.isfinite(x).all(), g
+        r = b - L.to_scipy() @ x
+        assert np.linalg.norm(r) / np.linalg.norm(b) <= 2e-8, g
+        xr, _ = O.OracleSolver(L, kcycle=1, outer_ksp_type="fcg").solve(b)
+        assert _rel(x, xr) <= 1e-6, g
