@@ -17,15 +17,16 @@ namespace {
 using namespace dev;
 
 // rows [r0, r1) of y = A X with a fused epilogue, G lanes per row (k = 1)
+// rowseg/frozen (group items): rows of converged graphs are skipped
 template <typename T, int G, Epi EP>
 __device__ void q_spmm_rows(const MatView<T> &A, const T *__restrict__ X, const EpiArgs &a,
-                            i64 r0, i64 r1) {
+                            i64 r0, i64 r1, const i32 *rowseg, const int *frozen) {
   constexpr int RPW = 32 / G;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int grp = lane / G, slot = lane % G;
   for (i64 base = r0 + (i64)warp * RPW; base < r1; base += (kQueueThreads / 32) * RPW) {
     const i64 r = base + grp;
-    const bool act = r < r1;
+    const bool act = r < r1 && !(rowseg && frozen[rowseg[r]]);
     T acc[1] = {(T)0};
     if (act) row_accumulate<T, 1, 1, G, true, EP == Epi::Split>(A, X, A.rp[r] + slot, A.rp[r + 1], 0, acc);
     reduce_slots<T, 1, 1, G>(acc);
@@ -34,13 +35,14 @@ __device__ void q_spmm_rows(const MatView<T> &A, const T *__restrict__ X, const 
 }
 
 template <typename T>
-__device__ void q_spmm(const QOp &op, const MatView<T> &A, i64 r0, i64 r1) {
+__device__ void q_spmm(const QOp &op, const MatView<T> &A, i64 r0, i64 r1, const i32 *rowseg,
+                       const int *frozen) {
   const T *X = (const T *)op.x0;
   switch (op.epi) {
-#define LG_Q_EPI(E)                                                         \
-  case E:                                                                   \
-    if (op.lanes == 8) q_spmm_rows<T, 8, E>(A, X, op.a, r0, r1);            \
-    else q_spmm_rows<T, 32, E>(A, X, op.a, r0, r1);                         \
+#define LG_Q_EPI(E)                                                               \
+  case E:                                                                         \
+    if (op.lanes == 8) q_spmm_rows<T, 8, E>(A, X, op.a, r0, r1, rowseg, frozen);  \
+    else q_spmm_rows<T, 32, E>(A, X, op.a, r0, r1, rowseg, frozen);               \
     break;
     LG_Q_EPI(Epi::Store)
     LG_Q_EPI(Epi::Resid)
@@ -99,6 +101,66 @@ __device__ void q_reduce(const QOp &op, i64 r0, i64 r1, double *dst,
   if (t == 0)
 #pragma unroll
     for (int v = 0; v < 3; v++) dst[v] = sh[v][0];
+}
+
+// Elementwise operations on rows [r0, r1).  Single graph g (rowseg null):
+// its columns are [g0, g1).  Group (rowseg set): each row's graph from
+// rowseg, rows of converged graphs skipped, columns from seg.
+template <typename T>
+__device__ void q_elementwise_group(const QOp &op, i64 r0, i64 r1, const i64 *seg,
+                                   const i32 *rowseg, const int *frozen) {
+  T *y0 = (T *)op.y0;
+  const T *x0 = (const T *)op.x0, *x1 = (const T *)op.x1;
+  for (i64 r = r0 + threadIdx.x; r < r1; r += kQueueThreads) {
+    const int g = rowseg[r];
+    if (frozen[g]) continue;
+    switch (op.kind) {
+      case QKind::Cheb0:
+        y0[r] = (x1[r] * (T)op.f) * x0[r];
+        break;
+      case QKind::Prolong:
+        y0[r] += x0[op.idx[r]];
+        break;
+      case QKind::Coarse: {
+        T s = 0;
+        for (i64 j = seg[g]; j < seg[g + 1]; j++) s += x1[r * op.n + j] * x0[j];
+        y0[r] = s;
+        break;
+      }
+      case QKind::Scale:
+        y0[r] = y0[r] * (T)op.f;
+        break;
+      case QKind::Zero:
+        y0[r] = (T)0;
+        break;
+      case QKind::Copy:
+        y0[r] = x0[r];
+        break;
+      case QKind::SubMean:
+        y0[r] = (T)((double)y0[r] - ((const double *)op.x1)[g]);
+        break;
+      case QKind::Dir: {
+        T v = x0[r] - (T)op.sc.mu[g];
+        if (x1) v = v - (T)op.sc.beta[g] * x1[r];
+        y0[r] = v;
+        break;
+      }
+      case QKind::Update: {
+        const T al = (T)op.sc.alpha[g];
+        y0[r] = y0[r] + al * x0[r];
+        if (op.flag) ((T *)op.y1)[r] = ((T *)op.y1)[r] - al * x1[r];
+        break;
+      }
+      case QKind::ToFloat:
+        ((float *)op.y0)[r] = (float)((const double *)op.x0)[r];
+        break;
+      case QKind::ToDouble:
+        ((double *)op.y0)[r] = (double)((const float *)op.x0)[r];
+        break;
+      default:
+        break;
+    }
+  }
 }
 
 template <typename T>
@@ -166,8 +228,8 @@ __device__ void q_item(const QOp &op, int g, int b, i64 r0, i64 r1, i64 g0, i64 
                        double *part, double (*sh)[kQueueThreads]) {
   switch (op.kind) {
     case QKind::Spmm:
-      if (op.dbl) q_spmm<double>(op, op.Ad, r0, r1);
-      else q_spmm<float>(op, op.Af, r0, r1);
+      if (op.dbl) q_spmm<double>(op, op.Ad, r0, r1, nullptr, nullptr);
+      else q_spmm<float>(op, op.Af, r0, r1, nullptr, nullptr);
       break;
     case QKind::ToFloat:
       for (i64 r = r0 + threadIdx.x; r < r1; r += kQueueThreads)
@@ -193,15 +255,12 @@ __device__ void q_item(const QOp &op, int g, int b, i64 r0, i64 r1, i64 g0, i64 
   }
 }
 
-// the graph's operation is complete: sum the block partials in block order
-__device__ void q_finalize(const QOp &op, int g, int nb, i64 ng, const double *part,
-                           int it_offset) {
-  if (op.kind != QKind::RedSum && op.kind != QKind::RedBeta && op.kind != QKind::RedAlpha &&
-      op.kind != QKind::RedNorm)
-    return;
-  double t[3] = {0, 0, 0};
-  for (int b = 0; b < nb; b++)
-    for (int v = 0; v < 3; v++) t[v] += __ldcg(part + ((i64)g * kQueueMaxBlocks + b) * 3 + v);
+__device__ bool q_is_reduction(QKind k) {
+  return k == QKind::RedSum || k == QKind::RedBeta || k == QKind::RedAlpha || k == QKind::RedNorm;
+}
+
+// a graph's reduction totals t: its scalars (and the outer convergence test)
+__device__ void q_scalars(const QOp &op, int g, const double (&t)[3], i64 ng, int it_offset) {
   switch (op.kind) {
     case QKind::RedSum:
       op.out[g] = t[0] / (double)ng;
@@ -227,54 +286,130 @@ __device__ void q_finalize(const QOp &op, int g, int nb, i64 ng, const double *p
   }
 }
 
+// the graph's operation is complete: sum the block partials in block order
+__device__ void q_finalize(const QOp &op, int g, int nb, i64 ng, const double *part,
+                           int it_offset) {
+  if (!q_is_reduction(op.kind)) return;
+  double t[3] = {0, 0, 0};
+  for (int b = 0; b < nb; b++)
+    for (int v = 0; v < 3; v++) t[v] += __ldcg(part + ((i64)g * kQueueMaxBlocks + b) * 3 + v);
+  q_scalars(op, g, t, ng, it_offset);
+}
+
+// Group item, reduction: a warp per graph (lane-strided sums, a fixed
+// shuffle tree), the graph's scalars written by lane 0.
+template <typename T>
+__device__ void q_reduce_group(const QOp &op, int glo, int cnt, const i64 *seg,
+                               const int *frozen, int it_offset) {
+  const T *x = (const T *)op.x0, *y = (const T *)op.x1, *w = (const T *)op.x2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int gi = warp; gi < cnt; gi += kQueueThreads / 32) {
+    const int g = glo + gi;
+    if (frozen[g]) continue;
+    double t[3] = {0, 0, 0};
+    for (i64 r = seg[g] + lane; r < seg[g + 1]; r += 32) {
+      const double xv = (double)x[r];
+      switch (op.kind) {
+        case QKind::RedSum:
+          t[0] += xv;
+          break;
+        case QKind::RedBeta:
+          t[0] += xv;
+          if (y) {
+            const double yv = (double)y[r];
+            t[1] += xv * yv;
+            t[2] += yv;
+          }
+          break;
+        case QKind::RedAlpha:
+          t[0] += xv * (double)y[r];
+          t[1] += xv * (double)w[r];
+          break;
+        default:
+          t[0] += xv * xv;
+          break;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int v = 0; v < 3; v++) t[v] += __shfl_xor_sync(0xffffffffu, t[v], o);
+    if (lane == 0) q_scalars(op, g, t, seg[g + 1] - seg[g], it_offset);
+  }
+}
+
+__device__ void q_group(const QOp &op, int glo, int cnt, const i64 *seg, const i32 *rowseg,
+                        const int *frozen, int it_offset) {
+  const i64 r0 = seg[glo], r1 = seg[glo + cnt];
+  if (q_is_reduction(op.kind)) {
+    if (op.dbl) q_reduce_group<double>(op, glo, cnt, seg, frozen, it_offset);
+    else q_reduce_group<float>(op, glo, cnt, seg, frozen, it_offset);
+  } else if (op.kind == QKind::Spmm) {
+    if (op.dbl) q_spmm<double>(op, op.Ad, r0, r1, rowseg, frozen);
+    else q_spmm<float>(op, op.Af, r0, r1, rowseg, frozen);
+  } else if (op.dbl || op.kind == QKind::ToFloat) {
+    q_elementwise_group<double>(op, r0, r1, seg, rowseg, frozen);
+  } else {
+    q_elementwise_group<float>(op, r0, r1, seg, rowseg, frozen);
+  }
+}
+
 __global__ void __launch_bounds__(kQueueThreads) k_queue(QueueArgs q) {
   __shared__ unsigned long long s_item;
   __shared__ int s_ctl, s_last;
   __shared__ double sh[3][kQueueThreads];
   const int tid = threadIdx.x;
+  volatile int *ev = &q.st->err;
   while (true) {
     if (tid == 0) {
-      int ctl = 0;  // 0: work, 1: the graph has converged (no work), 2: leave
       const unsigned long long t = atomicAdd(&q.st->ticket, 1ull);
-      if (t >= q.nitems) {
-        ctl = 2;
-      } else {
-        const unsigned long long it = q.items[t];
-        const int opi = (int)(it >> 40), g = (int)((it >> 20) & 0xfffff);
-        volatile int *pg = q.prog + g;
-        volatile int *ev = &q.st->err;
-        long long polls = 0;
-        while (*pg < opi) {
-          if (*ev) {
-            ctl = 2;
-            break;
-          }
-          if (++polls >= q.wait_limit) {
-            atomicExch(&q.st->err, 1);
-            ctl = 2;
-            break;
-          }
-          __nanosleep(64);
-        }
-        if (ctl == 0) {
-          __threadfence();
-          ctl = ((volatile const int *)q.frozen)[g] ? 1 : 0;
-        }
-        s_item = it;
-      }
-      s_ctl = ctl;
+      s_ctl = t >= q.nitems ? 2 : 0;  // 2: leave
+      if (t < q.nitems) s_item = q.items[t];
     }
     __syncthreads();
-    const int ctl = s_ctl;
-    if (ctl == 2) break;
+    if (s_ctl == 2) break;
     const unsigned long long it = s_item;
-    const int opi = (int)(it >> 40), g = (int)((it >> 20) & 0xfffff), b = (int)(it & 0xfffff);
+    const int opi = (int)(it >> 40), g = (int)((it >> 20) & 0xfffff);
+    const unsigned low = (unsigned)(it & 0xfffff);
+    const bool group = (low & kQueueGroup) != 0;
+    const int cnt = group ? (int)(low & (kQueueGroup - 1)) : 1;
+    // wait (bounded) until every graph of the item has finished the earlier
+    // operations; the threads share the graphs of a group
+    int bad = 0;
+    for (int gi = tid; gi < cnt; gi += kQueueThreads) {
+      volatile int *pg = q.prog + g + gi;
+      long long polls = 0;
+      while (*pg < opi) {
+        if (*ev) {
+          bad = 1;
+          break;
+        }
+        if (++polls >= q.wait_limit) {
+          atomicExch(&q.st->err, 1);
+          bad = 1;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (__syncthreads_or(bad)) break;
     const QOp &op = q.ops[opi];
     const i64 *seg = q.segs[op.seglev];
+    if (group) {
+      q_group(op, g, cnt, seg, q.rowsegs[op.seglev], (const int *)q.frozen, q.st->it_offset);
+      __threadfence();
+      __syncthreads();
+      if (tid < cnt) __threadfence();  // publish after the whole CTA's writes
+      for (int gi = tid; gi < cnt; gi += kQueueThreads) atomicExch(q.prog + g + gi, opi + 1);
+      continue;
+    }
+    const int b = (int)low;
+    const bool skip = ((volatile const int *)q.frozen)[g] != 0;
     const i64 g0 = seg[g], g1 = seg[g + 1];
     const i64 r0 = g0 + (i64)b * kQueueRows, r1 = min(g1, r0 + (i64)kQueueRows);
     const int nb = g1 > g0 ? (int)((g1 - g0 + kQueueRows - 1) / kQueueRows) : 1;
-    if (ctl == 0) q_item(op, g, b, r0, r1, g0, g1, q.part, sh);
+    if (!skip) q_item(op, g, b, r0, r1, g0, g1, q.part, sh);
     __syncthreads();
     if (tid == 0) {
       __threadfence();
@@ -283,7 +418,7 @@ __global__ void __launch_bounds__(kQueueThreads) k_queue(QueueArgs q) {
     __syncthreads();
     if (tid == 0 && s_last) {
       __threadfence();
-      if (ctl == 0) q_finalize(op, g, nb, g1 - g0, q.part, q.st->it_offset);
+      if (!skip) q_finalize(op, g, nb, g1 - g0, q.part, q.st->it_offset);
       q.blk[g] = 0;
       __threadfence();
       atomicExch(q.prog + g, opi + 1);

@@ -76,11 +76,19 @@ struct QueueState {
   int it_offset;  // outer iterations done before this launch (set by the host)
 };
 
+// An item is op << 40 | graph << 20 | low.  low < kQueueGroup: block `low`
+// of a graph with more than kQueueRows rows; low = kQueueGroup | c: the c
+// consecutive graphs from `graph`, every one with at most kQueueRows rows
+// and together at most kQueueRows (small graphs and coarse levels share an
+// item instead of taking one each).
+constexpr unsigned kQueueGroup = 1u << 19;
+
 struct QueueArgs {
   const QOp *ops = nullptr;
-  const unsigned long long *items = nullptr;  // op << 40 | graph << 20 | block
+  const unsigned long long *items = nullptr;
   unsigned long long nitems = 0;
-  const i64 *const *segs = nullptr;  // per level: nseg + 1 row offsets
+  const i64 *const *segs = nullptr;     // per level: nseg + 1 row offsets
+  const i32 *const *rowsegs = nullptr;  // per level: the graph of every row
   int nseg = 0;
   int *prog = nullptr;      // nseg
   int *blk = nullptr;       // nseg
