@@ -581,7 +581,6 @@ struct QueueRun {
   int prec = -1;
   QueueProgram first, more;
   DBuf<const i64 *> segs;
-  DBuf<const i32 *> rowsegs;
   DBuf<int> prog, blk;
   DBuf<double> part;
   DBuf<QueueState> st;
@@ -2787,35 +2786,37 @@ void queue_record(Handle &H, Work<T> &W, OuterWork &w, size_t base, int it0, Que
   QueueBuilder<T> B(H, W, w);
   for (int it = it0; it < it0 + kQueueIters; it++) B.outer(base, it);
   const i64 ns = H.h[base]->seginfo().nseg;
+  const size_t nops = B.ops.size();
+  // Items per graph: a block item per row block of an operation where the
+  // graph has more than kQueueRows rows, and one chain item for every run of
+  // consecutive operations where it has fewer.  Sorted (first operation,
+  // graph, block), every item depends only on items with smaller tickets.
   std::vector<unsigned long long> items;
-  for (size_t i = 0; i < B.ops.size(); i++) {
-    const std::vector<i64> &sg = H.h[B.ops[i].seglev]->seg_host;
-    const unsigned long long head = (unsigned long long)i << 40;
-    i64 g = 0;
-    while (g < ns) {
-      const i64 rows = sg[g + 1] - sg[g];
-      if (rows > kQueueRows) {  // a large graph: one item per row block
-        const i64 nb = cdiv(rows, kQueueRows);
+  for (i64 g = 0; g < ns; g++) {
+    auto rows = [&](size_t i) {
+      const std::vector<i64> &sg = H.h[B.ops[i].seglev]->seg_host;
+      return sg[g + 1] - sg[g];
+    };
+    size_t i = 0;
+    while (i < nops) {
+      const i64 r = rows(i);
+      if (r > kQueueRows) {
+        const i64 nb = cdiv(r, kQueueRows);
         if (nb > kQueueMaxBlocks)
           throw Error(LIGMG_ERR_UNSUPPORTED, "a graph of the batch is too large for the work queue");
         for (i64 b = 0; b < nb; b++)
-          items.push_back(head | ((unsigned long long)g << 20) | (unsigned long long)b);
-        g++;
+          items.push_back(((unsigned long long)i << 40) | ((unsigned long long)g << 20) |
+                          (unsigned long long)b);
+        i++;
         continue;
       }
-      // consecutive small graphs share an item (at most kQueueRows rows)
-      const i64 g0 = g;
-      i64 tot = 0;
-      while (g < ns && g - g0 < (i64)kQueueGroup - 1) {
-        const i64 r = sg[g + 1] - sg[g];
-        if (r > kQueueRows || (g > g0 && tot + r > kQueueRows)) break;
-        tot += r;
-        g++;
-      }
-      items.push_back(head | ((unsigned long long)g0 << 20) | kQueueGroup |
-                      (unsigned long long)(g - g0));
+      const size_t i0 = i;
+      while (i < nops && rows(i) <= kQueueRows && i - i0 < (size_t)kQueueChain - 1) i++;
+      items.push_back(((unsigned long long)i0 << 40) | ((unsigned long long)g << 20) |
+                      kQueueChain | (unsigned long long)(i - i0));
     }
   }
+  std::sort(items.begin(), items.end());
   if (B.ops.size() >= ((size_t)1 << 23) || ns >= ((i64)1 << 20))
     throw Error(LIGMG_ERR_UNSUPPORTED, "batch program too large for the work queue");
   P.ops.alloc((i64)B.ops.size(), H.s);
@@ -2858,15 +2859,9 @@ SolveResult outer_solve_queue(Handle &H, size_t base, OuterWork &w) {
     Q.base = base;
     Q.prec = prec;
     std::vector<const i64 *> segs;
-    std::vector<const i32 *> rowsegs;
-    for (auto &lv : H.h) {
-      segs.push_back(lv->segptr.p);
-      rowsegs.push_back(lv->rowseg.p);
-    }
+    for (auto &lv : H.h) segs.push_back(lv->segptr.p);
     Q.segs.alloc((i64)segs.size(), s);
     Q.segs.upload(segs.data(), (i64)segs.size());
-    Q.rowsegs.alloc((i64)rowsegs.size(), s);
-    Q.rowsegs.upload(rowsegs.data(), (i64)rowsegs.size());
     Q.prog.alloc(ns, s);
     Q.blk.alloc(ns, s);
     Q.part.alloc(ns * kQueueMaxBlocks * 3, s);
@@ -2882,7 +2877,6 @@ SolveResult outer_solve_queue(Handle &H, size_t base, OuterWork &w) {
     a.items = P.items.p;
     a.nitems = P.nitems;
     a.segs = Q.segs.p;
-    a.rowsegs = Q.rowsegs.p;
     a.nseg = (int)ns;
     a.prog = Q.prog.p;
     a.blk = Q.blk.p;

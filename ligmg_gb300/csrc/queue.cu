@@ -17,16 +17,15 @@ namespace {
 using namespace dev;
 
 // rows [r0, r1) of y = A X with a fused epilogue, G lanes per row (k = 1)
-// rowseg/frozen (group items): rows of converged graphs are skipped
 template <typename T, int G, Epi EP>
 __device__ void q_spmm_rows(const MatView<T> &A, const T *__restrict__ X, const EpiArgs &a,
-                            i64 r0, i64 r1, const i32 *rowseg, const int *frozen) {
+                            i64 r0, i64 r1) {
   constexpr int RPW = 32 / G;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int grp = lane / G, slot = lane % G;
   for (i64 base = r0 + (i64)warp * RPW; base < r1; base += (kQueueThreads / 32) * RPW) {
     const i64 r = base + grp;
-    const bool act = r < r1 && !(rowseg && frozen[rowseg[r]]);
+    const bool act = r < r1;
     T acc[1] = {(T)0};
     if (act) row_accumulate<T, 1, 1, G, true, EP == Epi::Split>(A, X, A.rp[r] + slot, A.rp[r + 1], 0, acc);
     reduce_slots<T, 1, 1, G>(acc);
@@ -35,14 +34,13 @@ __device__ void q_spmm_rows(const MatView<T> &A, const T *__restrict__ X, const 
 }
 
 template <typename T>
-__device__ void q_spmm(const QOp &op, const MatView<T> &A, i64 r0, i64 r1, const i32 *rowseg,
-                       const int *frozen) {
+__device__ void q_spmm(const QOp &op, const MatView<T> &A, i64 r0, i64 r1) {
   const T *X = (const T *)op.x0;
   switch (op.epi) {
 #define LG_Q_EPI(E)                                                               \
   case E:                                                                         \
-    if (op.lanes == 8) q_spmm_rows<T, 8, E>(A, X, op.a, r0, r1, rowseg, frozen);  \
-    else q_spmm_rows<T, 32, E>(A, X, op.a, r0, r1, rowseg, frozen);               \
+    if (op.lanes == 8) q_spmm_rows<T, 8, E>(A, X, op.a, r0, r1);                  \
+    else q_spmm_rows<T, 32, E>(A, X, op.a, r0, r1);                               \
     break;
     LG_Q_EPI(Epi::Store)
     LG_Q_EPI(Epi::Resid)
@@ -101,66 +99,6 @@ __device__ void q_reduce(const QOp &op, i64 r0, i64 r1, double *dst,
   if (t == 0)
 #pragma unroll
     for (int v = 0; v < 3; v++) dst[v] = sh[v][0];
-}
-
-// Elementwise operations on rows [r0, r1).  Single graph g (rowseg null):
-// its columns are [g0, g1).  Group (rowseg set): each row's graph from
-// rowseg, rows of converged graphs skipped, columns from seg.
-template <typename T>
-__device__ void q_elementwise_group(const QOp &op, i64 r0, i64 r1, const i64 *seg,
-                                   const i32 *rowseg, const int *frozen) {
-  T *y0 = (T *)op.y0;
-  const T *x0 = (const T *)op.x0, *x1 = (const T *)op.x1;
-  for (i64 r = r0 + threadIdx.x; r < r1; r += kQueueThreads) {
-    const int g = rowseg[r];
-    if (frozen[g]) continue;
-    switch (op.kind) {
-      case QKind::Cheb0:
-        y0[r] = (x1[r] * (T)op.f) * x0[r];
-        break;
-      case QKind::Prolong:
-        y0[r] += x0[op.idx[r]];
-        break;
-      case QKind::Coarse: {
-        T s = 0;
-        for (i64 j = seg[g]; j < seg[g + 1]; j++) s += x1[r * op.n + j] * x0[j];
-        y0[r] = s;
-        break;
-      }
-      case QKind::Scale:
-        y0[r] = y0[r] * (T)op.f;
-        break;
-      case QKind::Zero:
-        y0[r] = (T)0;
-        break;
-      case QKind::Copy:
-        y0[r] = x0[r];
-        break;
-      case QKind::SubMean:
-        y0[r] = (T)((double)y0[r] - ((const double *)op.x1)[g]);
-        break;
-      case QKind::Dir: {
-        T v = x0[r] - (T)op.sc.mu[g];
-        if (x1) v = v - (T)op.sc.beta[g] * x1[r];
-        y0[r] = v;
-        break;
-      }
-      case QKind::Update: {
-        const T al = (T)op.sc.alpha[g];
-        y0[r] = y0[r] + al * x0[r];
-        if (op.flag) ((T *)op.y1)[r] = ((T *)op.y1)[r] - al * x1[r];
-        break;
-      }
-      case QKind::ToFloat:
-        ((float *)op.y0)[r] = (float)((const double *)op.x0)[r];
-        break;
-      case QKind::ToDouble:
-        ((double *)op.y0)[r] = (double)((const float *)op.x0)[r];
-        break;
-      default:
-        break;
-    }
-  }
 }
 
 template <typename T>
@@ -228,8 +166,8 @@ __device__ void q_item(const QOp &op, int g, int b, i64 r0, i64 r1, i64 g0, i64 
                        double *part, double (*sh)[kQueueThreads]) {
   switch (op.kind) {
     case QKind::Spmm:
-      if (op.dbl) q_spmm<double>(op, op.Ad, r0, r1, nullptr, nullptr);
-      else q_spmm<float>(op, op.Af, r0, r1, nullptr, nullptr);
+      if (op.dbl) q_spmm<double>(op, op.Ad, r0, r1);
+      else q_spmm<float>(op, op.Af, r0, r1);
       break;
     case QKind::ToFloat:
       for (i64 r = r0 + threadIdx.x; r < r1; r += kQueueThreads)
@@ -296,64 +234,6 @@ __device__ void q_finalize(const QOp &op, int g, int nb, i64 ng, const double *p
   q_scalars(op, g, t, ng, it_offset);
 }
 
-// Group item, reduction: a warp per graph (lane-strided sums, a fixed
-// shuffle tree), the graph's scalars written by lane 0.
-template <typename T>
-__device__ void q_reduce_group(const QOp &op, int glo, int cnt, const i64 *seg,
-                               const int *frozen, int it_offset) {
-  const T *x = (const T *)op.x0, *y = (const T *)op.x1, *w = (const T *)op.x2;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int gi = warp; gi < cnt; gi += kQueueThreads / 32) {
-    const int g = glo + gi;
-    if (frozen[g]) continue;
-    double t[3] = {0, 0, 0};
-    for (i64 r = seg[g] + lane; r < seg[g + 1]; r += 32) {
-      const double xv = (double)x[r];
-      switch (op.kind) {
-        case QKind::RedSum:
-          t[0] += xv;
-          break;
-        case QKind::RedBeta:
-          t[0] += xv;
-          if (y) {
-            const double yv = (double)y[r];
-            t[1] += xv * yv;
-            t[2] += yv;
-          }
-          break;
-        case QKind::RedAlpha:
-          t[0] += xv * (double)y[r];
-          t[1] += xv * (double)w[r];
-          break;
-        default:
-          t[0] += xv * xv;
-          break;
-      }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-      for (int v = 0; v < 3; v++) t[v] += __shfl_xor_sync(0xffffffffu, t[v], o);
-    if (lane == 0) q_scalars(op, g, t, seg[g + 1] - seg[g], it_offset);
-  }
-}
-
-__device__ void q_group(const QOp &op, int glo, int cnt, const i64 *seg, const i32 *rowseg,
-                        const int *frozen, int it_offset) {
-  const i64 r0 = seg[glo], r1 = seg[glo + cnt];
-  if (q_is_reduction(op.kind)) {
-    if (op.dbl) q_reduce_group<double>(op, glo, cnt, seg, frozen, it_offset);
-    else q_reduce_group<float>(op, glo, cnt, seg, frozen, it_offset);
-  } else if (op.kind == QKind::Spmm) {
-    if (op.dbl) q_spmm<double>(op, op.Ad, r0, r1, rowseg, frozen);
-    else q_spmm<float>(op, op.Af, r0, r1, rowseg, frozen);
-  } else if (op.dbl || op.kind == QKind::ToFloat) {
-    q_elementwise_group<double>(op, r0, r1, seg, rowseg, frozen);
-  } else {
-    q_elementwise_group<float>(op, r0, r1, seg, rowseg, frozen);
-  }
-}
-
 __global__ void __launch_bounds__(kQueueThreads) k_queue(QueueArgs q) {
   __shared__ unsigned long long s_item;
   __shared__ int s_ctl, s_last;
@@ -371,13 +251,12 @@ __global__ void __launch_bounds__(kQueueThreads) k_queue(QueueArgs q) {
     const unsigned long long it = s_item;
     const int opi = (int)(it >> 40), g = (int)((it >> 20) & 0xfffff);
     const unsigned low = (unsigned)(it & 0xfffff);
-    const bool group = (low & kQueueGroup) != 0;
-    const int cnt = group ? (int)(low & (kQueueGroup - 1)) : 1;
-    // wait (bounded) until every graph of the item has finished the earlier
-    // operations; the threads share the graphs of a group
+    const bool chain = (low & kQueueChain) != 0;
+    const int cnt = chain ? (int)(low & (kQueueChain - 1)) : 1;
+    // wait (bounded) until the graph has finished the earlier operations
     int bad = 0;
-    for (int gi = tid; gi < cnt; gi += kQueueThreads) {
-      volatile int *pg = q.prog + g + gi;
+    if (tid == 0) {
+      volatile int *pg = q.prog + g;
       long long polls = 0;
       while (*pg < opi) {
         if (*ev) {
@@ -394,16 +273,26 @@ __global__ void __launch_bounds__(kQueueThreads) k_queue(QueueArgs q) {
     }
     __threadfence();
     if (__syncthreads_or(bad)) break;
-    const QOp &op = q.ops[opi];
-    const i64 *seg = q.segs[op.seglev];
-    if (group) {
-      q_group(op, g, cnt, seg, q.rowsegs[op.seglev], (const int *)q.frozen, q.st->it_offset);
-      __threadfence();
-      __syncthreads();
-      if (tid < cnt) __threadfence();  // publish after the whole CTA's writes
-      for (int gi = tid; gi < cnt; gi += kQueueThreads) atomicExch(q.prog + g + gi, opi + 1);
+    if (chain) {
+      // one graph's consecutive single-block operations, back to back
+      for (int i = opi; i < opi + cnt; i++) {
+        const QOp &op = q.ops[i];
+        const i64 *seg = q.segs[op.seglev];
+        const i64 g0 = seg[g], g1 = seg[g + 1];
+        const bool skip = ((volatile const int *)q.frozen)[g] != 0;
+        if (!skip) q_item(op, g, 0, g0, g1, g0, g1, q.part, sh);
+        __syncthreads();
+        if (tid == 0 && !skip) q_finalize(op, g, 1, g1 - g0, q.part, q.st->it_offset);
+        __syncthreads();
+      }
+      if (tid == 0) {
+        __threadfence();
+        atomicExch(q.prog + g, opi + cnt);
+      }
       continue;
     }
+    const QOp &op = q.ops[opi];
+    const i64 *seg = q.segs[op.seglev];
     const int b = (int)low;
     const bool skip = ((volatile const int *)q.frozen)[g] != 0;
     const i64 g0 = seg[g], g1 = seg[g + 1];

@@ -7,13 +7,15 @@
 // on one level's rows, and the batch's graphs own disjoint, contiguous row
 // ranges of every level (no aggregate, elimination or coarse block crosses
 // graphs), so an operation splits into (graph, row-block) work items that
-// depend only on the same graph's previous operation.  The items, ordered
-// operation-major then graph then block, form the queue; a cooperative launch
-// of resident CTAs takes them from one atomic ticket.  Before working on an
-// item a CTA waits (bounded) until its graph has finished the previous
-// operation; the CTA finishing a graph's last block of an operation sums that
-// operation's block partials in block order (reductions) and advances the
-// graph's progress counter.  Graphs therefore move through the program
+// depend only on the same graph's previous operation.  Where a graph's rows
+// fit one block (its coarse levels, small graphs), its consecutive operations
+// form one chain item run back to back by a single CTA.  The items, ordered
+// by first operation, then graph, then block, form the queue; a cooperative
+// launch of resident CTAs takes them from one atomic ticket.  Before working
+// on an item a CTA waits (bounded) until its graph has finished the earlier
+// operations; the CTA finishing a graph's last block of an operation sums
+// that operation's block partials in block order (reductions) and advances
+// the graph's progress counter.  Graphs therefore move through the program
 // independently, each stopping work as soon as it has converged.
 #pragma once
 #include "solve.cuh"
@@ -76,19 +78,19 @@ struct QueueState {
   int it_offset;  // outer iterations done before this launch (set by the host)
 };
 
-// An item is op << 40 | graph << 20 | low.  low < kQueueGroup: block `low`
-// of a graph with more than kQueueRows rows; low = kQueueGroup | c: the c
-// consecutive graphs from `graph`, every one with at most kQueueRows rows
-// and together at most kQueueRows (small graphs and coarse levels share an
-// item instead of taking one each).
-constexpr unsigned kQueueGroup = 1u << 19;
+// An item is op << 40 | graph << 20 | low.  low < kQueueChain: block `low`
+// of operation `op` for a graph with more than kQueueRows rows there;
+// low = kQueueChain | c: the c consecutive operations from `op` during which
+// the graph's rows fit one block, run back to back by one CTA (the graph's
+// coarse levels: thousands of small dependent operations with no hand-off
+// between CTAs).
+constexpr unsigned kQueueChain = 1u << 19;
 
 struct QueueArgs {
   const QOp *ops = nullptr;
   const unsigned long long *items = nullptr;
   unsigned long long nitems = 0;
-  const i64 *const *segs = nullptr;     // per level: nseg + 1 row offsets
-  const i32 *const *rowsegs = nullptr;  // per level: the graph of every row
+  const i64 *const *segs = nullptr;  // per level: nseg + 1 row offsets
   int nseg = 0;
   int *prog = nullptr;      // nseg
   int *blk = nullptr;       // nseg
