@@ -278,11 +278,13 @@ def spmv_roofline(S64, stream, peak, peak_kind, reps=20):
         run()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nvtx_push("spmv_roofline")
     e0.record(stream)
     for _ in range(reps):
         run()
     e1.record(stream)
     torch.cuda.synchronize()
+    nvtx_pop()
     sec = e0.elapsed_time(e1) / 1e3 / reps
     byt = 8.0 * (n + 1) + 12.0 * nnz + 16.0 * n
     traffic = SPMV_DRAM_BYTES_PER_NNZ * nnz if SPMV_DRAM_BYTES_PER_NNZ else None
@@ -564,6 +566,7 @@ def run_ours(args):
                         f"symmetrised, LCC; w~U(0.5,2)) n={n} nnz={L.nnz}; K-cycle + elimination; "
                         f"FP32 hierarchy in FP64 FCG; rtol 1e-8; k={k} RHS per step",
             "k": k, "rhs_per_s": 1e3 / value, "setup_s": setup_s,
+            "setup_phases_s": S.setup_times(),
             "first_solve_s": first_s, "autotune": True,
             "iters": iters, "converged": converged, "max_true_rel_residual": true_res,
             "levels": len(levels), "level_n": [l["n"] for l in levels],

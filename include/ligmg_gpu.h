@@ -255,6 +255,20 @@ typedef struct ligmg_level_desc {
 ligmg_status ligmg_import_hierarchy(int32_t num_levels, const ligmg_level_desc *levels,
                                     const ligmg_options *opts, ligmg_handle *out);
 
+/* Wall time of the setup phases (no reference counterpart; the reference
+ * times the whole setup with MPI_Wtime, multigrid.hpp:183,260).  Each phase
+ * ends with the handle's stream drained; seconds[LIGMG_SETUP_NPHASES]. */
+#define LIGMG_SETUP_VALIDATE 0     /* upload and input checks */
+#define LIGMG_SETUP_ELIMINATION 1  /* low-degree elimination selection and P/Q/R */
+#define LIGMG_SETUP_AGGREGATION 2  /* test vectors, strength, voting, aggregate ids */
+#define LIGMG_SETUP_GALERKIN 3     /* coarse matrices (RAP) */
+#define LIGMG_SETUP_SOLVE_DATA 4   /* inverse diagonals, row sums, restriction
+                                      matrices, single right-hand-side plans */
+#define LIGMG_SETUP_SMOOTHER 5     /* Chebyshev eigenvalue estimates */
+#define LIGMG_SETUP_COARSE 6       /* dense coarse pseudo-inverse */
+#define LIGMG_SETUP_NPHASES 7
+ligmg_status ligmg_setup_times(ligmg_handle h, double *seconds);
+
 /* Largest eigenvalue estimate of D^-1 A used by the level's Chebyshev smoother. */
 ligmg_status ligmg_level_lmax(ligmg_handle h, int32_t level, double *lmax);
 

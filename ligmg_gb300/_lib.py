@@ -80,6 +80,7 @@ def lib(path=None):
     L.ligmg_batch_create.argtypes = [C.c_int32, vp, vp, vp, vp, P(Options), P(vp)]
     L.ligmg_batch_solve.argtypes = [vp, vp, vp, vp, vp, P(Info)]
     L.ligmg_backward.argtypes = [vp, vp, vp, vp, P(Info)]
+    L.ligmg_setup_times.argtypes = [vp, P(C.c_double)]
     for name in header_functions():
         if name not in ("ligmg_default_options", "ligmg_status_string"):
             getattr(L, name).restype = C.c_int

@@ -681,6 +681,7 @@ struct ligmg_handle_s {
   std::vector<std::unique_ptr<lg::Level>> h;
   lg::i64 nnz0 = 0;
   double setup_s = 0;
+  double setup_phase[LIGMG_SETUP_NPHASES] = {0};  // seconds per setup phase
   std::map<int, std::unique_ptr<lg::Work<float>>> w32;
   std::map<int, std::unique_ptr<lg::Work<double>>> w64;
   std::map<int, std::unique_ptr<lg::OuterWork>> ow;
@@ -1941,17 +1942,29 @@ void make_hierarchy(Handle &H, i64 n, const i64 *rowptr, const i32 *col, const d
   ap.rejection_ratio = o.rejection_ratio;
   ap.rejection_to_seed = o.rejection_to_seed != 0;
   auto &h = H.h;
+  // per-phase wall time (the stream is drained at each phase boundary)
+  auto tp = std::chrono::steady_clock::now();
+  auto phase = [&](int ph) {
+    LG_CUDA(cudaStreamSynchronize(s));
+    auto t = std::chrono::steady_clock::now();
+    H.setup_phase[ph] += std::chrono::duration<double>(t - tp).count();
+    tp = t;
+  };
+  phase(LIGMG_SETUP_VALIDATE);
   while ((int)h.size() < o.max_levels && (h.empty() || h.back()->A.nnz > o.min_size)) {
     if (o.always_elim && o.elim_iters >= 1) {
       auto E = std::make_unique<Level>();
       E->type = LIGMG_LEVEL_ELIM;
       gpu_elimination(cur, o.elim_degree, o.elim_factor, E->elim, s);
+      phase(LIGMG_SETUP_ELIMINATION);
       if (E->elim.accepted) {
         DCsr<double> next;
         gpu_galerkin(cur, E->elim.P, next, s);
+        phase(LIGMG_SETUP_GALERKIN);
         E->A = std::move(cur);
         E->nc = E->elim.nc;
         finish_level(H, *E);
+        phase(LIGMG_SETUP_SOLVE_DATA);
         attach(*E);
         next_offsets(*E, E->elim.pos.p, E->nc);
         h.push_back(std::move(E));
@@ -1975,16 +1988,21 @@ void make_hierarchy(Handle &H, i64 n, const i64 *rowptr, const i32 *col, const d
         for (i64 i = 0; i < cn; i++) x[i] = x[i] - sm;
       }
     }
+    phase(LIGMG_SETUP_AGGREGATION);  // the host's test vectors count here
     gpu_aggregation(cur, ap, tvs.data(), G->agg, s);
     G->nc = G->agg.nc;
+    phase(LIGMG_SETUP_AGGREGATION);
     DCsr<double> next;
     gpu_galerkin_agg(cur, G->agg.agg.p, G->nc, next, s);
+    phase(LIGMG_SETUP_GALERKIN);
     G->A = std::move(cur);
     finish_level(H, *G);
     attach(*G);
     next_offsets(*G, G->agg.rank.p, G->nc);
+    phase(LIGMG_SETUP_SOLVE_DATA);
     estimate_lmax(H, *G);
     setup_smoother_params(o, *G);
+    phase(LIGMG_SETUP_SMOOTHER);
     h.push_back(std::move(G));
     cur = std::move(next);
   }
@@ -1995,6 +2013,7 @@ void make_hierarchy(Handle &H, i64 n, const i64 *rowptr, const i32 *col, const d
   st = gpu_coarse_pinv(C->A, C->pinv, s, nseg ? C->rowseg.p : nullptr,
                        nseg ? C->segptr.p : nullptr);
   if (st != LIGMG_OK) throw Error(st, "coarse pseudo-inverse");
+  phase(LIGMG_SETUP_COARSE);
   finish_level(H, *C);
   h.push_back(std::move(C));
   LG_CUDA(cudaStreamSynchronize(s));
@@ -3715,6 +3734,12 @@ ligmg_status ligmg_level_ids(ligmg_handle h, int32_t level, int32_t *ids) {
     LG_CUDA(cudaStreamSynchronize(h->s));
     return LIGMG_OK;
   });
+}
+
+ligmg_status ligmg_setup_times(ligmg_handle h, double *seconds) {
+  if (!h || !seconds) return LIGMG_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < LIGMG_SETUP_NPHASES; i++) seconds[i] = h->setup_phase[i];
+  return LIGMG_OK;
 }
 
 ligmg_status ligmg_level_lmax(ligmg_handle h, int32_t level, double *lmax) {

@@ -128,6 +128,15 @@ class Solver:
         check(lib().ligmg_level_ids(self._h, level, _p(ids)))
         return ids
 
+    SETUP_PHASES = ("validate", "elimination", "aggregation", "galerkin", "solve_data",
+                    "smoother", "coarse")
+
+    def setup_times(self):
+        """Seconds per setup phase (ligmg_setup_times)."""
+        arr = (C.c_double * len(self.SETUP_PHASES))()
+        check(lib().ligmg_setup_times(self._h, arr))
+        return dict(zip(self.SETUP_PHASES, list(arr)))
+
     def level_lmax(self, level):
         x = C.c_double()
         check(lib().ligmg_level_lmax(self._h, level, C.byref(x)))
