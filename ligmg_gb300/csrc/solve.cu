@@ -231,9 +231,12 @@ __device__ __forceinline__ void tile_unit(const MatView<T> &A, const T *__restri
   const int r0 = d.x, nr = d.y, e_rel = d.z;
   const i64 ab = (i64)d.w << 2;
   const int lb = lane * U;
-  // this lane's 16 row-start bits
-  const u32 word =
-      (__ldg(A.tbits + t * (kTilePos / 32) + (lane >> 1)) >> ((lane & 1) * 16)) & 0xffffu;
+  // this lane's U row-start bits
+  static_assert(U == 32 || U == 16 || U == 8 || U == 4, "entries per lane");
+  const int wbit = lane * U;
+  const u32 word = U == 32 ? __ldg(A.tbits + t * (kTilePos / 32) + lane)
+                           : (__ldg(A.tbits + t * (kTilePos / 32) + (wbit >> 5)) >> (wbit & 31)) &
+                                 ((1u << (U & 31)) - 1u);
   i32 c[U];
   T v[U];
 #pragma unroll
@@ -265,7 +268,7 @@ __device__ __forceinline__ void tile_unit(const MatView<T> &A, const T *__restri
   const int s_rel = __ffs(__shfl_sync(0xffffffffu, word, 0)) - 1;  // the tile's first entry
   const int lo = max(s_rel - lb, 0), hi = min(e_rel - lb, U);
   u32 okm = 0;  // this lane's entries of the tile
-  if (hi > lo) okm = ((1u << hi) - 1u) & ~((1u << lo) - 1u);
+  if (hi > lo) okm = (hi >= 32 ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
   T xv[U];
 #pragma unroll
   for (int j = 0; j < U; j++)

@@ -69,8 +69,11 @@ struct HubPlan {
 // Single right-hand side tile layout: at most kTilePos entries (counted from
 // the tile's first entry rounded down to a multiple of four) and kTileRows
 // rows per tile; a warp takes a tile, a lane 16 consecutive entries.
-constexpr int kTilePos = 512;
-constexpr int kTileRows = 64;
+#ifndef LG_TILE_POS
+#define LG_TILE_POS 512
+#endif
+constexpr int kTilePos = LG_TILE_POS;      // a multiple of 128 (4 entries per lane at least)
+constexpr int kTileRows = kTilePos / 8;
 // worthwhile from this many nonzeros per row on average
 constexpr double kTileMinMeanRow = 6.0;
 // Hub split unit U for k right-hand sides: the nonzeros a 32-lane group
