@@ -149,7 +149,7 @@ typedef struct ligmg_options {
   int32_t spmv_tiles;         /* 1 (default): single right-hand-side products
                                  of matrices averaging at least six entries
                                  per row use the nonzero-balanced tile layout
-                                 (a warp per tile of whole rows, a lane per 16
+                                 (a warp per tile of whole rows, a lane per 8
                                  consecutive entries); 0: one group of lanes
                                  per row */
   int64_t wait_spins;         /* polls of an incomplete barrier before a

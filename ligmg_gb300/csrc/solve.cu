@@ -154,20 +154,20 @@ __global__ void __launch_bounds__(256, 6) k_spmm(const MatView<T> A, const T *__
 // FP64 instruction holds the SM's FP64 pipe for ~16 clocks whatever its
 // active mask; a warp per row spends a five-step shuffle reduction and a
 // lane-0 epilogue (a dozen such instructions) on every row.  Here a warp
-// takes a tile of whole rows (at most kTilePos entries), a lane 16
+// takes a tile of whole rows (at most kTilePos entries), a lane kTilePos / 32
 // consecutive entries accumulated with one FMA each; rows crossing lanes are
 // combined by one segmented scan over the warp (five FP64 adds per tile),
 // complete row sums go to shared memory and the epilogue runs one row per
 // lane.  Every load of a tile (descriptor aside) is independent of the
 // others: one round trip brings the column indices, values and row-start
 // bits (16-byte vector loads that do not allocate in L1, so L1 keeps the
-// gathered vector), a second one all 16 gathers of a lane, and the
+// gathered vector), a second one all the gathers of a lane, and the
 // epilogue's inputs are prefetched into L1 before the gathers.  Summation
 // order: within a lane in entry order, across lanes by the scan's fixed tree.
 constexpr int kTileLane = kTilePos / 32;  // entries per lane
 constexpr int kTileWarps = 8;             // warps per block
 #ifndef LG_TILE_MIN_BLOCKS
-#define LG_TILE_MIN_BLOCKS 3  // resident blocks per SM the register budget is set for
+#define LG_TILE_MIN_BLOCKS 6  // resident blocks per SM the register budget is set for
 #endif
 
 __device__ __forceinline__ int4 ld_stream_i4(const i32 *p) {

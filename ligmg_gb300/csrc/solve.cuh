@@ -68,9 +68,9 @@ struct HubPlan {
 };
 // Single right-hand side tile layout: at most kTilePos entries (counted from
 // the tile's first entry rounded down to a multiple of four) and kTileRows
-// rows per tile; a warp takes a tile, a lane 16 consecutive entries.
+// rows per tile; a warp takes a tile, a lane 8 consecutive entries.
 #ifndef LG_TILE_POS
-#define LG_TILE_POS 512
+#define LG_TILE_POS 256
 #endif
 constexpr int kTilePos = LG_TILE_POS;      // a multiple of 128 (4 entries per lane at least)
 constexpr int kTileRows = kTilePos / 8;

@@ -1,5 +1,5 @@
 """Single right-hand-side products in the tile layout (spmv_tiles = 1: a warp
-per tile of whole rows, a lane per 16 consecutive entries, a segmented scan
+per tile of whole rows, a lane per 8 consecutive entries, a segmented scan
 across lanes) against the row layout (spmv_tiles = 0) and scipy, on every
 level of graphs with ragged, hub and short rows.  FP64 bar: 1e-12 relative to
 the largest |y|; the solves must converge in the same number of iterations
