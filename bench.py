@@ -658,13 +658,21 @@ def run_grid3d(args):
     S64.set_stream(stream.cuda_stream)
     b1 = [torch.from_numpy(G.rhs(L.n, seed=3)).to(dev).reshape(L.n, 1).contiguous()]
     ms64, inf64 = _timed_solves(S64, stream, b1, 1, 3, 1)
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        ms_c, osetup, oit, _, _ = cpu_baseline_oracle(L, G.rhs(L.n, seed=3), threads)
+        cpu = {"value": ms_c, "unit": "ms/RHS", "cores": threads, "kind": "port",
+               "sample": f"1 RHS, FP64 K-cycle FCG to rtol 1e-8 by the oracle, {oit} "
+                         f"iterations; oracle setup {osetup:.1f}s untimed"}
     out = {"metric": METRIC, "value": per_k[32]["ms_per_rhs"], "unit": "ms/RHS", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_k[32]["ms_per_rhs"] * 32,
            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
            "dtype": "fp32 cycle / fp64 outer", "data": "synthetic",
            "config": {"workload": f"grid3d {args.grid}^3 7-point, lognormal(0,1) weights, n={L.n} "
                                   f"nnz={L.nnz}; FP32 hierarchy, K-cycle, FCG rtol 1e-8",
-                      "per_k": per_k, "fp64_single_ms_per_rhs": ms64 / 3}}
+                      "per_k": per_k, "fp64_single_ms_per_rhs": ms64 / 3},
+           "cpu_baseline": cpu}
     print(json.dumps(out), flush=True)
 
 
@@ -711,7 +719,21 @@ def run_rgg_batch(args):
         if q == 1:
             xs_q = xs
         B.close()
-    O.set_threads(os.cpu_count() or 1)
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    cpu = None
+    if not args.no_cpu_baseline:
+        pick = np.random.default_rng(1).choice(len(gs), 8, replace=False)
+        t_cpu = 0.0
+        for g in pick:
+            R = O.OracleSolver(gs[g], kcycle=1, outer_ksp_type="fcg")
+            t0 = time.perf_counter()
+            R.solve(bs[g])
+            t_cpu += time.perf_counter() - t0
+        cpu = {"value": 1e3 * t_cpu / len(pick), "unit": "ms/RHS", "cores": threads,
+               "kind": "port", "sample": "8 random graphs of the batch, each one FP64 K-cycle FCG "
+                                         "solve to rtol 1e-8 by the oracle (setup untimed), "
+                                         "ms per graph"}
     order = np.argsort([g.n for g in gs])
     sample = [int(order[0]), int(order[len(order) // 2]), int(order[-1])]
     parity = {}
@@ -730,6 +752,7 @@ def run_rgg_batch(args):
                                   f"one RHS each; host-timed ligmg_batch_solve incl. H2D/D2H",
                       "vertices": int(sum(g.n for g in gs)), "nnz": int(sum(g.nnz for g in gs)),
                       "generation_s": gen_s, "arms": arms, "parity_vs_oracle": parity},
+           "cpu_baseline": cpu,
            "e2e": {"value": value, "unit": "ms/RHS",
                    "h2d_bytes_per_step": 8 * int(sum(g.n for g in gs)),
                    "d2h_bytes_per_step": 8 * int(sum(g.n for g in gs))}}
@@ -894,10 +917,12 @@ def run_adjoint(args):
     # the oracle's own solves: x, then lambda = L^+ (x - x_t)
     O.set_threads(os.cpu_count() or 1)
     R = O.OracleSolver(L, **kw)
+    t0 = time.perf_counter()
     xo, _ = R.solve(b)
     xo -= xo.mean()
     lam, _ = R.solve(xo - xt)
     lam -= lam.mean()
+    cpu_ms = (time.perf_counter() - t0) * 1e3
     gw_o = -(xo[u] - xo[v]) * (lam[u] - lam[v])
     rw, rb = rel(fd_w, gw[ew]), rel(fd_b, gb[ib])
     out = {"metric": "gradient of 0.5||x - x_t||^2 through the solve: ms per forward+backward",
@@ -917,7 +942,10 @@ def run_adjoint(args):
                       "vs_oracle_gradient_rel_err": float(np.linalg.norm(gw - gw_o) /
                                                           np.linalg.norm(gw_o)),
                       "vs_oracle_db_rel_err": float(np.linalg.norm(gb - lam) / np.linalg.norm(lam)),
-                      "fd_seconds": fd_s}}
+                      "fd_seconds": fd_s},
+           "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": os.cpu_count() or 1,
+                            "kind": "port", "sample": "the forward and adjoint solves by the "
+                                                      "oracle (FP64, rtol 1e-12), setup untimed"}}
     print(json.dumps(out), flush=True)
 
 
