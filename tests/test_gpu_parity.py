@@ -384,3 +384,45 @@ def test_fgmres_outer_matches_oracle(prec, k, restart):
         assert ir["status"] == 0
         assert abs(int(info.col_iters[c]) - ir["iters"]) <= 1
         assert _relerr(info.solution[:, c], xr) <= 1e-6
+
+
+@pytest.mark.parametrize("scale", [16, 18])
+def test_rmat_setup_bit_exact_at_scale(scale):
+    # larger R-MAT hierarchies (the headline graph is scale 20; bench.py
+    # checks it against the oracle in every run): every level's CSR, value
+    # bits and ids
+    L = G.rmat(scale, seed=0)
+    S, R = Solver(L, kcycle=1, outer_ksp_type="fcg"), O.OracleSolver(L, kcycle=1,
+                                                                      outer_ksp_type="fcg")
+    assert S.num_levels == R.num_levels
+    for l in range(R.num_levels):
+        assert S.level_info(l) == R.level_info(l), l
+        grp, gci, gv = S.level_matrix(l)
+        rrp, rci, rv = R.level_matrix(l)
+        assert np.array_equal(grp, rrp) and np.array_equal(gci, rci), l
+        assert np.array_equal(gv.view(np.int64), rv.view(np.int64)), l
+        if R.level_info(l)["type"] != "coarse":
+            assert np.array_equal(S.level_ids(l), R.level_ids(l)), l
+    base = 1 if R.level_info(0)["type"] == "elim" else 0
+    b = _proj(np.random.default_rng(9).standard_normal(R.level_info(base)["n"]))
+    assert _relerr(S.cycle(base, b), R.cycle(base, b)) <= 1e-12
+
+
+def test_grid256_plain_fp64_vcycle_matches_oracle():
+    # the C1 configuration: 256 x 256 5-point grid, unit weights, FP64
+    # V-cycle with Chebyshev(2,2) preconditioning FCG to rtol 1e-8
+    L = G.grid2d(256)
+    kw = dict(kcycle=0, outer_ksp_type="fcg", pre_smooth=2, post_smooth=2)
+    S, R = Solver(L, **kw), O.OracleSolver(L, **kw)
+    assert S.num_levels == R.num_levels
+    for l in range(R.num_levels - 1):
+        assert np.array_equal(S.level_ids(l), R.level_ids(l)), l
+        assert np.array_equal(S.level_matrix(l)[2].view(np.int64),
+                              R.level_matrix(l)[2].view(np.int64)), l
+    b = G.rhs(L.n, seed=7)
+    assert _relerr(S.cycle(0, b), R.cycle(0, b)) <= 1e-12
+    info = S.solve(b)
+    xr, ir = R.solve(b)
+    assert info.converged and abs(info.iters() - ir["iters"]) <= 1
+    assert info.true_rel_residual <= 1e-8
+    assert _relerr(info.solution, xr) <= 1e-6
