@@ -150,8 +150,12 @@ typedef struct ligmg_options {
                                  of matrices averaging at least six entries
                                  per row use the nonzero-balanced tile layout
                                  (a warp per tile of whole rows, a lane per 8
-                                 consecutive entries); 0: one group of lanes
-                                 per row */
+                                 consecutive entries; with autotune, a warp
+                                 per tile or a resident grid that fetches a
+                                 warp's next tile during this tile's gathers,
+                                 whichever is faster); 2: tiles, always the
+                                 resident pipelined grid; 0: one group of
+                                 lanes per row */
   int64_t wait_spins;         /* polls of an incomplete barrier before a
                                  device-side wait on other CTAs (the grid-mode
                                  tail kernel's barriers) gives up; the kernel
@@ -165,6 +169,15 @@ typedef struct ligmg_options {
                                  converges; 0: level-by-level kernels over the
                                  union of the graphs replayed from a CUDA
                                  graph */
+  int32_t spmm_streams;       /* products with 8 or more right-hand sides:
+                                 1 (default): with autotune, the row-stream
+                                 kernel (a warp per run of consecutive rows,
+                                 the next row's first indices fetched while
+                                 this row gathers) is timed against a warp per
+                                 row and kept where faster; 0: a warp per row;
+                                 2: row streams always (runs of ~2048
+                                 entries).  Results are the same bits either
+                                 way */
 } ligmg_options;
 
 /* ConvergenceInfo (util.hpp:143-170) of one solve.  For a batched solve the

@@ -80,6 +80,7 @@ class Options(C.Structure):
         ("spmv_tiles", C.c_int32),
         ("wait_spins", C.c_int64),
         ("batch_queue", C.c_int32),
+        ("spmm_streams", C.c_int32),
     ]
 
 
@@ -149,6 +150,7 @@ def default_options(**overrides) -> Options:
     o.spmv_tiles = 1
     o.wait_spins = 0
     o.batch_queue = 1
+    o.spmm_streams = 1
     for k, v in overrides.items():
         if k in ("smoother_type",) and isinstance(v, str):
             v = SMOOTHER[v]

@@ -218,7 +218,8 @@ struct Level {
   std::vector<i64> rp_host, rrp_host, crp_host;
   int lanesA = 32, lanesR = 32, lanesP = 4, lanesC = 32;
   bool autotune = true;  // options.autotune at creation
-  bool tiles = true;     // options.spmv_tiles at creation
+  int tiles = 1;         // options.spmv_tiles at creation
+  int streams = 1;       // options.spmm_streams at creation
   // Chebyshev coefficients
   double theta = 1, delta = 1;
   std::vector<double> c1, c2;
@@ -314,6 +315,10 @@ MatView<T> bare_view(const Level &L, int which) {
 //   threads/block    {64, 128, 256}: small blocks free their slot as soon as
 //                    their rows finish (rows differ widely in length)
 //   lanes per row    {4, 8, 16, 32} for k = 1 on levels without hub rows
+//   row streams      k >= 8: the row-stream kernel (a warp per run of
+//                    consecutive rows; 1, 2, 4 or 8 runs per resident warp;
+//                    five or six resident blocks per SM) against a warp per
+//                    row
 // The choice only changes launch shapes and, on hub rows, how a row's sum is
 // split into chunk partials (its rounding); autotune = 0 uses the defaults
 // (chunks of 32 U, 64 threads for k > 1, 256 for k = 1, the level's lanes).
@@ -330,9 +335,14 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   LG_CUDA(cudaStreamIsCapturing(s, &cs));
   if (!autotune || cs != cudaStreamCaptureStatusNone || n <= 0) {
-    if (tile_ok) best.build_tiles(rp.data(), n, s);
-    else best.build(rp.data(), n, 32 * (i64)unit, k, s);
+    if (tile_ok) {
+      best.build_tiles(rp.data(), n, s);
+      best.tile_pipe = L.tiles == 2;
+    } else {
+      best.build(rp.data(), n, 32 * (i64)unit, k, s);
+    }
     best.tb = k > 1 ? 64 : 256;
+    if (k >= 8 && L.streams == 2 && n > 0) best.build_stream(rp.data(), n, 2048, 5, s);
     return;
   }
   MatView<T> base = bare_view<T>(L, which);
@@ -378,6 +388,45 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
           cand_lanes = lanes;
         }
       }
+    // k >= 8: the row-stream kernel at five or six resident blocks per SM,
+    // with 1, 2, 4 or 8 streams per resident warp of the five-block launch
+    // (stream lengths from the level's own cost: entries plus 16 per row)
+    i64 cand_ps = 0;
+    int cand_sb = 0;
+    if (k >= 8 && L.streams != 0) {
+      const i64 cost = (rp[n] - rp[0]) + 16 * n;
+      const i64 resident = (i64)kSMs * 5 * 8;
+      std::vector<i64> lens;
+      for (int c : {1, 2, 4, 8}) {
+        const i64 ps = std::max<i64>(64, cdiv(cost, resident * c));
+        if (lens.empty() || ps != lens.back()) lens.push_back(ps);
+      }
+      for (i64 ps : lens) {
+        cand.build_stream(rp.data(), n, ps, 5, s);
+        if (cand.nstream == 0) break;
+        for (int sb : {5, 6}) {
+          MatView<T> m = base;
+          cand.fill(m);
+          m.stream_blocks = sb;
+          EpiArgs a;
+          a.y = Y.p;
+          spmm<T>(m, X.p, k, epi, a, s);
+          LG_CUDA(cudaEventRecord(e0, s));
+          for (int r = 0; r < 3; r++) spmm<T>(m, X.p, k, epi, a, s);
+          LG_CUDA(cudaEventRecord(e1, s));
+          LG_CUDA(cudaEventSynchronize(e1));
+          float ms = 0;
+          LG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          if (ms < cand_ms) {
+            cand_ms = ms;
+            cand_ps = ps;
+            cand_sb = sb;
+          }
+        }
+      }
+      if (cand_ps > 0) cand.build_stream(rp.data(), n, cand_ps, cand_sb, s);
+      else cand.nstream = 0;
+    }
     if (!have || cand_ms < best_ms) {
       best = std::move(cand);
       best.tb = cand_tb;
@@ -386,25 +435,38 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
       have = true;
     }
   }
+  if (k >= 8 && L.streams == 2 && best.nstream == 0) best.build_stream(rp.data(), n, 2048, 5, s);
   if (tile_ok) {
     HubPlan<T> cand;
     cand.build_tiles(rp.data(), n, s);
     if (cand.ntiles > 0) {
-      MatView<T> m = base;
-      cand.fill(m);
-      EpiArgs a;
-      a.y = Y.p;
-      spmm<T>(m, X.p, k, epi, a, s);
-      LG_CUDA(cudaEventRecord(e0, s));
-      for (int r = 0; r < 3; r++) spmm<T>(m, X.p, k, epi, a, s);
-      LG_CUDA(cudaEventRecord(e1, s));
-      LG_CUDA(cudaEventSynchronize(e1));
-      float ms = 0;
-      LG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      if (!have || ms < best_ms) {
+      // a warp per tile, or the pipelined resident grid
+      float tms = 1e30f;
+      int tpipe = 0;
+      for (int pipe : {0, 1}) {
+        if (L.tiles == 2 && pipe == 0) continue;  // pipelined tiles only
+        MatView<T> m = base;
+        cand.fill(m);
+        m.tile_pipe = pipe;
+        EpiArgs a;
+        a.y = Y.p;
+        spmm<T>(m, X.p, k, epi, a, s);
+        LG_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < 3; r++) spmm<T>(m, X.p, k, epi, a, s);
+        LG_CUDA(cudaEventRecord(e1, s));
+        LG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        LG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < tms) {
+          tms = ms;
+          tpipe = pipe;
+        }
+      }
+      if (!have || tms < best_ms || L.tiles == 2) {
         best = std::move(cand);
         best.tb = 256;
-        best_ms = ms;
+        best.tile_pipe = tpipe;
+        best_ms = tms;
         have = true;
       }
     }
@@ -1848,7 +1910,8 @@ void finish_level(Handle &H, Level &L) {
   LG_LAUNCH();
   L.lanesA = lanes_for(L.A.nnz, L.A.n);
   L.autotune = H.opts.autotune != 0;
-  L.tiles = H.opts.spmv_tiles != 0;
+  L.tiles = H.opts.spmv_tiles;
+  L.streams = H.opts.spmm_streams;
   L.rp_host = L.A.rp.to_host();
   // the FP64 single right-hand-side plan of A is built (and, with autotune,
   // its layout and launch shape timed) at setup: ligmg_spmv_device_noalloc
@@ -3259,6 +3322,7 @@ void ligmg_default_options(ligmg_options *o) {
   o->spmv_tiles = 1;
   o->wait_spins = 0;
   o->batch_queue = 1;
+  o->spmm_streams = 1;
 }
 
 const char *ligmg_status_string(ligmg_status s) {
@@ -3295,6 +3359,8 @@ ligmg_status ligmg_create(int64_t n, const int64_t *rowptr, const int32_t *col,
         (o.precision != LIGMG_PREC_FP64 && o.precision != LIGMG_PREC_FP32))
       return LIGMG_ERR_INVALID_ARGUMENT;
     if (o.outer_ksp_type == LIGMG_KSP_FGMRES && o.gmres_restart < 1)
+      return LIGMG_ERR_INVALID_ARGUMENT;
+    if (o.spmm_streams < 0 || o.spmm_streams > 2 || o.spmv_tiles < 0 || o.spmv_tiles > 2)
       return LIGMG_ERR_INVALID_ARGUMENT;
     if (o.smoother_type > LIGMG_SMOOTHER_CHEBYSHEV || o.outer_ksp_type > LIGMG_KSP_FGMRES ||
         (o.kcycle_ksp_type != LIGMG_KSP_FCG && o.kcycle_ksp_type != LIGMG_KSP_FGMRES) ||

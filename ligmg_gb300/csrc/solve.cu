@@ -117,6 +117,29 @@ void HubPlan<T>::build_tiles(const i64 *rp_host, i64 n, cudaStream_t s) {
 }
 
 template <typename T>
+void HubPlan<T>::build_stream(const i64 *rp_host, i64 n, i64 per_stream, int blocks,
+                              cudaStream_t s) {
+  nstream = 0;
+  stream_blocks = blocks;
+  if (n <= 0 || rp_host[n] >= ((i64)1 << 31) - 1 || n >= ((i64)1 << 31) - 1) return;
+  std::vector<i32> st{0};
+  i64 acc = 0;
+  for (i64 r = 0; r < n; r++) {
+    const i64 len = rp_host[r + 1] - rp_host[r];
+    acc += (thresh > 0 && len > thresh ? 0 : len) + 16;
+    if (acc >= per_stream) {
+      st.push_back((i32)(r + 1));
+      acc = 0;
+    }
+  }
+  if (st.back() != (i32)n) st.push_back((i32)n);
+  nstream = (i64)st.size() - 1;
+  srow.alloc((i64)st.size(), s);
+  srow.upload(st.data(), (i64)st.size());
+  LG_CUDA(cudaStreamSynchronize(s));
+}
+
+template <typename T>
 void HubPlan<T>::fill(MatView<T> &m) const {
   m.hub_thresh = thresh;
   m.nchunks = nchunks;
@@ -133,6 +156,10 @@ void HubPlan<T>::fill(MatView<T> &m) const {
   m.ntiles = ntiles;
   m.tdesc = tdesc.p;
   m.tbits = tbits.p;
+  m.tile_pipe = tile_pipe;
+  m.nstream = nstream;
+  m.srow = srow.p;
+  m.stream_blocks = stream_blocks;
 }
 template struct HubPlan<float>;
 template struct HubPlan<double>;
@@ -222,32 +249,73 @@ __device__ __forceinline__ void epilogue_prefetch(const EpiArgs &a, i64 r) {
   }
 }
 
+// A tile in registers: the descriptor, this lane's row-start bits and column
+// indices (fetched one tile ahead by the pipelined kernel), and its values.
+template <typename T>
+struct TileIdx {
+  int4 d;
+  u32 word;
+  i32 c[kTileLane];
+};
+
+// Row-start bits and column indices of tile t (descriptor d), and an L1
+// prefetch of the rows its epilogue reads.
 template <typename T, Epi EP>
-__device__ __forceinline__ void tile_unit(const MatView<T> &A, const T *__restrict__ X,
-                                          const EpiArgs &a, i64 t, int lane, T *ssum) {
-  constexpr bool SPLIT = EP == Epi::Split;
-  constexpr int U = kTileLane, VWV = 16 / (int)sizeof(T);
-  const int4 d = __ldg(A.tdesc + t);
-  const int r0 = d.x, nr = d.y, e_rel = d.z;
+__device__ __forceinline__ void tile_fetch(const MatView<T> &A, const EpiArgs &a, i64 t, int4 d,
+                                           int lane, TileIdx<T> &I) {
+  constexpr int U = kTileLane;
+  static_assert(U == 32 || U == 16 || U == 8 || U == 4, "entries per lane");
+  I.d = d;
+  const int e_rel = d.z;
   const i64 ab = (i64)d.w << 2;
   const int lb = lane * U;
-  // this lane's U row-start bits
-  static_assert(U == 32 || U == 16 || U == 8 || U == 4, "entries per lane");
   const int wbit = lane * U;
-  const u32 word = U == 32 ? __ldg(A.tbits + t * (kTilePos / 32) + lane)
-                           : (__ldg(A.tbits + t * (kTilePos / 32) + (wbit >> 5)) >> (wbit & 31)) &
-                                 ((1u << (U & 31)) - 1u);
-  i32 c[U];
-  T v[U];
+  I.word = U == 32 ? __ldg(A.tbits + t * (kTilePos / 32) + lane)
+                   : (__ldg(A.tbits + t * (kTilePos / 32) + (wbit >> 5)) >> (wbit & 31)) &
+                         ((1u << (U & 31)) - 1u);
 #pragma unroll
   for (int g = 0; g < U / 4; g++) {
     const int rel = lb + 4 * g;
     if (rel + 4 <= e_rel) {
       const int4 cc = ld_stream_i4(A.ci + ab + rel);
-      c[4 * g] = cc.x;
-      c[4 * g + 1] = cc.y;
-      c[4 * g + 2] = cc.z;
-      c[4 * g + 3] = cc.w;
+      I.c[4 * g] = cc.x;
+      I.c[4 * g + 1] = cc.y;
+      I.c[4 * g + 2] = cc.z;
+      I.c[4 * g + 3] = cc.w;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; q++) I.c[4 * g + q] = rel + q < e_rel ? __ldg(A.ci + ab + rel + q) : 0;
+    }
+  }
+  for (int i = lane; i < d.y; i += 32) epilogue_prefetch<T, EP>(a, (i64)d.x + i);
+}
+
+// This lane's entries of the tile (bit j: entry lane * U + j is in it)
+template <typename T>
+__device__ __forceinline__ u32 tile_mask(const TileIdx<T> &I, int lane) {
+  constexpr int U = kTileLane;
+  const int lb = lane * U;
+  const int s_rel = __ffs(__shfl_sync(0xffffffffu, I.word, 0)) - 1;  // the tile's first entry
+  const int lo = max(s_rel - lb, 0), hi = min(I.d.z - lb, U);
+  u32 okm = 0;
+  if (hi > lo) okm = (hi >= 32 ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+  return okm;
+}
+
+// The tile's values and gathered x entries (independent loads)
+template <typename T, Epi EP>
+__device__ __forceinline__ void tile_gather(const MatView<T> &A, const T *__restrict__ X,
+                                            const TileIdx<T> &I, u32 okm, int lane,
+                                            T (&v)[kTileLane], T (&xv)[kTileLane]) {
+  constexpr bool SPLIT = EP == Epi::Split;
+  constexpr int U = kTileLane, VWV = 16 / (int)sizeof(T);
+  const int e_rel = I.d.z;
+  const i64 ab = (i64)I.d.w << 2;
+  const int lb = lane * U;
+#pragma unroll
+  for (int g = 0; g < U / 4; g++) {
+    const int rel = lb + 4 * g;
+    if (rel + 4 <= e_rel) {
 #pragma unroll
       for (int h = 0; h < 4 / VWV; h++) {
         T tv[VWV];
@@ -257,22 +325,23 @@ __device__ __forceinline__ void tile_unit(const MatView<T> &A, const T *__restri
       }
     } else {
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const bool in = rel + q < e_rel;
-        c[4 * g + q] = in ? __ldg(A.ci + ab + rel + q) : 0;
-        v[4 * g + q] = in ? __ldg(A.v + ab + rel + q) : (T)0;
-      }
+      for (int q = 0; q < 4; q++) v[4 * g + q] = rel + q < e_rel ? __ldg(A.v + ab + rel + q) : (T)0;
     }
   }
-  for (int i = lane; i < nr; i += 32) epilogue_prefetch<T, EP>(a, (i64)r0 + i);
-  const int s_rel = __ffs(__shfl_sync(0xffffffffu, word, 0)) - 1;  // the tile's first entry
-  const int lo = max(s_rel - lb, 0), hi = min(e_rel - lb, U);
-  u32 okm = 0;  // this lane's entries of the tile
-  if (hi > lo) okm = (hi >= 32 ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
-  T xv[U];
 #pragma unroll
   for (int j = 0; j < U; j++)
-    xv[j] = ((okm >> j) & 1u) ? __ldg(xsrc<T, 1, SPLIT>(A, X, c[j])) : (T)0;
+    xv[j] = ((okm >> j) & 1u) ? __ldg(xsrc<T, 1, SPLIT>(A, X, I.c[j])) : (T)0;
+}
+
+// Row sums of the tile (lane sums in entry order, a segmented scan across
+// lanes) and the epilogue, one row per lane.
+template <typename T, Epi EP>
+__device__ __forceinline__ void tile_finish(const EpiArgs &a, const TileIdx<T> &I, u32 okm,
+                                            const T (&v)[kTileLane], const T (&xv)[kTileLane],
+                                            int lane, T *ssum) {
+  constexpr int U = kTileLane;
+  const int r0 = I.d.x, nr = I.d.y, e_rel = I.d.z;
+  const u32 word = I.word;
   // rows started before this lane: exclusive scan of the row-start counts
   const int cnt = __popc(word);
   int inc = cnt;
@@ -319,6 +388,18 @@ __device__ __forceinline__ void tile_unit(const MatView<T> &A, const T *__restri
     T r1[1] = {ssum[i]};
     epilogue<T, 1, 1, EP>(a, (i64)r0 + i, 0, r1);
   }
+  __syncwarp();
+}
+
+template <typename T, Epi EP>
+__device__ __forceinline__ void tile_unit(const MatView<T> &A, const T *__restrict__ X,
+                                          const EpiArgs &a, i64 t, int lane, T *ssum) {
+  TileIdx<T> I;
+  tile_fetch<T, EP>(A, a, t, __ldg(A.tdesc + t), lane, I);
+  const u32 okm = tile_mask(I, lane);
+  T v[kTileLane], xv[kTileLane];
+  tile_gather<T, EP>(A, X, I, okm, lane, v, xv);
+  tile_finish<T, EP>(a, I, okm, v, xv, lane, ssum);
 }
 
 template <typename T, Epi EP>
@@ -329,6 +410,209 @@ __global__ void __launch_bounds__(kTileWarps * 32, LG_TILE_MIN_BLOCKS)
   const i64 warp = (i64)blockIdx.x * kTileWarps + w;
   if (warp < A.ntiles) tile_unit<T, EP>(A, X, a, warp, lane, ssum[w]);
   else dev::hub_unit<T, 1, EP>(A, X, a, warp - A.ntiles, lane);
+}
+
+// Pipelined tiles: a resident grid whose warp w takes tiles w, w + W, w + 2W,
+// ... (W warps in the grid).  The one-warp-per-tile kernel waits for three
+// dependent round trips per tile (descriptor, column indices, gathers) of
+// which one gathers; here the lanes fetch the warp's next 32 descriptors with
+// one load, and the next tile's row-start bits and column indices are loaded
+// while this tile's gathers are in flight, so a tile costs about one round
+// trip.  Values are loaded with the gathers.  Same per-tile arithmetic, same
+// results.  Hub chunks follow, strided the same way.
+#ifndef LG_TILEP_MIN_BLOCKS
+#define LG_TILEP_MIN_BLOCKS 3  // 80 registers
+#endif
+__device__ __forceinline__ int4 shfl_int4(int4 v, int src) {
+  int4 r;
+  r.x = __shfl_sync(0xffffffffu, v.x, src);
+  r.y = __shfl_sync(0xffffffffu, v.y, src);
+  r.z = __shfl_sync(0xffffffffu, v.z, src);
+  r.w = __shfl_sync(0xffffffffu, v.w, src);
+  return r;
+}
+
+template <typename T, Epi EP>
+__global__ void __launch_bounds__(kTileWarps * 32, LG_TILEP_MIN_BLOCKS)
+    k_spmv_tile_pipe(const MatView<T> A, const T *__restrict__ X, const EpiArgs a) {
+  __shared__ T ssum[kTileWarps][kTileRows];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // tile counts fit 32 bits (the pipelined launch is used below 2^31 tiles)
+  const int gw = (int)blockIdx.x * kTileWarps + w;
+  const int nw = (int)gridDim.x * kTileWarps;
+  const int nt = (int)A.ntiles;
+  const int mine = gw < nt ? (nt - 1 - gw) / nw + 1 : 0;  // this warp's tiles
+  if (mine > 0) {
+    // lane l: descriptor of the warp's tile (batch + l)
+    int4 dl = lane < mine ? __ldg(A.tdesc + gw + (i64)lane * nw) : make_int4(0, 0, 0, 0);
+    TileIdx<T> cur;
+    tile_fetch<T, EP>(A, a, gw, shfl_int4(dl, 0), lane, cur);
+    for (int i = 0; i < mine; i++) {
+      const u32 okm = tile_mask(cur, lane);
+      T v[kTileLane], xv[kTileLane];
+      tile_gather<T, EP>(A, X, cur, okm, lane, v, xv);
+      TileIdx<T> nxt;
+      const int in = i + 1;
+      if (in < mine) {
+        if ((in & 31) == 0) {
+          const int q = in + lane;
+          dl = q < mine ? __ldg(A.tdesc + gw + (i64)q * nw) : make_int4(0, 0, 0, 0);
+        }
+        tile_fetch<T, EP>(A, a, gw + (i64)in * nw, shfl_int4(dl, in & 31), lane, nxt);
+      }
+      tile_finish<T, EP>(a, cur, okm, v, xv, lane, ssum[w]);
+      if (in < mine) cur = nxt;
+    }
+  }
+  for (i64 c = gw; c < A.nchunks; c += nw) dev::hub_unit<T, 1, EP>(A, X, a, c, lane);
+}
+
+// ---- k right-hand sides, row streams ---------------------------------------
+// The warp-per-row kernel pays, on every row, dependent round trips that
+// gather nothing: the row bounds, the first column indices and the
+// epilogue's input rows (about a third of a row's time on the large R-MAT
+// levels, whose rows take five or six gather steps).  Here warp w takes the
+// consecutive rows [srow[w], srow[w + 1]) (balanced by entries at plan time):
+// the next row's end is loaded while this row gathers, the last step of a
+// row fetches the next row's first column indices, and the epilogue's input
+// rows are prefetched into L1 in that step, one round trip before they are
+// read.  Steps are warp-uniform, U entries per slot, masked past the row's
+// end; every slot adds its entries in entry order, as the row kernel does,
+// so the results are the same bits.
+
+// L1 prefetch of the k-column rows (and per-row scalars) an epilogue reads
+template <typename T, int K, Epi EP>
+__device__ __forceinline__ void epilogue_prefetch_rows(const EpiArgs &a, i64 r, int lane) {
+  constexpr int RB = K * (int)sizeof(T);  // bytes of a vector's row
+  constexpr int LINES = (RB + 127) / 128;
+  const void *v0 = nullptr, *v1 = nullptr, *v2 = nullptr, *sc = nullptr;
+  if constexpr (EP == Epi::Resid || EP == Epi::ElimInterp) v0 = a.b;
+  if constexpr (EP == Epi::ChebZ) {
+    v0 = a.b;
+    sc = a.invd;
+  }
+  if constexpr (EP == Epi::ChebA || EP == Epi::Jacobi) {
+    v0 = a.b;
+    v1 = a.xin;
+    sc = a.invd;
+  }
+  if constexpr (EP == Epi::ChebB) {
+    v0 = a.rin;
+    v1 = a.din;
+    v2 = a.xin;
+    sc = a.invd;
+  }
+  if constexpr (EP == Epi::FcgDir) {
+    v0 = a.xin;
+    v1 = a.din;
+    v2 = a.rin;
+  }
+  if constexpr (EP == Epi::ElimInterp || EP == Epi::FcgDir) sc = a.q;
+  const int v = lane / LINES, l = lane % LINES;
+  const void *p = v == 0 ? v0 : v == 1 ? v1 : v == 2 ? v2 : nullptr;
+  if (p) prefetch_l1((const char *)p + r * RB + l * 128);
+  if (lane == 31 && sc) prefetch_l1((const T *)sc + r);
+}
+
+template <typename T, int K, Epi EP, int U>
+__device__ __forceinline__ void stream_unit(const MatView<T> &A, const T *__restrict__ X,
+                                            const EpiArgs &a, i64 w, int lane) {
+  constexpr bool SPLIT = EP == Epi::Split;
+  constexpr int VW = (K % VT<T>::W == 0) ? VT<T>::W : 1;
+  constexpr int L = K / VW;
+  constexpr int E = 32 / L;
+  constexpr int STEP = U * E;
+  const int slot = lane / L, ch = lane % L;
+  const T *__restrict__ av = A.v;
+  const i32 *__restrict__ ac = A.ci;
+  const i64 *__restrict__ rp = A.rp;
+  const int hub = (int)A.hub_thresh;  // 0: no hub rows
+  int r = __ldg(A.srow + w);
+  const int r1 = __ldg(A.srow + w + 1);
+  int b = (int)__ldg(rp + r), e = (int)__ldg(rp + r + 1);
+  int ee = (hub > 0 && e - b > hub) ? b : e;  // a hub row's entries belong to its chunks
+  i32 jn[U];
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int q = b + slot + u * E;
+    jn[u] = q < ee ? __ldg(ac + q) : -1;
+  }
+  while (true) {
+    const bool last = r + 1 >= r1;
+    const int en = last ? e : (int)__ldg(rp + r + 2);
+    T acc[VW];
+#pragma unroll
+    for (int q = 0; q < VW; q++) acc[q] = (T)0;
+    int kb = b;
+    while (true) {
+      i32 j[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) j[u] = jn[u];
+      const int kn = kb + STEP;
+      const bool more = kn < ee;
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int q = kn + slot + u * E;
+          jn[u] = q < ee ? __ldg(ac + q) : -1;
+        }
+      } else {  // the next row's first step, and this row's epilogue inputs
+        const int nee = (last || (hub > 0 && en - e > hub)) ? e : en;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int q = e + slot + u * E;
+          jn[u] = q < nee ? __ldg(ac + q) : -1;
+        }
+        if (ee > b || e == b) epilogue_prefetch_rows<T, K, EP>(a, r, lane);
+      }
+      T va[U], x[U][VW];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if (j[u] >= 0) {
+          va[u] = __ldg(av + kb + slot + u * E);
+          xload<T, VW, true>(xsrc<T, K, SPLIT>(A, X, j[u]) + ch * VW, x[u]);
+        } else {
+          va[u] = (T)0;
+#pragma unroll
+          for (int q = 0; q < VW; q++) x[u][q] = (T)0;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++)
+#pragma unroll
+        for (int q = 0; q < VW; q++) acc[q] += va[u] * x[u][q];
+      if (!more) break;
+      kb = kn;
+    }
+    reduce_slots<T, VW, L, 32>(acc);
+    if ((ee > b || e == b) && slot == 0) epilogue<T, K, VW, EP>(a, r, ch * VW, acc);
+    if (last) break;
+    r++;
+    b = e;
+    e = en;
+    ee = (hub > 0 && e - b > hub) ? b : e;
+  }
+}
+
+template <typename T, int K, Epi EP, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+    k_spmm_rs(const MatView<T> A, const T *__restrict__ X, const EpiArgs a) {
+  const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp < A.nstream) stream_unit<T, K, EP, 4>(A, X, a, warp, lane);
+  else dev::hub_unit<T, K, EP>(A, X, a, warp - A.nstream, lane);
+}
+
+// stream_blocks: the resident 256-thread blocks per SM the register budget is
+// set for (5: 48 registers; 6: 40)
+template <typename T, int K, Epi EP>
+void launch_spmm_rs(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t s) {
+  const i64 warps = A.nstream + A.nchunks;
+  if (A.stream_blocks == 6)
+    k_spmm_rs<T, K, EP, 6><<<grid_for(warps * 32, 256), 256, 0, s>>>(A, X, a);
+  else
+    k_spmm_rs<T, K, EP, 5><<<grid_for(warps * 32, 256), 256, 0, s>>>(A, X, a);
+  LG_LAUNCH();
 }
 
 template <typename T, int K, int G, Epi EP>
@@ -346,8 +630,18 @@ void dispatch_g(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t 
   if constexpr (K == 1) {
     // the tile layout reads 16-byte aligned column and value arrays
     if (A.ntiles > 0 && (((uintptr_t)A.ci | (uintptr_t)A.v) & 15) == 0) {
-      k_spmv_tile<T, EP><<<grid_for(A.ntiles + A.nchunks, kTileWarps), kTileWarps * 32, 0, s>>>(
-          A, X, a);
+      if (A.tile_pipe && A.ntiles < ((i64)1 << 31) - ((i64)kSMs << 8)) {
+        static int per_sm = 0;  // resident blocks of this instantiation
+        if (per_sm == 0)
+          LG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmv_tile_pipe<T, EP>,
+                                                                kTileWarps * 32, 0));
+        const i64 g = std::min<i64>((i64)std::max(per_sm, 1) * kSMs,
+                                    cdiv(A.ntiles + A.nchunks, kTileWarps));
+        k_spmv_tile_pipe<T, EP><<<(unsigned)g, kTileWarps * 32, 0, s>>>(A, X, a);
+      } else {
+        k_spmv_tile<T, EP><<<grid_for(A.ntiles + A.nchunks, kTileWarps), kTileWarps * 32, 0, s>>>(
+            A, X, a);
+      }
       LG_LAUNCH();
       return;
     }
@@ -359,6 +653,9 @@ void dispatch_g(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t 
       default: return launch_spmm<T, 1, 32, EP>(A, X, a, s);
     }
   } else {
+    if constexpr (K >= 8) {
+      if (A.nstream > 0) return launch_spmm_rs<T, K, EP>(A, X, a, s);
+    }
     launch_spmm<T, K, 32, EP>(A, X, a, s);
   }
 }

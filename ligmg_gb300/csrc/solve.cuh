@@ -33,9 +33,17 @@ struct MatView {
   i64 ntiles = 0;
   const int4 *tdesc = nullptr;
   const u32 *tbits = nullptr;
+  int tile_pipe = 0;  // 1: a resident grid, the next tile fetched during this one's gathers
   // Epi::Split only: the second gathered operand and the first column taken from it
   const T *x2 = nullptr;
   i64 xsplit = 0;
+  // k > 1, row streams (0 streams: a warp per row).  Stream w is the rows
+  // [srow[w], srow[w + 1]); hub rows in it are left to their chunks.
+  // stream_blocks: resident 256-thread blocks per SM of the launch's register
+  // budget (5 or 6).
+  i64 nstream = 0;
+  const i32 *srow = nullptr;
+  int stream_blocks = 5;
 };
 
 // Hub-row schedule owned by a level (built once at setup).
@@ -54,6 +62,11 @@ struct HubPlan {
   DBuf<int4> tdesc;
   DBuf<u32> tbits;
   i64 ntiles = 0;
+  int tile_pipe = 0;
+  // k > 1 row streams (MatView::srow); nstream = 0 when not built
+  DBuf<i32> srow;
+  i64 nstream = 0;
+  int stream_blocks = 5;
   // launch shape kept with the plan (picked by the autotuner or defaults)
   int tb = 256;    // threads per block
   int lanes = 0;   // lanes per row for k = 1 (0: the level's default)
@@ -64,6 +77,11 @@ struct HubPlan {
   // k = 1 tile layout: rows longer than a tile holds are hub rows (the split
   // is set so); the other rows are packed into tiles in order
   void build_tiles(const i64 *rp_host, i64 n, cudaStream_t s);
+  // k > 1 row streams over the rows of this plan (hub rows, already set by
+  // build, count as empty): consecutive rows until a stream holds about
+  // `per_stream` entries (a row costs its entries plus 16).  Not built
+  // (nstream = 0) when the matrix has 2^31 entries or more.
+  void build_stream(const i64 *rp_host, i64 n, i64 per_stream, int blocks, cudaStream_t s);
   void fill(MatView<T> &m) const;
 };
 // Single right-hand side tile layout: at most kTilePos entries (counted from

@@ -81,3 +81,21 @@ def test_tile_layout_solve_matches_row_layout(name, prec):
     assert a.true_rel_residual <= 2e-8
     x, y = a.solution - a.solution.mean(), c.solution - c.solution.mean()
     assert np.linalg.norm(x - y) <= 1e-6 * np.linalg.norm(y)
+
+
+@pytest.mark.parametrize("name", list(GRAPHS) + ["hub_star"])
+def test_pipelined_tiles_bit_equal_every_level(name):
+    # spmv_tiles = 2: the resident grid that fetches a warp's next tile during
+    # this tile's gathers; the per-tile arithmetic is the warp-per-tile
+    # kernel's, so with fixed shapes (autotune = 0) every level's product and
+    # a whole solve are the same bits
+    L = _hub_star() if name == "hub_star" else GRAPHS[name]()
+    P, W = Solver(L, spmv_tiles=2, autotune=0), Solver(L, spmv_tiles=1, autotune=0)
+    rng = np.random.default_rng(4)
+    for lvl in range(P.num_levels):
+        x = rng.standard_normal(P.level_info(lvl)["n"])
+        assert np.array_equal(P.spmv(lvl, x), W.spmv(lvl, x)), lvl
+    b = G.rhs(L.n, seed=22)
+    a, c = P.solve(b), W.solve(b)
+    assert a.converged and a.iters() == c.iters()
+    assert np.array_equal(a.solution, c.solution)
