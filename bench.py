@@ -293,7 +293,23 @@ def spmv_roofline(S64, stream, peak, peak_kind, reps=20):
             "traffic": traffic, "traffic_source": SPMV_TRAFFIC_SOURCE if traffic else None,
             "kernel": f"FP64 k=1 SpMV y = A x (layout picked by the setup autotuner), "
                       f"level {lv} n={n} nnz={nnz}",
-            "bytes_per_launch": byt, "us_per_launch": sec * 1e6, "launches_timed": reps}
+            "bytes_per_launch": byt, "us_per_launch": sec * 1e6, "launches_timed": reps,
+            "gather": gather_roof(n, 8, nnz, sec)}
+
+
+def gather_roof(n, width, nnz, sec):
+    """The same launch against the gather ceiling measured on this GPU: one
+    random `width`-byte row of x per entry, from a table of the level's n rows
+    (ligmg_measure_gather_peak), entries per second over that ceiling."""
+    from ligmg_gb300 import Solver
+    try:
+        peak = Solver.gather_peak(n, width, nnz)
+    except Exception as e:  # measurement only
+        return {"error": str(e)}
+    ach = nnz / sec
+    return {"bound": "l2-gather", "achieved": ach, "peak": peak, "unit": "rows/s",
+            "frac": ach / peak, "row_bytes": width, "table_rows": n,
+            "peak_source": "measured in this run (ligmg_measure_gather_peak)"}
 
 
 def run_reference(args):
@@ -520,7 +536,15 @@ def run_ours(args):
             nnz_top = level_nnz_of(S, top["level"])
             traffic = SPMM_K32_DRAM_BYTES_PER_NNZ * nnz_top if nnz_top else None
             traffic_src = SPMM_K32_TRAFFIC_SOURCE
+        gath = None
+        if top["kind"] in ("cheb_a", "cheb_b", "spmv", "resid"):
+            # one gathered X row (k values) per entry of the level's A
+            lv_top = S.level_info(top["level"])
+            gath = gather_roof(lv_top["n"], top["k"] * (8 if top["fp64"] else 4), lv_top["nnz"],
+                               per_launch_s) if top["k"] * (8 if top["fp64"] else 4) in (4, 8, 128) \
+                else None
         roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "gather": gath,
                 "traffic": traffic, "traffic_source": traffic_src, "peak_source": peak_kind,
                 "kernel": f"spmm_{top['kind']} level {top['level']} k={top['k']} "
                           f"{'fp64' if top['fp64'] else 'fp32'}",
@@ -589,6 +613,13 @@ def run_ours(args):
                       "share_of_profiled": tails[0]["seconds"] / (profiled_ms / 1e3),
                       "note": "coarse levels from `level` down as one persistent kernel in "
                               "shared memory (kept by the autotuner)"} if tails else None),
+            "gathers_by_level": [
+                {"level": r["level"], "kind": r["kind"],
+                 "rows_per_s": S.level_info(r["level"])["nnz"] * r["launches"] / r["seconds"],
+                 "l2_to_sm_tbs": S.level_info(r["level"])["nnz"] * r["launches"] / r["seconds"]
+                 * r["k"] * (8 if r["fp64"] else 4) / 1e12}
+                for r in sorted(stats, key=lambda r: (r["level"], r["kind"]))
+                if r["kind"] in ("cheb_a", "cheb_b", "spmv") and 1 <= r["level"] <= 4],
             "profile_table": [[r["level"], r["kind"], round(r["launches"] / args.steps, 1),
                                round(r["seconds"] * 1e3 / args.steps, 3)]
                               for r in sorted(stats, key=lambda r: -r["seconds"])],

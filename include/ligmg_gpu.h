@@ -178,6 +178,21 @@ typedef struct ligmg_options {
                                  2: row streams always (runs of ~2048
                                  entries).  Results are the same bits either
                                  way */
+  int32_t tail_cluster;       /* shared-memory coarse tail (tail_rows = 0):
+                                 0 (default): one CTA per column slice, from
+                                 the first level whose matrices fit in shared
+                                 memory; 1: when a shallower level's work
+                                 vectors fit although its matrices do not, the
+                                 tail starts there instead and runs a column
+                                 slice on a cluster of CTAs that divide the
+                                 products with matrices left in global memory
+                                 (distributed shared memory, hardware cluster
+                                 barriers); with autotune the cluster size is
+                                 timed and the tail kept only where a whole
+                                 preconditioner application is faster (on
+                                 R-MAT 20 it is not: a CTA's eight warps walk
+                                 their rows' L2 round trips one row after
+                                 another) */
 } ligmg_options;
 
 /* ConvergenceInfo (util.hpp:143-170) of one solve.  For a batched solve the
@@ -330,6 +345,24 @@ ligmg_status ligmg_get_stream(ligmg_handle h, void **stream);
 /* Kernels launched by this library in this process so far (kernels run
  * from the library's CUDA graphs are counted on every replay). */
 ligmg_status ligmg_launch_count(int64_t *count);
+
+/* Message of the last call in this thread that returned an error status
+ * (the failing CUDA call and its error string, or the check that failed);
+ * valid until the next failing call in the thread. */
+const char *ligmg_last_error(void);
+
+/* The gather ceiling of the running GPU (no reference counterpart; a
+ * measurement entry for roofline reports).  Every entry of a sparse product
+ * gathers one row of the right-hand-side block; on the large levels that
+ * block lies in L2, so the products are bound by the rate of random row
+ * gathers from L2, not by HBM.  Times `count` gathers of `width`-byte rows
+ * (4, 8 or 128) at pseudo-random positions (read from an index array in
+ * order, as a product reads column indices) of a zeroed table of `rows` rows,
+ * every SM full of warps with independent gathers in flight, and returns
+ * rows per second.  Allocates (rows * width + 4 count bytes) and frees on a
+ * private stream. */
+ligmg_status ligmg_measure_gather_peak(int64_t rows, int32_t width, int64_t count,
+                                       double *rows_per_s);
 
 /* Input preparation on the GPU (the reference CLI's --cc / --adj steps,
  * src/main.cpp:70-110, with largest_cc of include/ligmg/cc.hpp:24-106).

@@ -81,6 +81,7 @@ class Options(C.Structure):
         ("wait_spins", C.c_int64),
         ("batch_queue", C.c_int32),
         ("spmm_streams", C.c_int32),
+        ("tail_cluster", C.c_int32),
     ]
 
 
@@ -151,6 +152,7 @@ def default_options(**overrides) -> Options:
     o.wait_spins = 0
     o.batch_queue = 1
     o.spmm_streams = 1
+    o.tail_cluster = 0
     for k, v in overrides.items():
         if k in ("smoother_type",) and isinstance(v, str):
             v = SMOOTHER[v]

@@ -70,6 +70,9 @@ def lib(path=None):
     L.ligmg_set_stream.argtypes = [vp, vp]
     L.ligmg_get_stream.argtypes = [vp, P(vp)]
     L.ligmg_launch_count.argtypes = [P(C.c_int64)]
+    L.ligmg_last_error.restype = C.c_char_p
+    L.ligmg_last_error.argtypes = []
+    L.ligmg_measure_gather_peak.argtypes = [C.c_int64, C.c_int32, C.c_int64, P(C.c_double)]
     L.ligmg_spmv_device_noalloc.argtypes = [vp, C.c_int32, vp, vp]
     L.ligmg_forward.argtypes = [vp, vp, vp, P(Info)]
     L.ligmg_solve_pcg_jacobi.argtypes = [vp, vp, vp, P(Info)]
@@ -82,7 +85,7 @@ def lib(path=None):
     L.ligmg_backward.argtypes = [vp, vp, vp, vp, P(Info)]
     L.ligmg_setup_times.argtypes = [vp, P(C.c_double)]
     for name in header_functions():
-        if name not in ("ligmg_default_options", "ligmg_status_string"):
+        if name not in ("ligmg_default_options", "ligmg_status_string", "ligmg_last_error"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -90,5 +93,6 @@ def lib(path=None):
 
 def check(status, what=""):
     if status not in (0, 1):
-        raise LigmgError(status, what)
+        msg = lib().ligmg_last_error()
+        raise LigmgError(status, f"{what}: {msg.decode()}" if msg else what)
     return status

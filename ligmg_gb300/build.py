@@ -26,6 +26,7 @@ UNITS = {
     "tail.cu": [],
     "prep.cu": [],
     "queue.cu": [],
+    "peaks.cu": [],
     "api.cu": [],
 }
 

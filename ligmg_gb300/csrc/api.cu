@@ -23,6 +23,7 @@
 #include "prep.cuh"
 #include "tail.cuh"
 #include "queue.cuh"
+#include "peaks.cuh"
 
 namespace lg {
 namespace {
@@ -587,6 +588,7 @@ struct TailState {
   float best_ms = 0;    // autotune: time of one launch in the chosen shape
   int start = 0;        // first level of the tail (0: none)
   bool smem_mode = false;
+  bool cluster = false; // shared-memory mode in clusters (sl.cluster CTAs per slice)
   int G = 0;            // grid mode: CTAs of the cooperative launch
   int nops = 0;
   double bytes = 0;     // compulsory bytes of a visit: its input and output
@@ -1155,8 +1157,13 @@ struct TailCopy {
   size_t off, bytes;
 };
 template <typename T>
+// spill (cluster mode): read-only arrays go to shared memory level by level,
+// deepest first, while they fit after the program and the work vectors; the
+// other levels' arrays stay in global memory (their products are divided
+// among a cluster's CTAs).  Otherwise everything must fit.
 bool tail_record(Handle &H, Work<T> &W, size_t start, int smem_avail, int kl,
-                 std::vector<TOp<T>> &ops, TailSmemLaunch &sl, std::vector<TailCopy> &consts) {
+                 std::vector<TOp<T>> &ops, TailSmemLaunch &sl, std::vector<TailCopy> &consts,
+                 bool spill = false) {
   TailBuilder<T> B(H, W);
   B.whole_rows = smem_avail > 0;  // a CTA of its own: the chunk partials are global
   LevelWork<T> &top = W.lw[start];
@@ -1171,6 +1178,9 @@ bool tail_record(Handle &H, Work<T> &W, size_t start, int smem_avail, int kl,
     const char *base;
     size_t gbytes, bytes;
     long long off;
+    size_t lev = 0;     // read-only arrays: their level
+    bool keep = true;   // read-only arrays: placed in shared memory
+    bool used = false;  // read-only arrays: read by the program
     bool inside(const void *p) const {
       const char *c = (const char *)p;
       return c >= base && c < base + gbytes;
@@ -1190,7 +1200,7 @@ bool tail_record(Handle &H, Work<T> &W, size_t start, int smem_avail, int kl,
     }
     const Level &L = *H.h[l];
     auto add = [&](const void *p, size_t bytes) {
-      if (p && bytes) cons.push_back({(const char *)p, bytes, bytes, -1});
+      if (p && bytes) cons.push_back({(const char *)p, bytes, bytes, -1, l});
     };
     const size_t n = (size_t)L.A.n, sv = sizeof(T);
     add(L.A.rp.p, 8 * (n + 1));
@@ -1246,10 +1256,48 @@ bool tail_record(Handle &H, Work<T> &W, size_t start, int smem_avail, int kl,
   auto con_fields = [](TOp<T> &op, auto &&f) {
     f(op.A.rp); f(op.A.ci); f(op.A.v); f(op.a.invd); f(op.a.q); f(op.x1); f(op.idx);
   };
+  for (TOp<T> &op : ops)
+    con_fields(op, [&](auto &p) {
+      if (owner(vecs, p)) return;
+      if (Reg *r = owner(cons, p)) r->used = true;
+    });
+  if (spill) {
+    // the work vectors and scalar slots the program touches
+    size_t wbytes = 0;
+    std::vector<const Reg *> seen;
+    auto count = [&](const Reg *r) {
+      if (!r || std::find(seen.begin(), seen.end(), r) != seen.end()) return;
+      seen.push_back(r);
+      wbytes += up16(r->bytes);
+    };
+    for (TOp<T> &op : ops) {
+      vec_fields(op, [&](auto &p) {
+        if (p && !owner(cons, p)) count(owner(vecs, p));
+      });
+      sc_fields(op, [&](auto &p) {
+        if (p) count(owner(scs, p));
+      });
+    }
+    count(owner(vecs, top.in.p));
+    count(owner(vecs, top.out.p));
+    long long budget = (long long)smem_avail - (long long)total - (long long)wbytes;
+    for (Reg &r : cons) r.keep = false;
+    for (size_t l = W.lw.size(); l-- > start;) {
+      size_t lb = 0;
+      for (const Reg &r : cons)
+        if (r.lev == l && r.used) lb += up16(r.bytes);
+      if ((long long)lb > budget) break;  // this level and the shallower ones stay global
+      budget -= (long long)lb;
+      for (Reg &r : cons)
+        if (r.lev == l) r.keep = true;
+    }
+  }
   // image first (program, then read-only arrays), then the writable regions
   for (TOp<T> &op : ops)
     con_fields(op, [&](auto &p) {
-      if (!owner(vecs, p)) claim(owner(cons, p));
+      if (owner(vecs, p)) return;
+      Reg *r = owner(cons, p);
+      if (r && r->keep) claim(r);
     });
   sl.image_bytes = (int)total;
   bool ok = true;
@@ -1278,7 +1326,7 @@ bool tail_record(Handle &H, Work<T> &W, size_t start, int smem_avail, int kl,
     con_fields(op, [&](auto &p) {
       if (owner(vecs, p)) return;
       Reg *r = owner(cons, p);
-      if (r) tag(p, r->off + ((const char *)p - r->base));
+      if (r && r->off >= 0) tag(p, r->off + ((const char *)p - r->base));
     });
     vec_fields(op, [&](auto &p) {
       Reg *r = owner(vecs, p);
@@ -1335,12 +1383,30 @@ void tail_plan(Handle &H, Work<T> &W) {
   std::vector<TOp<T>> ops;
   std::vector<TailCopy> consts;
   TailSmemLaunch sl;
+  size_t plain = 0;  // shallowest start of the plain shared-memory mode
   for (size_t t = 1; t < H.h.size(); t++) {
     if (tail_record<T>(H, W, t, avail, 1, ops, sl, consts)) {
-      ts.start = (int)t;
-      ts.smem_mode = true;
-      return;
+      plain = t;
+      break;
     }
+  }
+  // cluster mode: the shallowest start whose work vectors fit (the larger
+  // levels' matrices stay in global memory), when shallower than `plain`
+  if (H.opts.tail_cluster && tail_cluster_ok<T>(1, 2, 0)) {
+    const size_t lim_t = plain ? plain : H.h.size();
+    for (size_t t = 1; t < lim_t; t++) {
+      if (H.h[t]->type == LIGMG_LEVEL_COARSE) break;
+      if (tail_record<T>(H, W, t, avail, 1, ops, sl, consts, true)) {
+        ts.start = (int)t;
+        ts.smem_mode = true;
+        ts.cluster = true;
+        return;
+      }
+    }
+  }
+  if (plain) {
+    ts.start = (int)plain;
+    ts.smem_mode = true;
   }
 }
 
@@ -1359,14 +1425,17 @@ void tail_launch(Handle &H, Work<T> &W, int G) {
 // Upload the shared-memory image of `kl` columns per CTA (program followed by
 // the read-only arrays).
 template <typename T>
-bool tail_build_smem(Handle &H, Work<T> &W, int kl) {
+bool tail_build_smem(Handle &H, Work<T> &W, int kl, int cluster = 1) {
   TailState<T> &ts = W.tail;
   const int avail = tail_smem_prepare<T>(kl, 0);
   std::vector<TOp<T>> ops;
   std::vector<TailCopy> consts;
   TailSmemLaunch sl;
-  if (!tail_record<T>(H, W, (size_t)ts.start, avail, kl, ops, sl, consts)) return false;
+  if (!tail_record<T>(H, W, (size_t)ts.start, avail, kl, ops, sl, consts, ts.cluster))
+    return false;
   tail_smem_prepare<T>(kl, sl.smem);
+  if (ts.cluster && !tail_cluster_ok<T>(kl, cluster, sl.smem)) return false;
+  sl.cluster = ts.cluster ? cluster : 1;
   ts.image.alloc(sl.image_bytes, H.s);
   LG_CUDA(cudaMemcpyAsync(ts.image.p, ops.data(), sizeof(TOp<T>) * ops.size(),
                           cudaMemcpyHostToDevice, H.s));
@@ -1418,23 +1487,30 @@ void tail_prepare(Handle &H, Work<T> &W) {
   };
   float best = 1e30f;
   if (ts.smem_mode) {
-    int best_kl = 0;
+    int best_kl = 0, best_cl = 1;
     std::vector<int> kls = tail_slices(k);
-    if (!H.opts.autotune) kls = {kls.back()};  // fewest CTAs
+    // without autotune: the widest slice that fits (fewest CTAs)
+    if (!H.opts.autotune) std::reverse(kls.begin(), kls.end());
+    std::vector<int> cls{1};
+    if (ts.cluster) cls = H.opts.autotune ? std::vector<int>{2, 4, 8, 16} : std::vector<int>{4};
     for (int kl : kls) {
-      if (!tail_build_smem<T>(H, W, kl)) continue;
-      const float ms = time_once(0);
-      if (ms < best) {
-        best = ms;
-        best_kl = kl;
+      for (int cl : cls) {
+        if (!tail_build_smem<T>(H, W, kl, cl)) continue;
+        const float ms = time_once(0);
+        if (ms < best) {
+          best = ms;
+          best_kl = kl;
+          best_cl = cl;
+        }
       }
+      if (!H.opts.autotune && best_kl) break;
     }
     if (best_kl == 0) {
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
       return;
     }
-    if (best_kl != ts.sl.kl) tail_build_smem<T>(H, W, best_kl);
+    if (best_kl != ts.sl.kl || best_cl != ts.sl.cluster) tail_build_smem<T>(H, W, best_kl, best_cl);
   } else {
     std::vector<TOp<T>> ops;
     std::vector<TailCopy> consts;
@@ -1733,9 +1809,9 @@ struct Engine {
       if (ts.on && o().verbose)
         fprintf(stderr, "[ligmg] tail k=%d from level %zu (%s, %d ops, %d CTAs, %d B shared): "
                         "%.1f us per visit alone\n",
-                k, start, ts.smem_mode ? "shared" : "grid", ts.nops,
-                ts.smem_mode ? k / ts.sl.kl : ts.G, ts.smem_mode ? ts.sl.smem : 0,
-                1e3 * ts.best_ms);
+                k, start, ts.smem_mode ? (ts.cluster ? "shared, clusters" : "shared") : "grid",
+                ts.nops, ts.smem_mode ? k / ts.sl.kl * ts.sl.cluster : ts.G,
+                ts.smem_mode ? ts.sl.smem : 0, 1e3 * ts.best_ms);
     }
     if (!ts.on) return false;
     timed(H, (int)start, LIGMG_KERNEL_TAIL, k, sizeof(T) == 8, ts.bytes,
@@ -3253,18 +3329,31 @@ bool k_supported(int k) {
   return k == 1 || k == 2 || k == 4 || k == 8 || k == 16 || k == 32 || k == 64;
 }
 
+// the message of the last failed call in this thread (ligmg_last_error)
+thread_local std::string g_last_error;
+
 template <typename F>
-ligmg_status guard(F &&f) {
+ligmg_status guard_impl(F &&f) {
   try {
     (void)cudaGetLastError();  // a failed earlier call must not leak into this one
     return f();
   } catch (const Error &e) {
+    g_last_error = e.what();
     return e.status;
   } catch (const std::bad_alloc &) {
+    g_last_error = "host allocation failed";
     return LIGMG_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return LIGMG_ERR_INTERNAL;
   } catch (...) {
+    g_last_error = "unknown error";
     return LIGMG_ERR_INTERNAL;
   }
+}
+template <typename F>
+ligmg_status guard(F &&f) {
+  return guard_impl(std::forward<F>(f));
 }
 
 }  // namespace
@@ -3323,6 +3412,7 @@ void ligmg_default_options(ligmg_options *o) {
   o->wait_spins = 0;
   o->batch_queue = 1;
   o->spmm_streams = 1;
+  o->tail_cluster = 0;
 }
 
 const char *ligmg_status_string(ligmg_status s) {
@@ -3877,6 +3967,19 @@ ligmg_status ligmg_get_stream(ligmg_handle h, void **stream) {
   if (!h || !stream) return LIGMG_ERR_INVALID_ARGUMENT;
   *stream = (void *)h->s;
   return LIGMG_OK;
+}
+
+const char *ligmg_last_error(void) { return g_last_error.c_str(); }
+
+ligmg_status ligmg_measure_gather_peak(int64_t rows, int32_t width, int64_t count,
+                                       double *rows_per_s) {
+  if (!rows_per_s || rows <= 0 || rows > (int64_t)0xffffffff || count <= 0 ||
+      (width != 4 && width != 8 && width != 128))
+    return LIGMG_ERR_INVALID_ARGUMENT;
+  return guard([&]() -> ligmg_status {
+    *rows_per_s = gather_peak(rows, width, count);
+    return LIGMG_OK;
+  });
 }
 
 ligmg_status ligmg_launch_count(int64_t *count) {

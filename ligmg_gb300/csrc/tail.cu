@@ -73,8 +73,64 @@ __device__ __forceinline__ P *res(P *p) {
   return p;
 }
 
+// part / nparts (cluster mode): this CTA's share of the units, whose rows
+// [*rbeg, *rend) it computes; otherwise part = 0, nparts = 1.
+// ---- cluster mode (shared-memory mode launched as clusters of CTAs) --------
+// A column slice is run by a cluster: every CTA holds the whole program and
+// full copies of the slice's work vectors in its shared memory and runs every
+// operation itself (identical inputs, identical order: identical results),
+// except the products with a matrix left in global memory (the larger
+// levels', too large for shared memory): their rows are divided among the
+// cluster's CTAs; each CTA computes its rows into its own copies, the cluster
+// meets at a hardware barrier (every CTA is past the earlier operations,
+// which may read the old values), each CTA writes its rows into every peer's
+// copies (distributed shared memory) and the cluster meets again.  CTAs run
+// ahead of one another only between these products.
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+               "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cluster_size() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void st_peer(unsigned local, unsigned rank, float v) {
+  unsigned ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(local), "r"(rank));
+  asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(ra), "f"(v) : "memory");
+}
+__device__ __forceinline__ void st_peer(unsigned local, unsigned rank, double v) {
+  unsigned ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(local), "r"(rank));
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(ra), "d"(v) : "memory");
+}
+// rows [r0, r1) of a shared-memory vector (n x K) into every peer's copy
+template <typename T, int K, int NT>
+__device__ void cluster_push(const void *tagged, i64 r0, i64 r1, unsigned me, unsigned cs) {
+  const unsigned long long u = (unsigned long long)tagged;
+  if (!tagged || (u & ~kSmemOffMask) != kSmemTag) return;
+  const T *v = reinterpret_cast<const T *>(tail_smem + (u & kSmemOffMask));
+  const unsigned base = (unsigned)__cvta_generic_to_shared(v);
+  for (i64 t = r0 * K + threadIdx.x; t < r1 * K; t += NT) {
+    const T x = v[t];
+    for (unsigned p = 0; p < cs; p++)
+      if (p != me) st_peer(base + (unsigned)(t * (i64)sizeof(T)), p, x);
+  }
+}
+template <typename P>
+__device__ __forceinline__ bool is_global(const P *p) {
+  return ((unsigned long long)p & ~kSmemOffMask) != kSmemTag;
+}
+
 template <typename T, int K, bool SM>
-__device__ void run_spmm(const TOp<T> &op, i64 gwarp, i64 nwarps, int lane) {
+__device__ void run_spmm(const TOp<T> &op, i64 gwarp, i64 nwarps, int lane, int part = 0,
+                         int nparts = 1, i64 *rbeg = nullptr, i64 *rend = nullptr) {
   const i64 units = op.A.n + op.A.nchunks;
   EpiArgs a = op.a;
   MatView<T> A = op.A;
@@ -104,17 +160,24 @@ __device__ void run_spmm(const TOp<T> &op, i64 gwarp, i64 nwarps, int lane) {
   bool narrow = false;
   if constexpr (SM && L <= 8) narrow = (A.rp[A.n] - A.rp[0]) * L <= (i64)64 * A.n;
   const i64 units8 = (A.n + 3) / 4;
+  // this part's units: [u0, u1) of `units` (or of units8, four rows each)
+  const i64 nu = narrow ? units8 : units;
+  const i64 u0 = nu * part / nparts, u1 = nu * (part + 1) / nparts;
+  if (rbeg) {
+    *rbeg = narrow ? min(u0 * 4, A.n) : min(u0, A.n);
+    *rend = narrow ? min(u1 * 4, A.n) : min(u1, A.n);
+  }
   switch (op.epi) {
 #define LG_TAIL_EPI(E)                                                        \
   case E:                                                                     \
     if constexpr (SM && L <= 8) {                                             \
       if (narrow) {                                                           \
-        for (i64 u = gwarp; u < units8; u += nwarps)                          \
+        for (i64 u = u0 + gwarp; u < u1; u += nwarps)                         \
           spmm_unit<T, K, 8, E, !SM>(A, X, a, u, lane);                       \
         break;                                                                \
       }                                                                       \
     }                                                                         \
-    for (i64 u = gwarp; u < units; u += nwarps)                               \
+    for (i64 u = u0 + gwarp; u < u1; u += nwarps)                             \
       spmm_unit<T, K, 32, E, !SM>(A, X, a, u, lane);                          \
     break;
     LG_TAIL_EPI(Epi::Store)
@@ -251,17 +314,26 @@ __global__ void __launch_bounds__(NT, 1)
   // cooperating CTAs: all of them (grid mode) or this one (shared-memory mode)
   const int cta = SM ? 0 : (int)blockIdx.x;
   const int ncta = SM ? 1 : (int)gridDim.x;
+  // cluster mode: this CTA's rank in its cluster and the cluster's size (1:
+  // a plain shared-memory launch); a cluster runs one column slice
+  unsigned crank = 0, csize = 1;
+  if constexpr (SM) {
+    crank = cluster_rank();
+    csize = cluster_size();
+  }
+  const int slice = (int)(blockIdx.x / csize);
   if constexpr (SM) {
     // stage the program, the read-only arrays and this CTA's column slice of
     // the start level's input
     uint4 *dst = reinterpret_cast<uint4 *>(tail_smem);
     for (int w = threadIdx.x; w < image_vec; w += NT) dst[w] = __ldg(image + w);
     T *sin = reinterpret_cast<T *>(tail_smem + io.in_off);
-    const int c0 = (int)blockIdx.x * K;
+    const int c0 = slice * K;
     for (i64 t = threadIdx.x; t < io.n * K; t += NT)
       sin[t] = io.gin[(t / K) * io.kg + c0 + (t % K)];
     __syncthreads();
     ops = reinterpret_cast<const TOp<T> *>(tail_smem);
+    if (csize > 1) cluster_sync_all();  // every peer started before any remote store
   }
   const int lane = threadIdx.x & 31;
   const i64 gwarp = ((i64)cta * NT + threadIdx.x) >> 5;
@@ -284,7 +356,22 @@ __global__ void __launch_bounds__(NT, 1)
     }
     switch (op.kind) {
       case TOpKind::Spmm:
-        run_spmm<T, K, SM>(op, gwarp, nwarps, lane);
+        if (SM && csize > 1 && is_global(op.A.rp)) {
+          // own rows into this CTA's copies; then, once every peer has
+          // finished the operations before this one (a peer may still read
+          // the old values of these outputs there), into the peers' copies
+          i64 r0 = 0, r1 = 0;
+          run_spmm<T, K, SM>(op, gwarp, nwarps, lane, (int)crank, (int)csize, &r0, &r1);
+          __syncthreads();
+          cluster_sync_all();
+          cluster_push<T, K, NT>(op.a.y, r0, r1, crank, csize);
+          cluster_push<T, K, NT>(op.a.rout, r0, r1, crank, csize);
+          cluster_push<T, K, NT>(op.a.dout, r0, r1, crank, csize);
+          cluster_push<T, K, NT>(op.a.xout, r0, r1, crank, csize);
+          cluster_sync_all();
+        } else {
+          run_spmm<T, K, SM>(op, gwarp, nwarps, lane);
+        }
         break;
       case TOpKind::Cheb0: {
         const T f = (T)op.f;
@@ -371,9 +458,11 @@ __global__ void __launch_bounds__(NT, 1)
   }
   if constexpr (SM) {  // write this CTA's column slice of the output back
     const T *sout = reinterpret_cast<const T *>(tail_smem + io.out_off);
-    const int c0 = (int)blockIdx.x * K;
-    for (i64 t = threadIdx.x; t < io.n * K; t += NT)
-      io.gout[(t / K) * io.kg + c0 + (t % K)] = sout[t];
+    const int c0 = slice * K;
+    if (crank == 0)
+      for (i64 t = threadIdx.x; t < io.n * K; t += NT)
+        io.gout[(t / K) * io.kg + c0 + (t % K)] = sout[t];
+    if (csize > 1) cluster_sync_all();  // no peer leaves while stores may target it
   }
 }
 
@@ -399,9 +488,55 @@ void launch_grid(const TOp<T> *ops, int nops, int G, double *partial, TailSync *
 template <typename T, int KL>
 void launch_smem(const TailSmemLaunch &L, int k, TailSync *sync, cudaStream_t s) {
   TailIO<T> io{(const T *)L.gin, (T *)L.gout, L.n, k, L.in_off, L.out_off};
-  k_tail<T, KL, true, kTailSmemThreads><<<k / KL, kTailSmemThreads, L.smem, s>>>(
-      nullptr, L.nops, nullptr, sync, (const uint4 *)L.image, L.image_bytes / 16, io);
+  if (L.cluster > 1) {
+    if (L.cluster > 8)
+      LG_CUDA(cudaFuncSetAttribute(k_tail<T, KL, true, kTailSmemThreads>,
+                                   cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)L.cluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(k / KL * L.cluster));
+    cfg.blockDim = dim3(kTailSmemThreads);
+    cfg.dynamicSmemBytes = (size_t)L.smem;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    LG_CUDA(cudaLaunchKernelEx(&cfg, k_tail<T, KL, true, kTailSmemThreads>,
+                               (const TOp<T> *)nullptr, L.nops, (double *)nullptr, sync,
+                               (const uint4 *)L.image, L.image_bytes / 16, io));
+  } else {
+    k_tail<T, KL, true, kTailSmemThreads><<<k / KL, kTailSmemThreads, L.smem, s>>>(
+        nullptr, L.nops, nullptr, sync, (const uint4 *)L.image, L.image_bytes / 16, io);
+  }
   LG_LAUNCH();
+}
+
+template <typename T, int KL>
+bool cluster_ok_k(int cl, int smem) {
+  if (cl > 8)
+    LG_CUDA(cudaFuncSetAttribute(k_tail<T, KL, true, kTailSmemThreads>,
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)cl;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)cl);
+  cfg.blockDim = dim3(kTailSmemThreads);
+  cfg.dynamicSmemBytes = (size_t)smem;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_tail<T, KL, true, kTailSmemThreads>, &cfg) !=
+      cudaSuccess) {
+    cudaGetLastError();  // not launchable in this shape: clear the error
+    return false;
+  }
+  return n > 0;
 }
 
 template <typename T, int K>
@@ -422,9 +557,15 @@ int smem_limit_k(int want) {
   cudaFuncAttributes fa{};
   LG_CUDA(cudaFuncGetAttributes(&fa, k_tail<T, KL, true, kTailSmemThreads>));
   const int avail = optin - (int)fa.sharedSizeBytes;
-  if (want > 0 && want <= avail)
+  // the opt-in is a property of the kernel, shared by every handle of the
+  // process: it only grows, so a launch prepared by one handle stays valid
+  // after another handle prepares a smaller one
+  static int opted = 0;
+  if (want > opted && want <= avail) {
     LG_CUDA(cudaFuncSetAttribute(k_tail<T, KL, true, kTailSmemThreads>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, want));
+    opted = want;
+  }
   return avail;
 }
 
@@ -450,6 +591,16 @@ void launch_tail_smem(const TailSmemLaunch &L, int k, TailSync *sync, cudaStream
     case 4: return launch_smem<T, 4>(L, k, sync, s);
     case 8: return launch_smem<T, 8>(L, k, sync, s);
     default: throw Error(LIGMG_ERR_UNSUPPORTED, "tail program: columns per CTA must be 1, 4 or 8");
+  }
+}
+
+template <typename T>
+bool tail_cluster_ok(int kl, int cl, int smem) {
+  switch (kl) {
+    case 1: return cluster_ok_k<T, 1>(cl, smem);
+    case 4: return cluster_ok_k<T, 4>(cl, smem);
+    case 8: return cluster_ok_k<T, 8>(cl, smem);
+    default: return false;
   }
 }
 
@@ -483,6 +634,8 @@ template void launch_tail_smem<double>(const TailSmemLaunch &, int, TailSync *, 
 template int tail_max_ctas<float>(int);
 template int tail_max_ctas<double>(int);
 template int tail_smem_prepare<float>(int, int);
+template bool tail_cluster_ok<float>(int, int, int);
+template bool tail_cluster_ok<double>(int, int, int);
 template int tail_smem_prepare<double>(int, int);
 
 }  // namespace lg

@@ -82,14 +82,22 @@ void launch_tail_grid(const TOp<T> *ops, int nops, int k, int G, double *partial
 // runs the program and writes its slice of the result at out_off to gout.
 struct TailSmemLaunch {
   int kl = 0, nops = 0, smem = 0, image_bytes = 0;
+  int cluster = 1;  // CTAs per column slice (cluster mode when > 1)
   const void *image = nullptr;
   const void *gin = nullptr;
   void *gout = nullptr;
   i64 n = 0;
   unsigned in_off = 0, out_off = 0;
 };
+// Cluster mode (L.cluster > 1): k / kl clusters of L.cluster CTAs, the
+// products with matrices outside shared memory divided among a cluster's
+// CTAs (distributed shared memory, hardware cluster barriers).
 template <typename T>
 void launch_tail_smem(const TailSmemLaunch &L, int k, TailSync *sync, cudaStream_t s);
+// Whether clusters of `cl` CTAs with `smem` bytes of dynamic shared memory
+// each can be launched for kl columns per CTA (0 bytes: the opted-in size).
+template <typename T>
+bool tail_cluster_ok(int kl, int cl, int smem);
 
 // CTAs of kTailThreads threads that can be resident at once for the
 // k-column grid-mode kernel (0: unavailable for k).

@@ -336,6 +336,15 @@ class Solver:
         check(lib().ligmg_launch_count(C.byref(x)))
         return x.value
 
+    @staticmethod
+    def gather_peak(rows, width, count):
+        """Random `width`-byte rows (4, 8 or 128) per second that the running
+        GPU gathers from a table of `rows` rows (ligmg_measure_gather_peak)."""
+        x = C.c_double()
+        check(lib().ligmg_measure_gather_peak(int(rows), int(width), int(count), C.byref(x)),
+              "ligmg_measure_gather_peak")
+        return x.value
+
     def solve_batched_device(self, b_ptr, k, x_ptr):
         """Device pointers (n x k row-major FP64) on the handle's device."""
         info, hist, ci, ct = self._info(k)
