@@ -358,11 +358,12 @@ const char *ligmg_last_error(void);
  * gathers from L2, not by HBM.  Times `count` gathers of `width`-byte rows
  * (4, 8 or 128) at pseudo-random positions (read from an index array in
  * order, as a product reads column indices) of a zeroed table of `rows` rows,
- * every SM full of warps with independent gathers in flight, and returns
- * rows per second.  Allocates (rows * width + 4 count bytes) and frees on a
+ * blocks_per_sm blocks of 256 threads per SM (1..8; 0: 8, every warp slot)
+ * with independent gathers in flight, and returns rows per second.
+ * count <= 2^31.  Allocates (rows * width + 4 count bytes) and frees on a
  * private stream. */
 ligmg_status ligmg_measure_gather_peak(int64_t rows, int32_t width, int64_t count,
-                                       double *rows_per_s);
+                                       int32_t blocks_per_sm, double *rows_per_s);
 
 /* Input preparation on the GPU (the reference CLI's --cc / --adj steps,
  * src/main.cpp:70-110, with largest_cc of include/ligmg/cc.hpp:24-106).

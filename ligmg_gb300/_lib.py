@@ -72,7 +72,8 @@ def lib(path=None):
     L.ligmg_launch_count.argtypes = [P(C.c_int64)]
     L.ligmg_last_error.restype = C.c_char_p
     L.ligmg_last_error.argtypes = []
-    L.ligmg_measure_gather_peak.argtypes = [C.c_int64, C.c_int32, C.c_int64, P(C.c_double)]
+    L.ligmg_measure_gather_peak.argtypes = [C.c_int64, C.c_int32, C.c_int64, C.c_int32,
+                                            P(C.c_double)]
     L.ligmg_spmv_device_noalloc.argtypes = [vp, C.c_int32, vp, vp]
     L.ligmg_forward.argtypes = [vp, vp, vp, P(Info)]
     L.ligmg_solve_pcg_jacobi.argtypes = [vp, vp, vp, P(Info)]

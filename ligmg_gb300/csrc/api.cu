@@ -315,7 +315,8 @@ MatView<T> bare_view(const Level &L, int which) {
 //                    warps' chunks (8 U and 16 U are tried there only)
 //   threads/block    {64, 128, 256}: small blocks free their slot as soon as
 //                    their rows finish (rows differ widely in length)
-//   lanes per row    {4, 8, 16, 32} for k = 1 on levels without hub rows
+//   lanes per row    {4, 8, 16, 32} for k = 1 on levels without hub rows;
+//                    32 or 16 (two rows per warp) for k = 8 .. 32
 //   row streams      k >= 8: the row-stream kernel (a warp per run of
 //                    consecutive rows; 1, 2, 4 or 8 runs per resident warp;
 //                    five or six resident blocks per SM) against a warp per
@@ -366,6 +367,9 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
     chunks_seen = cand.nchunks > 0;
     std::vector<int> lane_opts{0};
     if (k == 1 && cand.nchunks == 0) lane_opts = {4, 8, 16, 32};
+    // k = 8 .. 32 without hub rows: also two rows per warp (16 lanes each)
+    const bool half = k >= 8 && k <= 32 && cand.nchunks == 0;
+    if (half) lane_opts = {0, 16};
     float cand_ms = 1e30f;
     int cand_tb = 256, cand_lanes = 0;
     for (int lanes : lane_opts)
@@ -373,7 +377,8 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
         MatView<T> m = base;
         cand.fill(m);
         m.tb = tb;
-        if (lanes) m.lanes_per_row = lanes;
+        if (half) m.krow_lanes = lanes ? lanes : 32;
+        else if (lanes) m.lanes_per_row = lanes;
         EpiArgs a;
         a.y = Y.p;
         spmm<T>(m, X.p, k, epi, a, s);
@@ -431,7 +436,8 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
     if (!have || cand_ms < best_ms) {
       best = std::move(cand);
       best.tb = cand_tb;
-      best.lanes = cand_lanes;
+      best.lanes = half ? 0 : cand_lanes;
+      best.krow_lanes = half && cand_lanes ? cand_lanes : 32;
       best_ms = cand_ms;
       have = true;
     }
@@ -3972,12 +3978,13 @@ ligmg_status ligmg_get_stream(ligmg_handle h, void **stream) {
 const char *ligmg_last_error(void) { return g_last_error.c_str(); }
 
 ligmg_status ligmg_measure_gather_peak(int64_t rows, int32_t width, int64_t count,
-                                       double *rows_per_s) {
-  if (!rows_per_s || rows <= 0 || rows > (int64_t)0xffffffff || count <= 0 ||
+                                       int32_t blocks_per_sm, double *rows_per_s) {
+  if (!rows_per_s || rows <= 0 || rows > (int64_t)INT32_MAX || count <= 0 ||
+      count > ((int64_t)1 << 31) || blocks_per_sm < 0 || blocks_per_sm > 8 ||
       (width != 4 && width != 8 && width != 128))
     return LIGMG_ERR_INVALID_ARGUMENT;
   return guard([&]() -> ligmg_status {
-    *rows_per_s = gather_peak(rows, width, count);
+    *rows_per_s = gather_peak(rows, width, count, blocks_per_sm);
     return LIGMG_OK;
   });
 }

@@ -9,7 +9,9 @@
 // running GPU with the products' own access pattern stripped to the gathers:
 // `count` rows of `width` bytes at pseudo-random positions (an index array
 // read in order, as a product reads its column indices) of a table of `rows`
-// rows, every SM full of warps with independent gathers in flight.
+// rows, every SM full of warps with independent gathers in flight (or
+// `blocks_per_sm` blocks of 256 threads per SM, to see how the rate depends
+// on the gathers in flight).
 #include "peaks.cuh"
 
 namespace lg {
@@ -84,7 +86,7 @@ __global__ void __launch_bounds__(kPeakThreads) k_peak_rows(const float4 *__rest
 
 }  // namespace
 
-double gather_peak(i64 rows, int width, i64 count) {
+double gather_peak(i64 rows, int width, i64 count, int blocks_per_sm) {
   cudaStream_t s;
   LG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   void *tab = nullptr, *sink = nullptr;
@@ -102,7 +104,8 @@ double gather_peak(i64 rows, int width, i64 count) {
     int dev = 0, sms = 0;
     LG_CUDA(cudaGetDevice(&dev));
     LG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const unsigned grid = (unsigned)(sms * kPeakBlocksPerSM);
+    const unsigned grid =
+        (unsigned)(sms * (blocks_per_sm > 0 ? blocks_per_sm : kPeakBlocksPerSM));
     auto launch = [&] {
       if (width == 4)
         k_peak_elems<float, 8><<<grid, kPeakThreads, 0, s>>>((const float *)tab, idx, count,

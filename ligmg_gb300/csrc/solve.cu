@@ -157,6 +157,7 @@ void HubPlan<T>::fill(MatView<T> &m) const {
   m.tdesc = tdesc.p;
   m.tbits = tbits.p;
   m.tile_pipe = tile_pipe;
+  m.krow_lanes = krow_lanes;
   m.nstream = nstream;
   m.srow = srow.p;
   m.stream_blocks = stream_blocks;
@@ -655,6 +656,9 @@ void dispatch_g(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t 
   } else {
     if constexpr (K >= 8) {
       if (A.nstream > 0) return launch_spmm_rs<T, K, EP>(A, X, a, s);
+      // short rows: two rows per warp, half the lanes each (no hub chunks)
+      if constexpr (K <= 32)
+        if (A.krow_lanes == 16 && A.nchunks == 0) return launch_spmm<T, K, 16, EP>(A, X, a, s);
     }
     launch_spmm<T, K, 32, EP>(A, X, a, s);
   }

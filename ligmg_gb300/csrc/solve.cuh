@@ -23,6 +23,7 @@ struct MatView {
   int *hub_counter = nullptr;  // one per hub row, zero between launches
   T *partial = nullptr;        // nchunks x K
   int lanes_per_row = 32;      // 4, 8, 16 or 32 (single-RHS layout)
+  int krow_lanes = 32;         // k = 8 .. 32, a warp per row: 32, or 16 (two rows per warp)
   int tb = 256;                // threads per block of the launch (64, 128 or 256)
   // single right-hand side, tile layout (0 tiles: row layout).  Tile t:
   // tdesc[t] = {first row, rows, e, abase / 4}: its entries are [abase + s,
@@ -70,6 +71,7 @@ struct HubPlan {
   // launch shape kept with the plan (picked by the autotuner or defaults)
   int tb = 256;    // threads per block
   int lanes = 0;   // lanes per row for k = 1 (0: the level's default)
+  int krow_lanes = 32;  // lanes per row for k = 8 .. 32 (32 or 16)
   i64 split = 0;   // target entries per chunk: rows longer than 2 x split are
                    // cut into chunks of about split entries (at most 256 chunks)
   // rows longer than `over` entries (default 2 x split_len) are split

@@ -337,11 +337,13 @@ class Solver:
         return x.value
 
     @staticmethod
-    def gather_peak(rows, width, count):
+    def gather_peak(rows, width, count, blocks_per_sm=0):
         """Random `width`-byte rows (4, 8 or 128) per second that the running
-        GPU gathers from a table of `rows` rows (ligmg_measure_gather_peak)."""
+        GPU gathers from a table of `rows` rows (ligmg_measure_gather_peak);
+        blocks_per_sm 256-thread blocks per SM (0: every warp slot)."""
         x = C.c_double()
-        check(lib().ligmg_measure_gather_peak(int(rows), int(width), int(count), C.byref(x)),
+        check(lib().ligmg_measure_gather_peak(int(rows), int(width), int(count),
+                                              int(blocks_per_sm), C.byref(x)),
               "ligmg_measure_gather_peak")
         return x.value
 
