@@ -193,6 +193,15 @@ typedef struct ligmg_options {
                                  R-MAT 20 it is not: a CTA's eight warps walk
                                  their rows' L2 round trips one row after
                                  another) */
+  int32_t pdl;                /* 1: the solve's kernels are launched with
+                                 programmatic dependent launch: a kernel may
+                                 be scheduled while the one before it runs and
+                                 waits on the device for its completion
+                                 (launch latency overlapped; small grids only
+                                 release their successors early); 0
+                                 (default): ordinary stream order.  Same
+                                 results either way; on R-MAT 20 the solves
+                                 took the same time within run-to-run noise */
 } ligmg_options;
 
 /* ConvergenceInfo (util.hpp:143-170) of one solve.  For a batched solve the

@@ -3218,6 +3218,7 @@ void check_tails(Handle &H) {
 ligmg_status solve_device(Handle &H, int k, int from, const double *dB, double *dX,
                           ligmg_info *info) {
   auto t0 = std::chrono::steady_clock::now();
+  DepLaunchScope dep(H.opts.pdl != 0);
   cudaStream_t s = H.s;
   if (from < 0 || from >= (int)H.h.size()) throw Error(LIGMG_ERR_INVALID_ARGUMENT, "from");
   Level &F = *H.h[from];
@@ -3419,6 +3420,7 @@ void ligmg_default_options(ligmg_options *o) {
   o->batch_queue = 1;
   o->spmm_streams = 1;
   o->tail_cluster = 0;
+  o->pdl = 0;
 }
 
 const char *ligmg_status_string(ligmg_status s) {
@@ -3456,7 +3458,8 @@ ligmg_status ligmg_create(int64_t n, const int64_t *rowptr, const int32_t *col,
       return LIGMG_ERR_INVALID_ARGUMENT;
     if (o.outer_ksp_type == LIGMG_KSP_FGMRES && o.gmres_restart < 1)
       return LIGMG_ERR_INVALID_ARGUMENT;
-    if (o.spmm_streams < 0 || o.spmm_streams > 2 || o.spmv_tiles < 0 || o.spmv_tiles > 2)
+    if (o.spmm_streams < 0 || o.spmm_streams > 2 || o.spmv_tiles < 0 || o.spmv_tiles > 2 ||
+        o.pdl < 0 || o.pdl > 1)
       return LIGMG_ERR_INVALID_ARGUMENT;
     if (o.smoother_type > LIGMG_SMOOTHER_CHEBYSHEV || o.outer_ksp_type > LIGMG_KSP_FGMRES ||
         (o.kcycle_ksp_type != LIGMG_KSP_FCG && o.kcycle_ksp_type != LIGMG_KSP_FGMRES) ||

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <stdexcept>
+#include <utility>
 #include <string>
 #include <vector>
 
@@ -53,6 +54,49 @@ struct SyncFreeScope {
 };
 
 constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+
+// ---- programmatic dependent launch (the solve's kernels) -------------------
+// A kernel launched with launch_dep may be scheduled while the kernel before
+// it on the stream is still running; it first waits (griddepcontrol.wait)
+// until that kernel has completed and its writes are visible, so only its
+// launch latency overlaps.  A grid releases its dependents at its own start
+// only when it is small (at most 1024 threads per SM): the dependents'
+// waiting blocks are then resident beside it and never take the slots a
+// later wave of a large grid would need.  Every kernel launched through
+// launch_dep calls dep_prologue() before its first memory access.
+constexpr long long kDepMaxThreads = (long long)kSMs * 1024;
+__device__ __forceinline__ void dep_prologue() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if ((long long)gridDim.x * gridDim.y * gridDim.z * blockDim.x * blockDim.y * blockDim.z <=
+      kDepMaxThreads)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+// Set (in this thread) while a handle with options.pdl solves.
+extern thread_local bool g_dep_launch;
+struct DepLaunchScope {
+  bool prev;
+  explicit DepLaunchScope(bool on) : prev(g_dep_launch) { g_dep_launch = on; }
+  ~DepLaunchScope() { g_dep_launch = prev; }
+};
+template <typename... KArgs, typename... Args>
+inline void launch_dep(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t s, Args &&...args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = g_dep_launch ? 1 : 0;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    throw Error(LIGMG_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  }
+}
 
 inline i64 cdiv(i64 a, i64 b) { return (a + b - 1) / b; }
 inline unsigned grid_for(i64 work, int per_block) {

@@ -5,6 +5,7 @@ namespace lg {
 
 int64_t g_launches = 0;
 thread_local bool g_free_sync = false;
+thread_local bool g_dep_launch = false;
 
 namespace {
 

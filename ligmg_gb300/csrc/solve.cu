@@ -173,6 +173,7 @@ using namespace dev;
 template <typename T, int K, int G, Epi EP>
 __global__ void __launch_bounds__(256, 6) k_spmm(const MatView<T> A, const T *__restrict__ X,
                                               const EpiArgs a) {
+  dep_prologue();
   const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   dev::spmm_unit<T, K, G, EP>(A, X, a, warp, threadIdx.x & 31);
 }
@@ -406,6 +407,7 @@ __device__ __forceinline__ void tile_unit(const MatView<T> &A, const T *__restri
 template <typename T, Epi EP>
 __global__ void __launch_bounds__(kTileWarps * 32, LG_TILE_MIN_BLOCKS)
     k_spmv_tile(const MatView<T> A, const T *__restrict__ X, const EpiArgs a) {
+  dep_prologue();
   __shared__ T ssum[kTileWarps][kTileRows];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const i64 warp = (i64)blockIdx.x * kTileWarps + w;
@@ -436,6 +438,7 @@ __device__ __forceinline__ int4 shfl_int4(int4 v, int src) {
 template <typename T, Epi EP>
 __global__ void __launch_bounds__(kTileWarps * 32, LG_TILEP_MIN_BLOCKS)
     k_spmv_tile_pipe(const MatView<T> A, const T *__restrict__ X, const EpiArgs a) {
+  dep_prologue();
   __shared__ T ssum[kTileWarps][kTileRows];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // tile counts fit 32 bits (the pipelined launch is used below 2^31 tiles)
@@ -598,6 +601,7 @@ __device__ __forceinline__ void stream_unit(const MatView<T> &A, const T *__rest
 template <typename T, int K, Epi EP, int MINB>
 __global__ void __launch_bounds__(256, MINB)
     k_spmm_rs(const MatView<T> A, const T *__restrict__ X, const EpiArgs a) {
+  dep_prologue();
   const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp < A.nstream) stream_unit<T, K, EP, 4>(A, X, a, warp, lane);
@@ -610,9 +614,9 @@ template <typename T, int K, Epi EP>
 void launch_spmm_rs(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t s) {
   const i64 warps = A.nstream + A.nchunks;
   if (A.stream_blocks == 6)
-    k_spmm_rs<T, K, EP, 6><<<grid_for(warps * 32, 256), 256, 0, s>>>(A, X, a);
+    launch_dep(k_spmm_rs<T, K, EP, 6>, grid_for(warps * 32, 256), 256, 0, s, A, X, a);
   else
-    k_spmm_rs<T, K, EP, 5><<<grid_for(warps * 32, 256), 256, 0, s>>>(A, X, a);
+    launch_dep(k_spmm_rs<T, K, EP, 5>, grid_for(warps * 32, 256), 256, 0, s, A, X, a);
   LG_LAUNCH();
 }
 
@@ -622,7 +626,7 @@ void launch_spmm(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t
   i64 warps = cdiv(A.n, RPW) + ((G == 32) ? A.nchunks : 0);
   if (warps == 0) return;
   const int tb = (A.tb == 64 || A.tb == 128) ? A.tb : 256;
-  k_spmm<T, K, G, EP><<<grid_for(warps * 32, tb), tb, 0, s>>>(A, X, a);
+  launch_dep(k_spmm<T, K, G, EP>, grid_for(warps * 32, tb), tb, 0, s, A, X, a);
   LG_LAUNCH();
 }
 
@@ -638,9 +642,9 @@ void dispatch_g(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t 
                                                                 kTileWarps * 32, 0));
         const i64 g = std::min<i64>((i64)std::max(per_sm, 1) * kSMs,
                                     cdiv(A.ntiles + A.nchunks, kTileWarps));
-        k_spmv_tile_pipe<T, EP><<<(unsigned)g, kTileWarps * 32, 0, s>>>(A, X, a);
+        launch_dep(k_spmv_tile_pipe<T, EP>, (unsigned)g, kTileWarps * 32, 0, s, A, X, a);
       } else {
-        k_spmv_tile<T, EP><<<grid_for(A.ntiles + A.nchunks, kTileWarps), kTileWarps * 32, 0, s>>>(
+        launch_dep(k_spmv_tile<T, EP>, grid_for(A.ntiles + A.nchunks, kTileWarps), kTileWarps * 32, 0, s, 
             A, X, a);
       }
       LG_LAUNCH();
@@ -706,18 +710,21 @@ namespace {
 
 template <typename T>
 __global__ void k_cheb_init_zero(i64 n, int k, const T *b, const T *invd, T scale, T *d) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n * k) d[t] = (invd[t / k] * scale) * b[t];
 }
 
 template <typename T>
 __global__ void k_fill(i64 cnt, T *x, T v) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < cnt) x[t] = v;
 }
 
 template <typename T>
 __global__ void k_prolong_agg(i64 n, int k, const i32 *agg, const T *xc, T *x) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
   i64 i = t / k;
@@ -726,6 +733,7 @@ __global__ void k_prolong_agg(i64 n, int k, const i32 *agg, const T *xc, T *x) {
 
 template <typename T>
 __global__ void k_coarse_apply(i64 n, int k, const T *pinv, const T *b, T *x) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
   i64 i = t / k;
@@ -737,12 +745,14 @@ __global__ void k_coarse_apply(i64 n, int k, const T *pinv, const T *b, T *x) {
 
 template <typename T>
 __global__ void k_scale(i64 nk, T *x, T f) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < nk) x[t] = x[t] * f;
 }
 
 template <typename S, typename D>
 __global__ void k_convert(i64 cnt, const S *src, D *dst) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < cnt) dst[t] = (D)src[t];
 }
@@ -758,6 +768,7 @@ constexpr i64 kRedBig = i64(1) << 17;
 template <typename T, int OP, int BS>
 __global__ void __launch_bounds__(BS) k_colred(i64 n, int k, const T *x, const T *y,
                                                 i64 rows_per_block, double *part) {
+  dep_prologue();
   __shared__ double sh0[BS], sh1[BS];
   const int tid = threadIdx.x;
   const int c = tid % k, rsub = tid / k, rstride = BS / k;
@@ -807,6 +818,7 @@ __global__ void __launch_bounds__(BS) k_colred(i64 n, int k, const T *x, const T
 // a fixed shared-memory tree (deterministic order)
 __global__ void __launch_bounds__(128) k_colred_final(int nb, int width, const double *part,
                                                       double *out) {
+  dep_prologue();
   __shared__ double sh[128];
   const int j = blockIdx.x, tid = threadIdx.x;
   double s = 0;
@@ -830,6 +842,7 @@ int colred_blocks(i64 n, int k) {
 
 template <typename T>
 __global__ void k_sub_mean(i64 n, int k, T *x, const double *colsum, double inv_n) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
   double mu = colsum[t % k] * inv_n;  // a product: an FP64 division per element is slow here
@@ -838,6 +851,7 @@ __global__ void k_sub_mean(i64 n, int k, T *x, const double *colsum, double inv_
 
 template <typename T>
 __global__ void k_axpby(i64 n, int k, T *y, const T *x, const double *alpha, double sa, double sb) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
   double a = alpha ? alpha[t % k] : 1.0;
@@ -846,12 +860,14 @@ __global__ void k_axpby(i64 n, int k, T *y, const T *x, const double *alpha, dou
 
 template <typename T>
 __global__ void k_scale_cols(i64 n, int k, T *y, const T *x, const double *coef) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
   y[t] = (T)((double)x[t] * coef[t % k]);
 }
 
 __global__ void k_rsqrt_cols(int k, const double *sq, double *out) {
+  dep_prologue();
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= k) return;
   const double v = sq[c];
@@ -862,6 +878,7 @@ __global__ void k_rsqrt_cols(int k, const double *sq, double *out) {
 // matrix column by column, then back substitution of the rotated triangle
 // (the arithmetic of the outer FGMRES, all steps at once).
 __global__ void k_gmres_small(int k, int m, const double *Hb, const double *b2, double *y) {
+  dep_prologue();
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= k) return;
   double R[kGmresInnerMax + 1][kGmresInnerMax], cs[kGmresInnerMax], sn[kGmresInnerMax],
@@ -895,6 +912,7 @@ __global__ void k_gmres_small(int k, int m, const double *Hb, const double *b2, 
 
 template <typename T>
 __global__ void k_fcg_direction(i64 n, int k, T *p, const T *z, const T *pp, const double *beta) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
   if (pp) p[t] = z[t] - (T)beta[t % k] * pp[t];
@@ -914,6 +932,7 @@ __device__ __forceinline__ T col_scalar(const double *d, const float *f, int c) 
 template <typename T>
 __global__ void k_fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, const double *alpha,
                              const float *alpha_f, int upd_r, int x_zero) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
   const T a = col_scalar<T>(alpha, alpha_f, (int)(t % k));
@@ -923,6 +942,7 @@ __global__ void k_fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, c
 
 template <typename T>
 __global__ void k_cg_direction(i64 n, int k, T *p, const T *z, const double *beta) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
   p[t] = z[t] + (T)beta[t % k] * p[t];
@@ -930,6 +950,7 @@ __global__ void k_cg_direction(i64 n, int k, T *p, const T *z, const double *bet
 
 __global__ void k_scal_div(int k, const double *num, const double *den, double *out,
                            const int *frozen) {
+  dep_prologue();
   int c = threadIdx.x + blockIdx.x * blockDim.x;
   if (c >= k) return;
   double d = den[c];
@@ -937,6 +958,7 @@ __global__ void k_scal_div(int k, const double *num, const double *den, double *
 }
 
 __global__ void k_scal_beta(int k, const double *zq, const double *eta_prev, double *beta) {
+  dep_prologue();
   int c = threadIdx.x + blockIdx.x * blockDim.x;
   if (c >= k) return;
   double e = eta_prev[c];
@@ -977,6 +999,7 @@ template <typename T, int OP, int BS>
 __global__ void __launch_bounds__(BS)
     k_fused_red(i64 n, int k, const T *x, const T *y, const T *w, i64 rows_per_block,
                 double *scratch, FcgScalars sc, double *out) {
+  dep_prologue();
   constexpr int NV = (OP == 2) ? 3 : (OP == 3 ? 2 : 1);
   __shared__ double sh[NV][BS];
   __shared__ int last;
@@ -1103,6 +1126,7 @@ __global__ void __launch_bounds__(BS)
 template <typename T>
 __global__ void k_fcg_dir(i64 n, int k, T *p, const T *z, const T *pp, FcgScalars sc,
                           float2 *pdf) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
   int c = (int)(t % k);
@@ -1209,6 +1233,7 @@ template <int K, int G>
 __global__ void __launch_bounds__(256) k_spmm_df(const MatView<double> A,
                                                  const float2 *__restrict__ vdf,
                                                  const float2 *__restrict__ X, double *Y) {
+  dep_prologue();
   constexpr int VW = (K % 2 == 0) ? 2 : 1;
   constexpr int L = K / VW;
   static_assert(L <= G && G <= 32 && (G % L) == 0, "bad layout");
@@ -1278,11 +1303,12 @@ void launch_df(const MatView<double> &A, const float2 *vdf, const float2 *X, dou
   constexpr int RPW = 32 / G;
   i64 warps = cdiv(A.n, RPW) + ((G == 32) ? A.nchunks : 0);
   if (warps == 0) return;
-  k_spmm_df<K, G><<<grid_for(warps * 32, 256), 256, 0, s>>>(A, vdf, X, Y);
+  launch_dep(k_spmm_df<K, G>, grid_for(warps * 32, 256), 256, 0, s, A, vdf, X, Y);
   LG_LAUNCH();
 }
 
 __global__ void k_split_df(i64 cnt, const double *v, float2 *o) {
+  dep_prologue();
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cnt) return;
   double x = v[t];
@@ -1463,15 +1489,15 @@ void fcg_beta(i64 n, int k, const T *z, const T *qp, FcgScalars sc, double *scra
               cudaStream_t s) {
   int nb = fused_blocks(n, k);
   if (red_threads(n, k) == kRedBS)
-    k_fused_red<T, 2, kRedBS><<<nb, kRedBS, 0, s>>>(n, k, z, qp, nullptr, cdiv(n, nb), scratch, sc, nullptr);
+    launch_dep(k_fused_red<T, 2, kRedBS>, nb, kRedBS, 0, s, n, k, z, qp, nullptr, cdiv(n, nb), scratch, sc, nullptr);
   else
-    k_fused_red<T, 2, 256><<<nb, 256, 0, s>>>(n, k, z, qp, nullptr, cdiv(n, nb), scratch, sc, nullptr);
+    launch_dep(k_fused_red<T, 2, 256>, nb, 256, 0, s, n, k, z, qp, nullptr, cdiv(n, nb), scratch, sc, nullptr);
   LG_LAUNCH();
 }
 template <typename T>
 void fcg_dir(i64 n, int k, T *p, const T *z, const T *pp, FcgScalars sc, cudaStream_t s,
              float2 *pdf) {
-  k_fcg_dir<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, p, z, pp, sc, pdf);
+  launch_dep(k_fcg_dir<T>, grid_for(n * k, 256), 256, 0, s, n, k, p, z, pp, sc, pdf);
   LG_LAUNCH();
 }
 
@@ -1499,7 +1525,7 @@ void spmm_df(const MatView<double> &A, const float2 *vdf, const float2 *X, int k
 
 void split_df(i64 count, const double *v, float2 *out, cudaStream_t s) {
   if (count <= 0) return;
-  k_split_df<<<grid_for(count, 256), 256, 0, s>>>(count, v, out);
+  launch_dep(k_split_df, grid_for(count, 256), 256, 0, s, count, v, out);
   LG_LAUNCH();
 }
 template <typename T>
@@ -1507,9 +1533,9 @@ void fcg_alpha(i64 n, int k, const T *p, const T *q, const T *r, FcgScalars sc,
                double *scratch, cudaStream_t s) {
   int nb = fused_blocks(n, k);
   if (red_threads(n, k) == kRedBS)
-    k_fused_red<T, 3, kRedBS><<<nb, kRedBS, 0, s>>>(n, k, p, q, r, cdiv(n, nb), scratch, sc, nullptr);
+    launch_dep(k_fused_red<T, 3, kRedBS>, nb, kRedBS, 0, s, n, k, p, q, r, cdiv(n, nb), scratch, sc, nullptr);
   else
-    k_fused_red<T, 3, 256><<<nb, 256, 0, s>>>(n, k, p, q, r, cdiv(n, nb), scratch, sc, nullptr);
+    launch_dep(k_fused_red<T, 3, 256>, nb, 256, 0, s, n, k, p, q, r, cdiv(n, nb), scratch, sc, nullptr);
   LG_LAUNCH();
 }
 template <typename T>
@@ -1517,42 +1543,42 @@ void col_dot1(i64 n, int k, const T *x, const T *y, double *out, double *scratch
   int nb = fused_blocks(n, k);
   FcgScalars none{};
   if (red_threads(n, k) == kRedBS)
-    k_fused_red<T, 1, kRedBS><<<nb, kRedBS, 0, s>>>(n, k, x, y, nullptr, cdiv(n, nb), scratch, none, out);
+    launch_dep(k_fused_red<T, 1, kRedBS>, nb, kRedBS, 0, s, n, k, x, y, nullptr, cdiv(n, nb), scratch, none, out);
   else
-    k_fused_red<T, 1, 256><<<nb, 256, 0, s>>>(n, k, x, y, nullptr, cdiv(n, nb), scratch, none, out);
+    launch_dep(k_fused_red<T, 1, 256>, nb, 256, 0, s, n, k, x, y, nullptr, cdiv(n, nb), scratch, none, out);
   LG_LAUNCH();
 }
 
 template <typename T>
 void cheb_init_zero(i64 n, int k, const T *b, const T *invd, double scale, T *d, cudaStream_t s) {
-  k_cheb_init_zero<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, b, invd, (T)scale, d);
+  launch_dep(k_cheb_init_zero<T>, grid_for(n * k, 256), 256, 0, s, n, k, b, invd, (T)scale, d);
   LG_LAUNCH();
 }
 template <typename T>
 void fill_value(i64 cnt, T *x, T v, cudaStream_t s) {
   if (cnt <= 0) return;
-  k_fill<T><<<grid_for(cnt, 256), 256, 0, s>>>(cnt, x, v);
+  launch_dep(k_fill<T>, grid_for(cnt, 256), 256, 0, s, cnt, x, v);
   LG_LAUNCH();
 }
 template <typename T>
 void prolong_agg(i64 n, int k, const i32 *agg, const T *xc, T *x, cudaStream_t s) {
-  k_prolong_agg<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, agg, xc, x);
+  launch_dep(k_prolong_agg<T>, grid_for(n * k, 256), 256, 0, s, n, k, agg, xc, x);
   LG_LAUNCH();
 }
 template <typename T>
 void coarse_apply(i64 n, int k, const T *pinv, const T *b, T *x, cudaStream_t s) {
-  k_coarse_apply<T><<<grid_for(n * k, 128), 128, 0, s>>>(n, k, pinv, b, x);
+  launch_dep(k_coarse_apply<T>, grid_for(n * k, 128), 128, 0, s, n, k, pinv, b, x);
   LG_LAUNCH();
 }
 template <typename T>
 void scale_vec(i64 n, int k, T *x, double f, cudaStream_t s) {
-  k_scale<T><<<grid_for(n * k, 256), 256, 0, s>>>(n * k, x, (T)f);
+  launch_dep(k_scale<T>, grid_for(n * k, 256), 256, 0, s, n * k, x, (T)f);
   LG_LAUNCH();
 }
 template <typename S, typename D>
 void convert(i64 count, const S *src, D *dst, cudaStream_t s) {
   if (count <= 0) return;
-  k_convert<S, D><<<grid_for(count, 256), 256, 0, s>>>(count, src, dst);
+  launch_dep(k_convert<S, D>, grid_for(count, 256), 256, 0, s, count, src, dst);
   LG_LAUNCH();
 }
 
@@ -1569,75 +1595,75 @@ void col_reduce(i64 n, int k, Red op, const T *x, const T *y, double *out, doubl
   int width = k;
   switch (op) {
     case Red::Sum:
-      if (big) k_colred<T, 0, kRedBS><<<nb, kRedBS, 0, s>>>(n, k, x, y, rpb, scratch);
-      else k_colred<T, 0, 256><<<nb, 256, 0, s>>>(n, k, x, y, rpb, scratch);
+      if (big) launch_dep(k_colred<T, 0, kRedBS>, nb, kRedBS, 0, s, n, k, x, y, rpb, scratch);
+      else launch_dep(k_colred<T, 0, 256>, nb, 256, 0, s, n, k, x, y, rpb, scratch);
       break;
     case Red::Dot:
-      if (big) k_colred<T, 1, kRedBS><<<nb, kRedBS, 0, s>>>(n, k, x, y, rpb, scratch);
-      else k_colred<T, 1, 256><<<nb, 256, 0, s>>>(n, k, x, y, rpb, scratch);
+      if (big) launch_dep(k_colred<T, 1, kRedBS>, nb, kRedBS, 0, s, n, k, x, y, rpb, scratch);
+      else launch_dep(k_colred<T, 1, 256>, nb, 256, 0, s, n, k, x, y, rpb, scratch);
       break;
     case Red::Sum2Dot:
-      if (big) k_colred<T, 2, kRedBS><<<nb, kRedBS, 0, s>>>(n, k, x, y, rpb, scratch);
-      else k_colred<T, 2, 256><<<nb, 256, 0, s>>>(n, k, x, y, rpb, scratch);
+      if (big) launch_dep(k_colred<T, 2, kRedBS>, nb, kRedBS, 0, s, n, k, x, y, rpb, scratch);
+      else launch_dep(k_colred<T, 2, 256>, nb, 256, 0, s, n, k, x, y, rpb, scratch);
       width = 2 * k;
       break;
   }
   LG_LAUNCH();
-  k_colred_final<<<width, 128, 0, s>>>(nb, width, scratch, out);
+  launch_dep(k_colred_final, width, 128, 0, s, nb, width, scratch, out);
   LG_LAUNCH();
 }
 
 template <typename T>
 void sub_mean(i64 n, int k, T *x, const double *colsum, cudaStream_t s) {
-  k_sub_mean<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, x, colsum, 1.0 / (double)n);
+  launch_dep(k_sub_mean<T>, grid_for(n * k, 256), 256, 0, s, n, k, x, colsum, 1.0 / (double)n);
   LG_LAUNCH();
 }
 template <typename T>
 void axpby_cols(i64 n, int k, T *y, const T *x, const double *alpha, double sa, double sb,
                 cudaStream_t s) {
-  k_axpby<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, y, x, alpha, sa, sb);
+  launch_dep(k_axpby<T>, grid_for(n * k, 256), 256, 0, s, n, k, y, x, alpha, sa, sb);
   LG_LAUNCH();
 }
 template <typename T>
 void scale_cols(i64 n, int k, T *y, const T *x, const double *coef, cudaStream_t s) {
-  k_scale_cols<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, y, x, coef);
+  launch_dep(k_scale_cols<T>, grid_for(n * k, 256), 256, 0, s, n, k, y, x, coef);
   LG_LAUNCH();
 }
 void rsqrt_cols(int k, const double *sq, double *out, cudaStream_t s) {
-  k_rsqrt_cols<<<1, 64 * cdiv(k, 64), 0, s>>>(k, sq, out);
+  launch_dep(k_rsqrt_cols, 1, 64 * cdiv(k, 64), 0, s, k, sq, out);
   LG_LAUNCH();
 }
 void gmres_small(int k, int m, const double *Hb, const double *b2, double *y, cudaStream_t s) {
   if (m < 1 || m > kGmresInnerMax) throw Error(LIGMG_ERR_INVALID_ARGUMENT, "inner FGMRES steps");
-  k_gmres_small<<<1, 64 * cdiv(k, 64), 0, s>>>(k, m, Hb, b2, y);
+  launch_dep(k_gmres_small, 1, 64 * cdiv(k, 64), 0, s, k, m, Hb, b2, y);
   LG_LAUNCH();
 }
 template <typename T>
 void fcg_direction(i64 n, int k, T *p, const T *z, const T *pprev, const double *beta,
                    cudaStream_t s) {
-  k_fcg_direction<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, p, z, pprev, beta);
+  launch_dep(k_fcg_direction<T>, grid_for(n * k, 256), 256, 0, s, n, k, p, z, pprev, beta);
   LG_LAUNCH();
 }
 template <typename T>
 void fcg_update(i64 n, int k, T *x, T *r, const T *p, const T *q, const double *alpha,
                 bool update_r, cudaStream_t s, const float *alpha_f, bool x_zero) {
-  k_fcg_update<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, x, r, p, q, alpha, alpha_f,
+  launch_dep(k_fcg_update<T>, grid_for(n * k, 256), 256, 0, s, n, k, x, r, p, q, alpha, alpha_f,
                                                        update_r ? 1 : 0, x_zero ? 1 : 0);
   LG_LAUNCH();
 }
 template <typename T>
 void cg_direction(i64 n, int k, T *p, const T *z, const double *beta, cudaStream_t s) {
-  k_cg_direction<T><<<grid_for(n * k, 256), 256, 0, s>>>(n, k, p, z, beta);
+  launch_dep(k_cg_direction<T>, grid_for(n * k, 256), 256, 0, s, n, k, p, z, beta);
   LG_LAUNCH();
 }
 
 void scal_div(int k, const double *num, const double *den, double *out, const int *frozen,
               cudaStream_t s) {
-  k_scal_div<<<1, 128, 0, s>>>(k, num, den, out, frozen);
+  launch_dep(k_scal_div, 1, 128, 0, s, k, num, den, out, frozen);
   LG_LAUNCH();
 }
 void scal_beta(int k, const double *zq, const double *eta_prev, double *beta, cudaStream_t s) {
-  k_scal_beta<<<1, 128, 0, s>>>(k, zq, eta_prev, beta);
+  launch_dep(k_scal_beta, 1, 128, 0, s, k, zq, eta_prev, beta);
   LG_LAUNCH();
 }
 

@@ -308,6 +308,7 @@ __global__ void __launch_bounds__(NT, 1)
     k_tail(const TOp<T> *__restrict__ ops, int nops, double *partial, TailSync *gs,
            const uint4 *__restrict__ image, int image_vec, TailIO<T> io) {
   static_assert(NT % K == 0 && NT >= 64, "tail block size");
+  dep_prologue();
   __shared__ double sh[3][NT];
   __shared__ T scal[2][64];  // column scalars in the data's type (converted once)
   __shared__ int sh_abort;
@@ -508,8 +509,9 @@ void launch_smem(const TailSmemLaunch &L, int k, TailSync *sync, cudaStream_t s)
                                (const TOp<T> *)nullptr, L.nops, (double *)nullptr, sync,
                                (const uint4 *)L.image, L.image_bytes / 16, io));
   } else {
-    k_tail<T, KL, true, kTailSmemThreads><<<k / KL, kTailSmemThreads, L.smem, s>>>(
-        nullptr, L.nops, nullptr, sync, (const uint4 *)L.image, L.image_bytes / 16, io);
+    launch_dep(k_tail<T, KL, true, kTailSmemThreads>, k / KL, kTailSmemThreads, (size_t)L.smem, s,
+               (const TOp<T> *)nullptr, L.nops, (double *)nullptr, sync, (const uint4 *)L.image,
+               L.image_bytes / 16, io);
   }
   LG_LAUNCH();
 }
