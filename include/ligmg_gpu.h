@@ -193,6 +193,15 @@ typedef struct ligmg_options {
                                  R-MAT 20 it is not: a CTA's eight warps walk
                                  their rows' L2 round trips one row after
                                  another) */
+  int32_t spmm_tiles;         /* products with 2 or more right-hand sides and
+                                 rows of at most 128 bytes (FP32 k <= 32, FP64
+                                 k <= 16): 1 (default): with autotune, tiles
+                                 of whole rows walked in steps of consecutive
+                                 entries across row boundaries (no step half
+                                 empty on short rows) are timed against the
+                                 other layouts and kept where faster; 0:
+                                 never; 2: always.  Sums are taken in a
+                                 different fixed order than a warp per row */
   int32_t pdl;                /* 1: the solve's kernels are launched with
                                  programmatic dependent launch: a kernel may
                                  be scheduled while the one before it runs and

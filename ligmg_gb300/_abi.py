@@ -82,6 +82,7 @@ class Options(C.Structure):
         ("batch_queue", C.c_int32),
         ("spmm_streams", C.c_int32),
         ("tail_cluster", C.c_int32),
+        ("spmm_tiles", C.c_int32),
         ("pdl", C.c_int32),
     ]
 
@@ -154,6 +155,7 @@ def default_options(**overrides) -> Options:
     o.batch_queue = 1
     o.spmm_streams = 1
     o.tail_cluster = 0
+    o.spmm_tiles = 1
     o.pdl = 0
     for k, v in overrides.items():
         if k in ("smoother_type",) and isinstance(v, str):

@@ -221,6 +221,7 @@ struct Level {
   bool autotune = true;  // options.autotune at creation
   int tiles = 1;         // options.spmv_tiles at creation
   int streams = 1;       // options.spmm_streams at creation
+  int ktiles = 1;        // options.spmm_tiles at creation
   // Chebyshev coefficients
   double theta = 1, delta = 1;
   std::vector<double> c1, c2;
@@ -317,6 +318,8 @@ MatView<T> bare_view(const Level &L, int which) {
 //                    their rows finish (rows differ widely in length)
 //   lanes per row    {4, 8, 16, 32} for k = 1 on levels without hub rows;
 //                    32 or 16 (two rows per warp) for k = 8 .. 32
+//   k-column tiles   rows of at most 128 bytes: tiles of whole rows in steps
+//                    of consecutive entries (k_spmm_ktile)
 //   row streams      k >= 8: the row-stream kernel (a warp per run of
 //                    consecutive rows; 1, 2, 4 or 8 runs per resident warp;
 //                    five or six resident blocks per SM) against a warp per
@@ -334,6 +337,8 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
   // lane's run of entries on average
   const bool tile_ok = k == 1 && L.tiles && n > 0 &&
                        (double)(rp[n] - rp[0]) >= kTileMinMeanRow * (double)n;
+  // k columns: tiles of whole rows for rows of at most 128 bytes
+  const bool ktile_ok = k >= 2 && k * (int)sizeof(T) <= 128 && L.ktiles != 0 && n > 0;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   LG_CUDA(cudaStreamIsCapturing(s, &cs));
   if (!autotune || cs != cudaStreamCaptureStatusNone || n <= 0) {
@@ -345,6 +350,11 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
     }
     best.tb = k > 1 ? 64 : 256;
     if (k >= 8 && L.streams == 2 && n > 0) best.build_stream(rp.data(), n, 2048, 5, s);
+    if (ktile_ok && L.ktiles == 2) {
+      HubPlan<T> cand;
+      cand.build_tiles(rp.data(), n, s, k);
+      if (cand.ntiles > 0) best = std::move(cand);
+    }
     return;
   }
   MatView<T> base = bare_view<T>(L, which);
@@ -443,6 +453,29 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
     }
   }
   if (k >= 8 && L.streams == 2 && best.nstream == 0) best.build_stream(rp.data(), n, 2048, 5, s);
+  if (ktile_ok) {
+    HubPlan<T> cand;
+    cand.build_tiles(rp.data(), n, s, k);
+    if (cand.ntiles > 0) {
+      MatView<T> m = base;
+      cand.fill(m);
+      EpiArgs a;
+      a.y = Y.p;
+      spmm<T>(m, X.p, k, epi, a, s);
+      LG_CUDA(cudaEventRecord(e0, s));
+      for (int r = 0; r < 3; r++) spmm<T>(m, X.p, k, epi, a, s);
+      LG_CUDA(cudaEventRecord(e1, s));
+      LG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      LG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (!have || ms < best_ms || L.ktiles == 2) {
+        best = std::move(cand);
+        best.tb = 256;
+        best_ms = ms;
+        have = true;
+      }
+    }
+  }
   if (tile_ok) {
     HubPlan<T> cand;
     cand.build_tiles(rp.data(), n, s);
@@ -1994,6 +2027,7 @@ void finish_level(Handle &H, Level &L) {
   L.autotune = H.opts.autotune != 0;
   L.tiles = H.opts.spmv_tiles;
   L.streams = H.opts.spmm_streams;
+  L.ktiles = H.opts.spmm_tiles;
   L.rp_host = L.A.rp.to_host();
   // the FP64 single right-hand-side plan of A is built (and, with autotune,
   // its layout and launch shape timed) at setup: ligmg_spmv_device_noalloc
@@ -3420,6 +3454,7 @@ void ligmg_default_options(ligmg_options *o) {
   o->batch_queue = 1;
   o->spmm_streams = 1;
   o->tail_cluster = 0;
+  o->spmm_tiles = 1;
   o->pdl = 0;
 }
 
@@ -3459,7 +3494,7 @@ ligmg_status ligmg_create(int64_t n, const int64_t *rowptr, const int32_t *col,
     if (o.outer_ksp_type == LIGMG_KSP_FGMRES && o.gmres_restart < 1)
       return LIGMG_ERR_INVALID_ARGUMENT;
     if (o.spmm_streams < 0 || o.spmm_streams > 2 || o.spmv_tiles < 0 || o.spmv_tiles > 2 ||
-        o.pdl < 0 || o.pdl > 1)
+        o.pdl < 0 || o.pdl > 1 || o.spmm_tiles < 0 || o.spmm_tiles > 2)
       return LIGMG_ERR_INVALID_ARGUMENT;
     if (o.smoother_type > LIGMG_SMOOTHER_CHEBYSHEV || o.outer_ksp_type > LIGMG_KSP_FGMRES ||
         (o.kcycle_ksp_type != LIGMG_KSP_FCG && o.kcycle_ksp_type != LIGMG_KSP_FGMRES) ||

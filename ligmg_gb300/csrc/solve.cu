@@ -68,11 +68,11 @@ void HubPlan<T>::build(const i64 *rp_host, i64 n, i64 split_len, int kmax, cudaS
 }
 
 template <typename T>
-void HubPlan<T>::build_tiles(const i64 *rp_host, i64 n, cudaStream_t s) {
+void HubPlan<T>::build_tiles(const i64 *rp_host, i64 n, cudaStream_t s, int kmax) {
   // rows of up to kTilePos - 4 entries always fit a tile (after rounding the
   // start down by at most three); longer ones become hub rows, cut into
   // chunks of about 1024 entries (at least two)
-  build(rp_host, n, 1024, 1, s, kTilePos - 4);
+  build(rp_host, n, 1024, kmax, s, kTilePos - 4);
   const i64 nnz = rp_host[n];
   std::vector<int4> desc;
   std::vector<u32> bits;
@@ -620,6 +620,197 @@ void launch_spmm_rs(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStrea
   LG_LAUNCH();
 }
 
+// ---- k right-hand sides, tiles of whole rows --------------------------------
+// On levels with short rows a warp per row (or per run of rows) spends most
+// 16-entry steps partly masked: a 33-entry row takes three.  Here a warp
+// takes a tile of whole rows (the single right-hand side layout: at most
+// kTilePos entries from a 4-aligned start, row-start bitmap) and walks its
+// entries in steps of U E consecutive entries whatever the rows: slot s (L
+// lanes, VW columns each) takes U contiguous entries, adds them in order,
+// closes the rows that start and end inside them into shared memory, and a
+// segmented scan across the slots (restarted at a slot holding a row start)
+// completes the rows that cross slots; the row still open at a step's end is
+// carried into the next step's first slot.  The next step's column indices
+// and values are loaded during this step's gathers.  Summation order is
+// fixed (entry order in a slot, the scan's tree across slots, step order).
+constexpr int kKTileWarps = 8;
+// row sums of a warp's tile live in static shared memory: rows of at most 128
+// bytes (FP32 k <= 32, FP64 k <= 16)
+template <typename T, int K>
+constexpr bool ktile_fits() {
+  return K >= 2 && K * (int)sizeof(T) <= 128;
+}
+
+template <typename T, int K, Epi EP>
+__device__ __forceinline__ void ktile_load(const MatView<T> &A, i64 ab, int p0, int e_rel,
+                                           i32 (&c)[4], T (&v)[4]) {
+  constexpr int VWV = 16 / (int)sizeof(T);
+  if (p0 + 4 <= e_rel) {
+    const int4 cc = ld_stream_i4(A.ci + ab + p0);
+    c[0] = cc.x;
+    c[1] = cc.y;
+    c[2] = cc.z;
+    c[3] = cc.w;
+#pragma unroll
+    for (int h = 0; h < 4 / VWV; h++) {
+      T tv[VWV];
+      ld_stream_v(A.v + ab + p0 + h * VWV, tv);
+#pragma unroll
+      for (int q = 0; q < VWV; q++) v[h * VWV + q] = tv[q];
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const bool in = p0 + u < e_rel;
+      c[u] = in ? __ldg(A.ci + ab + p0 + u) : 0;
+      v[u] = in ? __ldg(A.v + ab + p0 + u) : (T)0;
+    }
+  }
+}
+
+template <typename T, int K, Epi EP>
+__device__ __forceinline__ void ktile_unit(const MatView<T> &A, const T *__restrict__ X,
+                                           const EpiArgs &a, i64 t, int lane, T *ssum) {
+  constexpr bool SPLIT = EP == Epi::Split;
+  constexpr int VW = (K % VT<T>::W == 0) ? VT<T>::W : 1;
+  constexpr int L = K / VW;  // lanes per entry
+  constexpr int E = 32 / L;  // slots
+  constexpr int U = 4;       // contiguous entries per slot and step
+  constexpr int STEP = U * E;
+  constexpr int NW = kTilePos / 32;  // bitmap words
+  static_assert(NW <= 32 && STEP % 4 == 0, "tile layout");
+  const int slot = lane / L, ch = lane % L;
+  const int4 d = __ldg(A.tdesc + t);
+  const int r0 = d.x, nr = d.y, e_rel = d.z;
+  const i64 ab = (i64)d.w << 2;
+  // lane w < NW: bitmap word w and the row starts in the words before it
+  const u32 wl = lane < NW ? __ldg(A.tbits + t * NW + lane) : 0u;
+  int pw = __popc(wl);
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, pw, o);
+    if (lane >= o) pw += y;
+  }
+  pw -= __popc(wl);  // exclusive
+  const int nsteps = (e_rel + STEP - 1) / STEP;
+  for (int i = 0; i < nr; i++) epilogue_prefetch_rows<T, K, EP>(a, (i64)r0 + i, lane);
+  T carry[VW];
+#pragma unroll
+  for (int q = 0; q < VW; q++) carry[q] = (T)0;
+  i32 cn[4];
+  T vn[4];
+  ktile_load<T, K, EP>(A, ab, slot * U, e_rel, cn, vn);
+  for (int j = 0; j < nsteps; j++) {
+    const int p0 = j * STEP + slot * U;  // this slot's first entry (from ab)
+    i32 c[4];
+    T va[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      c[u] = cn[u];
+      va[u] = vn[u];
+    }
+    if (j + 1 < nsteps) ktile_load<T, K, EP>(A, ab, p0 + STEP, e_rel, cn, vn);
+    // this slot's entries of the tile: [s_rel, e_rel) (s_rel < 4: the first
+    // row start, in word 0)
+    const u32 w0 = __shfl_sync(0xffffffffu, wl, 0);
+    const int s_rel = __ffs(w0) - 1;
+    T x[4][VW];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const bool ok = p0 + u >= s_rel && p0 + u < e_rel;
+      if (ok) {
+        xload<T, VW, true>(xsrc<T, K, SPLIT>(A, X, c[u]) + ch * VW, x[u]);
+      } else {
+        va[u] = (T)0;
+#pragma unroll
+        for (int q = 0; q < VW; q++) x[u][q] = (T)0;
+      }
+    }
+    const int wi = p0 >> 5;
+    const u32 wd = __shfl_sync(0xffffffffu, wl, wi < NW ? wi : 0);
+    const u32 b4 = wi < NW ? (wd >> (p0 & 31)) & 0xFu : 0u;
+    const int pre = __shfl_sync(0xffffffffu, pw, wi < NW ? wi : 0) +
+                    (wi < NW ? __popc(wd & ((1u << (p0 & 31)) - 1u)) : 0);
+    T run[VW], hs[VW];
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      run[q] = slot == 0 ? carry[q] : (T)0;
+      hs[q] = (T)0;
+    }
+    bool cont = true, brk = false;
+    int ri = pre - 1;  // the row open at this slot's first entry
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      if ((b4 >> u) & 1u) {  // a row starts: close the open one
+        if (cont) {
+#pragma unroll
+          for (int q = 0; q < VW; q++) hs[q] = run[q];
+        } else {
+#pragma unroll
+          for (int q = 0; q < VW; q++) ssum[ri * K + ch * VW + q] = run[q];
+        }
+        cont = false;
+        brk = true;
+        ri++;
+#pragma unroll
+        for (int q = 0; q < VW; q++) run[q] = (T)0;
+      }
+#pragma unroll
+      for (int q = 0; q < VW; q++) run[q] += va[u] * x[u][q];
+    }
+    // inclusive scan of the slots' open sums, restarted at a slot with a row start
+    T S[VW];
+#pragma unroll
+    for (int q = 0; q < VW; q++) S[q] = run[q];
+    int f = brk;
+#pragma unroll
+    for (int o = 1; o < E; o <<= 1) {
+      T su[VW];
+#pragma unroll
+      for (int q = 0; q < VW; q++) su[q] = __shfl_up_sync(0xffffffffu, S[q], o * L);
+      const int fu = __shfl_up_sync(0xffffffffu, f, o * L);
+      if (slot >= o) {
+        if (!f)
+#pragma unroll
+          for (int q = 0; q < VW; q++) S[q] += su[q];
+        f |= fu;
+      }
+    }
+    T sp[VW];
+#pragma unroll
+    for (int q = 0; q < VW; q++) sp[q] = __shfl_up_sync(0xffffffffu, S[q], L);
+    // the row open at this slot's start ends inside it: previous slots' open
+    // sum (the carry is in slot 0's own head) plus this slot's head
+    if (brk && pre > 0)
+#pragma unroll
+      for (int q = 0; q < VW; q++) ssum[(pre - 1) * K + ch * VW + q] = (slot > 0 ? sp[q] : (T)0) + hs[q];
+#pragma unroll
+    for (int q = 0; q < VW; q++) carry[q] = __shfl_sync(0xffffffffu, S[q], (E - 1) * L + ch);
+  }
+  if (slot == 0)  // the tile's last row ends with the tile
+#pragma unroll
+    for (int q = 0; q < VW; q++) ssum[(nr - 1) * K + ch * VW + q] = carry[q];
+  __syncwarp();
+  for (int i = slot; i < nr; i += E) {
+    T acc[VW];
+#pragma unroll
+    for (int q = 0; q < VW; q++) acc[q] = ssum[i * K + ch * VW + q];
+    epilogue<T, K, VW, EP>(a, (i64)r0 + i, ch * VW, acc);
+  }
+  __syncwarp();
+}
+
+template <typename T, int K, Epi EP>
+__global__ void __launch_bounds__(kKTileWarps * 32, 4)
+    k_spmm_ktile(const MatView<T> A, const T *__restrict__ X, const EpiArgs a) {
+  dep_prologue();
+  __shared__ T ssum[kKTileWarps][kTileRows * K];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const i64 warp = (i64)blockIdx.x * kKTileWarps + w;
+  if (warp < A.ntiles) ktile_unit<T, K, EP>(A, X, a, warp, lane, ssum[w]);
+  else dev::hub_unit<T, K, EP>(A, X, a, warp - A.ntiles, lane);
+}
+
 template <typename T, int K, int G, Epi EP>
 void launch_spmm(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t s) {
   constexpr int RPW = 32 / G;
@@ -658,6 +849,14 @@ void dispatch_g(const MatView<T> &A, const T *X, const EpiArgs &a, cudaStream_t 
       default: return launch_spmm<T, 1, 32, EP>(A, X, a, s);
     }
   } else {
+    if constexpr (ktile_fits<T, K>()) {
+      if (A.ntiles > 0 && (((uintptr_t)A.ci | (uintptr_t)A.v) & 15) == 0) {
+        launch_dep(k_spmm_ktile<T, K, EP>, grid_for(A.ntiles + A.nchunks, kKTileWarps),
+                   kKTileWarps * 32, 0, s, A, X, a);
+        LG_LAUNCH();
+        return;
+      }
+    }
     if constexpr (K >= 8) {
       if (A.nstream > 0) return launch_spmm_rs<T, K, EP>(A, X, a, s);
       // short rows: two rows per warp, half the lanes each (no hub chunks)

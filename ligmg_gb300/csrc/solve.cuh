@@ -78,7 +78,7 @@ struct HubPlan {
   void build(const i64 *rp_host, i64 n, i64 split_len, int kmax, cudaStream_t s, i64 over = 0);
   // k = 1 tile layout: rows longer than a tile holds are hub rows (the split
   // is set so); the other rows are packed into tiles in order
-  void build_tiles(const i64 *rp_host, i64 n, cudaStream_t s);
+  void build_tiles(const i64 *rp_host, i64 n, cudaStream_t s, int kmax = 1);
   // k > 1 row streams over the rows of this plan (hub rows, already set by
   // build, count as empty): consecutive rows until a stream holds about
   // `per_stream` entries (a row costs its entries plus 16).  Not built

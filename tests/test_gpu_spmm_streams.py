@@ -76,3 +76,28 @@ def test_invalid_stream_option_rejected():
     with pytest.raises(LigmgError) as e:
         Solver(G.grid2d(8), spmm_streams=3)
     assert e.value.status == 2
+
+
+@pytest.mark.parametrize("prec,k", [("fp32", 32), ("fp32", 8), ("fp64", 16)])
+@pytest.mark.parametrize("name", list(GRAPHS))
+def test_k_column_tiles_match_row_kernel(name, prec, k):
+    # spmm_tiles = 2: tiles of whole rows walked in steps of consecutive
+    # entries across row boundaries (segmented sums across the warp's
+    # slots); a different fixed summation order than a warp per row, so the
+    # solves agree to rounding: same iterations (within one), solutions to
+    # 1e-6 (FP32 hierarchy) or 1e-9 (FP64), both at the tolerance
+    L = GRAPHS[name]()
+    B = G.rhs(L.n, k=k, seed=13).reshape(L.n, k)
+    kw = dict(precision=prec, kcycle=1, outer_ksp_type="fcg", autotune=0)
+    a = Solver(L, spmm_tiles=2, **kw).solve_batched(B)
+    c = Solver(L, spmm_tiles=0, **kw).solve_batched(B)
+    assert a.converged and c.converged
+    assert abs(a.iters() - c.iters()) <= 1
+    assert a.true_rel_residual <= 2e-8
+    x = a.solution - a.solution.mean(axis=0)
+    y = c.solution - c.solution.mean(axis=0)
+    tol = 1e-6 if prec == "fp32" else 1e-9
+    assert np.linalg.norm(x - y) <= tol * np.linalg.norm(y)
+    # deterministic: a second solve on the same handle is the same bits
+    again = Solver(L, spmm_tiles=2, **kw).solve_batched(B)
+    assert np.array_equal(again.solution, a.solution)
