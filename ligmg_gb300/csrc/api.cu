@@ -221,6 +221,10 @@ struct Level {
   bool autotune = true;  // options.autotune at creation
   int tiles = 1;         // options.spmv_tiles at creation
   int streams = 1;       // options.spmm_streams at creation
+  // row streams of A for the double-float outer product (built on first use;
+  // -1: not yet, 0: none)
+  DBuf<i32> dfsrow;
+  i64 dfnstream = -1;
   int ktiles = 1;        // options.spmm_tiles at creation
   // Chebyshev coefficients
   double theta = 1, delta = 1;
@@ -524,6 +528,32 @@ const HubPlan<T> &plan_for(const Level &L, int which, int k, cudaStream_t s) {
   HubPlan<T> &p = plans<T>(L, which)[k];
   if (!p.built) build_plan<T>(L, which, k, p, L.autotune, s);
   return p;
+}
+
+// The view of A for the double-float outer product with k columns: A's
+// hub-row chunks (from the FP64 plan for k) and, for k >= 8, row streams of
+// its other rows, one run per four resident warps' worth of entries (built
+// on first use, outside graph capture).
+MatView<double> df_view(Level &L, MatView<double> A, int k, cudaStream_t s) {
+  if (k < 8 || L.streams == 0) return A;
+  if (L.dfnstream < 0) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    LG_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return A;
+    const i64 n = A.n;
+    const i64 cost = (L.rp_host[n] - L.rp_host[0]) + 16 * n;
+    const i64 per = std::max<i64>(64, cdiv(cost, (i64)kSMs * 4 * 8 * 4));
+    std::vector<i32> st = row_stream_starts(L.rp_host.data(), n, A.hub_thresh, per);
+    L.dfnstream = st.size() >= 2 ? (i64)st.size() - 1 : 0;
+    if (L.dfnstream > 0) {
+      L.dfsrow.alloc((i64)st.size(), s);
+      L.dfsrow.upload(st.data(), (i64)st.size());
+      LG_CUDA(cudaStreamSynchronize(s));
+    }
+  }
+  A.nstream = L.dfnstream;
+  A.srow = L.dfsrow.p;
+  return A;
 }
 
 template <typename T>
@@ -2467,7 +2497,7 @@ SolveResult outer_solve(Handle &H, size_t base, OuterWork &w, int k) {
       a.y = Q;
       timed(H, (int)base, LIGMG_KERNEL_SPMV, k, 1, core_bytes(n, L.A.nnz, n, k, 8) + 8.0 * n * k,
             [&] {
-              if (dfprod) spmm_df(A, L.Adf.p, w.Pdf.p, k, Q, s);
+              if (dfprod) spmm_df(df_view(L, A, k, s), L.Adf.p, w.Pdf.p, k, Q, s);
               else spmm<double>(A, P, k, Epi::Store, a, s);
             });
       timed(H, (int)base, LIGMG_KERNEL_OUTER, k, 1, 9.0 * nk, [&] {

@@ -116,23 +116,30 @@ void HubPlan<T>::build_tiles(const i64 *rp_host, i64 n, cudaStream_t s, int kmax
   }
 }
 
-template <typename T>
-void HubPlan<T>::build_stream(const i64 *rp_host, i64 n, i64 per_stream, int blocks,
-                              cudaStream_t s) {
-  nstream = 0;
-  stream_blocks = blocks;
-  if (n <= 0 || rp_host[n] >= ((i64)1 << 31) - 1 || n >= ((i64)1 << 31) - 1) return;
-  std::vector<i32> st{0};
+std::vector<i32> row_stream_starts(const i64 *rp_host, i64 n, i64 hub_thresh, i64 per_stream) {
+  std::vector<i32> st;
+  if (n <= 0 || rp_host[n] >= ((i64)1 << 31) - 1 || n >= ((i64)1 << 31) - 1) return st;
+  st.push_back(0);
   i64 acc = 0;
   for (i64 r = 0; r < n; r++) {
     const i64 len = rp_host[r + 1] - rp_host[r];
-    acc += (thresh > 0 && len > thresh ? 0 : len) + 16;
+    acc += (hub_thresh > 0 && len > hub_thresh ? 0 : len) + 16;
     if (acc >= per_stream) {
       st.push_back((i32)(r + 1));
       acc = 0;
     }
   }
   if (st.back() != (i32)n) st.push_back((i32)n);
+  return st;
+}
+
+template <typename T>
+void HubPlan<T>::build_stream(const i64 *rp_host, i64 n, i64 per_stream, int blocks,
+                              cudaStream_t s) {
+  nstream = 0;
+  stream_blocks = blocks;
+  std::vector<i32> st = row_stream_starts(rp_host, n, thresh, per_stream);
+  if (st.size() < 2) return;
   nstream = (i64)st.size() - 1;
   srow.alloc((i64)st.size(), s);
   srow.upload(st.data(), (i64)st.size());
@@ -1428,6 +1435,151 @@ __device__ __forceinline__ void df_reduce_slots(float (&sh)[VW], float (&sl)[VW]
     }
 }
 
+// Hub chunk c of the double-float product (32 lanes): chunk partials in
+// FP64, the last chunk of a row sums them in chunk order.
+template <int K>
+__device__ __forceinline__ void df_hub_unit(const MatView<double> &A,
+                                            const float2 *__restrict__ vdf,
+                                            const float2 *__restrict__ X, double *Y, i64 c,
+                                            int lane) {
+  constexpr int VW = (K % 2 == 0) ? 2 : 1;
+  constexpr int L = K / VW;
+  constexpr int E = 32 / L;
+  const int slot = lane / L, ch = lane % L;
+  if (c >= A.nchunks) return;
+  float sh[VW], sl[VW];
+#pragma unroll
+  for (int q = 0; q < VW; q++) sh[q] = sl[q] = 0.f;
+  df_row<K, VW, E>(A, vdf, X, A.ch_beg[c] + slot, A.ch_end[c], ch, sh, sl);
+  df_reduce_slots<VW, L, 32>(sh, sl);
+  double *part = A.partial;
+  if (slot == 0)
+#pragma unroll
+    for (int q = 0; q < VW; q++) part[c * K + ch * VW + q] = (double)sh[q] + (double)sl[q];
+  __threadfence();
+  __syncwarp();
+  int last = 0;
+  if (lane == 0) last = atomicAdd(&A.hub_counter[A.ch_hub[c]], 1) == A.ch_cnt[c] - 1;
+  last = __shfl_sync(0xffffffffu, last, 0);
+  if (!last) return;
+  __threadfence();
+  const i64 first = A.ch_first[c];
+  const int cnt = A.ch_cnt[c];
+  double t[VW];
+#pragma unroll
+  for (int q = 0; q < VW; q++) t[q] = 0.0;
+  for (int u = slot; u < cnt; u += E)
+#pragma unroll
+    for (int q = 0; q < VW; q++) t[q] += __ldcg(part + (first + u) * K + ch * VW + q);
+#pragma unroll
+  for (int o = L; o < 32; o <<= 1)
+#pragma unroll
+    for (int q = 0; q < VW; q++) t[q] += __shfl_xor_sync(0xffffffffu, t[q], o);
+  if (slot == 0)
+#pragma unroll
+    for (int q = 0; q < VW; q++) Y[A.ch_row[c] * K + ch * VW + q] = t[q];
+  if (lane == 0) A.hub_counter[A.ch_hub[c]] = 0;
+}
+
+// Row streams of the double-float product (the k >= 8 row-stream layout of
+// k_spmm_rs): warp w takes rows [srow[w], srow[w + 1]); the next row's end
+// and first column indices are loaded during this row's gathers; steps are
+// warp-uniform and masked past a row's end; every slot adds its entries in
+// entry order as df_row does, so the sums are the same.
+template <int K>
+__device__ __forceinline__ void df_stream_unit(const MatView<double> &A,
+                                               const float2 *__restrict__ vdf,
+                                               const float2 *__restrict__ X, double *Y, i64 w,
+                                               int lane) {
+  constexpr int VW = (K % 2 == 0) ? 2 : 1;
+  constexpr int L = K / VW;
+  constexpr int E = 32 / L;
+  constexpr int STEP = 4 * E;
+  const int slot = lane / L, ch = lane % L;
+  const i32 *__restrict__ ac = A.ci;
+  const i64 *__restrict__ rp = A.rp;
+  const int hub = (int)A.hub_thresh;
+  int r = __ldg(A.srow + w);
+  const int r1 = __ldg(A.srow + w + 1);
+  int b = (int)__ldg(rp + r), e = (int)__ldg(rp + r + 1);
+  int ee = (hub > 0 && e - b > hub) ? b : e;
+  i32 jn[4];
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const int q = b + slot + u * E;
+    jn[u] = q < ee ? __ldg(ac + q) : -1;
+  }
+  while (true) {
+    const bool last = r + 1 >= r1;
+    const int en = last ? e : (int)__ldg(rp + r + 2);
+    float sh[VW], sl[VW];
+#pragma unroll
+    for (int q = 0; q < VW; q++) sh[q] = sl[q] = 0.f;
+    int kb = b;
+    while (true) {
+      i32 j[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) j[u] = jn[u];
+      const int kn = kb + STEP;
+      const bool more = kn < ee;
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int q = kn + slot + u * E;
+          jn[u] = q < ee ? __ldg(ac + q) : -1;
+        }
+      } else {
+        const int nee = (last || (hub > 0 && en - e > hub)) ? e : en;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int q = e + slot + u * E;
+          jn[u] = q < nee ? __ldg(ac + q) : -1;
+        }
+      }
+      float2 a[4];
+      float h[4][VW], l[4][VW];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (j[u] >= 0) {
+          a[u] = __ldg(vdf + kb + slot + u * E);
+          df_ldg<VW>(X + (i64)j[u] * K + ch * VW, h[u], l[u]);
+        } else {
+          a[u] = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int q = 0; q < VW; q++) h[u][q] = l[u][q] = 0.f;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < VW; q++)
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (j[u] >= 0) df_fma(a[u].x, a[u].y, h[u][q], l[u][q], sh[q], sl[q]);
+      if (!more) break;
+      kb = kn;
+    }
+    df_reduce_slots<VW, L, 32>(sh, sl);
+    if ((ee > b || e == b) && slot == 0)
+#pragma unroll
+      for (int q = 0; q < VW; q++) Y[(i64)r * K + ch * VW + q] = (double)sh[q] + (double)sl[q];
+    if (last) break;
+    r++;
+    b = e;
+    e = en;
+    ee = (hub > 0 && e - b > hub) ? b : e;
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(256, 4) k_spmm_df_rs(const MatView<double> A,
+                                                       const float2 *__restrict__ vdf,
+                                                       const float2 *__restrict__ X, double *Y) {
+  dep_prologue();
+  const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp < A.nstream) df_stream_unit<K>(A, vdf, X, Y, warp, lane);
+  else df_hub_unit<K>(A, vdf, X, Y, warp - A.nstream, lane);
+}
+
 template <int K, int G>
 __global__ void __launch_bounds__(256) k_spmm_df(const MatView<double> A,
                                                  const float2 *__restrict__ vdf,
@@ -1461,39 +1613,7 @@ __global__ void __launch_bounds__(256) k_spmm_df(const MatView<double> A,
       for (int q = 0; q < VW; q++) Y[r * K + ch * VW + q] = (double)sh[q] + (double)sl[q];
     return;
   }
-  if constexpr (G == 32) {
-    const i64 c = warp - nregw;
-    if (c >= A.nchunks) return;
-    df_row<K, VW, E>(A, vdf, X, A.ch_beg[c] + slot, A.ch_end[c], ch, sh, sl);
-    df_reduce_slots<VW, L, G>(sh, sl);
-    double *part = A.partial;
-    if (slot == 0)
-#pragma unroll
-      for (int q = 0; q < VW; q++) part[c * K + ch * VW + q] = (double)sh[q] + (double)sl[q];
-    __threadfence();
-    __syncwarp();
-    int last = 0;
-    if (lane == 0) last = atomicAdd(&A.hub_counter[A.ch_hub[c]], 1) == A.ch_cnt[c] - 1;
-    last = __shfl_sync(0xffffffffu, last, 0);
-    if (!last) return;
-    __threadfence();
-    const i64 first = A.ch_first[c];
-    const int cnt = A.ch_cnt[c];
-    double t[VW];
-#pragma unroll
-    for (int q = 0; q < VW; q++) t[q] = 0.0;
-    for (int u = slot; u < cnt; u += E)
-#pragma unroll
-      for (int q = 0; q < VW; q++) t[q] += __ldcg(part + (first + u) * K + ch * VW + q);
-#pragma unroll
-    for (int o = L; o < G; o <<= 1)
-#pragma unroll
-      for (int q = 0; q < VW; q++) t[q] += __shfl_xor_sync(0xffffffffu, t[q], o);
-    if (slot == 0)
-#pragma unroll
-      for (int q = 0; q < VW; q++) Y[A.ch_row[c] * K + ch * VW + q] = t[q];
-    if (lane == 0) A.hub_counter[A.ch_hub[c]] = 0;
-  }
+  if constexpr (G == 32) df_hub_unit<K>(A, vdf, X, Y, warp - nregw, lane);
 }
 
 template <int K, int G>
@@ -1702,6 +1822,17 @@ void fcg_dir(i64 n, int k, T *p, const T *z, const T *pp, FcgScalars sc, cudaStr
 
 void spmm_df(const MatView<double> &A, const float2 *vdf, const float2 *X, int k, double *Y,
              cudaStream_t s) {
+  if (A.nstream > 0 && (k == 8 || k == 16 || k == 32 || k == 64)) {
+    const unsigned g = grid_for((A.nstream + A.nchunks) * 32, 256);
+    switch (k) {
+      case 8: launch_dep(k_spmm_df_rs<8>, g, 256, 0, s, A, vdf, X, Y); break;
+      case 16: launch_dep(k_spmm_df_rs<16>, g, 256, 0, s, A, vdf, X, Y); break;
+      case 32: launch_dep(k_spmm_df_rs<32>, g, 256, 0, s, A, vdf, X, Y); break;
+      default: launch_dep(k_spmm_df_rs<64>, g, 256, 0, s, A, vdf, X, Y); break;
+    }
+    LG_LAUNCH();
+    return;
+  }
   bool hub = A.nchunks > 0;
   int g = hub ? 32 : A.lanes_per_row;
   switch (k) {

@@ -86,6 +86,12 @@ struct HubPlan {
   void build_stream(const i64 *rp_host, i64 n, i64 per_stream, int blocks, cudaStream_t s);
   void fill(MatView<T> &m) const;
 };
+// Row streams: the first row of every run of consecutive rows holding about
+// per_stream entries (a row costs its entries plus 16; rows longer than
+// hub_thresh count as empty), then n; empty when the matrix has 2^31 entries
+// or rows or more.
+std::vector<i32> row_stream_starts(const i64 *rp_host, i64 n, i64 hub_thresh, i64 per_stream);
+
 // Single right-hand side tile layout: at most kTilePos entries (counted from
 // the tile's first entry rounded down to a multiple of four) and kTileRows
 // rows per tile; a warp takes a tile, a lane 8 consecutive entries.
