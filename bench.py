@@ -96,12 +96,13 @@ def dist_info():
 
 # DRAM bytes per matrix entry of the k = 32 FP32 SpMM with the fused
 # Chebyshev epilogue, from an ncu capture of a smaller case of the same kernel
-# (R-MAT 19 level 1, the ChebZ launch: 183.3 MB over 15,448,585 entries);
-# roofline.traffic scales it by the dominant launch's entries.  Levels whose
-# vectors stay in L2 move less, so this is an upper estimate there.
-SPMM_K32_DRAM_BYTES_PER_NNZ = 183.30e6 / 15448585
-SPMM_K32_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_spmm<float, 32, "
-                           "ChebZ> on R-MAT 19 level 1 (15,448,585 entries, 183.3 MB, 11.9 "
+# (the row-stream k_spmm_rs, R-MAT 19 level 1, the ChebZ launch: 157.8 MB read
+# and 22.7 MB written over 15,448,585 entries); roofline.traffic scales it by
+# the dominant launch's entries.  Levels whose vectors stay in L2 move less,
+# so this is an upper estimate there.
+SPMM_K32_DRAM_BYTES_PER_NNZ = 180.56e6 / 15448585
+SPMM_K32_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_spmm_rs<float, 32, "
+                           "ChebZ> on R-MAT 19 level 1 (15,448,585 entries, 157.8 + 22.7 MB, 11.7 "
                            "bytes per entry), scaled by the launch's entries")
 
 
@@ -115,10 +116,10 @@ def level_nnz_of(S, level):
 # DRAM bytes per matrix entry of the FP64 single right-hand-side SpMV
 # (k_spmv_tile, y = A x), from an ncu capture of a smaller case of the same
 # kernel (see SPMV_TRAFFIC_SOURCE); scaled to a launch by its entries.
-SPMV_DRAM_BYTES_PER_NNZ = 194.58e6 / 15448585
-SPMV_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_spmv_tile (FP64, "
-                       "y = A x) on R-MAT 19 level 1 (15,448,585 entries): 194.58 MB per "
-                       "launch, 12.6 bytes per entry, scaled by this launch's entries")
+SPMV_DRAM_BYTES_PER_NNZ = 213.96e6 / 15448585
+SPMV_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_spmv_tile<double, "
+                       "Store> on R-MAT 19 level 1 (15,448,585 entries): 193.2 MB read + 20.7 MB "
+                       "written per launch, 13.9 bytes per entry, scaled by this launch's entries")
 
 
 def peaks():
@@ -532,7 +533,7 @@ def run_ours(args):
         traffic, traffic_src = None, None
         if not top["fp64"] and top["kind"] in ("cheb_b", "spmv"):
             # DRAM bytes per entry of the k = 32 FP32 Chebyshev SpMM measured on a
-            # smaller case (profiles/spmm_k32_fp32_rmat19.md), scaled by entries
+            # smaller case (SPMM_K32_TRAFFIC_SOURCE), scaled by entries
             nnz_top = level_nnz_of(S, top["level"])
             traffic = SPMM_K32_DRAM_BYTES_PER_NNZ * nnz_top if nnz_top else None
             traffic_src = SPMM_K32_TRAFFIC_SOURCE
