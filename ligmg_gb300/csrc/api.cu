@@ -364,8 +364,34 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
   MatView<T> base = bare_view<T>(L, which);
   DBuf<T> X(L.A.n * k, s), Y(n * k, s);
   X.zero();
-  const Epi epi = which == MAT_C ? Epi::Split : Epi::Store;
+  // the yardstick: A's k-column plans are timed on the smoother's most
+  // frequent product (a later Chebyshev step: r, d, x and D^-1 read, x
+  // written), whose epilogue traffic separates the layouts; the others on
+  // their own epilogue (C: the residual restriction) or y = A x
+  const bool cheb = which == MAT_A && k > 1;
+  const Epi epi = which == MAT_C ? Epi::Split : (cheb ? Epi::ChebB : Epi::Store);
   if (which == MAT_C) base.x2 = X.p;  // both halves of the operand
+  DBuf<T> Rv, Xv, invd;
+  if (cheb) {
+    Rv.alloc(n * k, s);
+    Rv.zero();
+    Xv.alloc(n * k, s);
+    Xv.zero();
+    invd.alloc(n, s);
+    invd.zero();
+  }
+  auto bench_args = [&] {
+    EpiArgs a;
+    a.y = Y.p;
+    if (cheb) {
+      a.rin = Rv.p;
+      a.din = X.p;
+      a.xin = Xv.p;
+      a.xout = Y.p;
+      a.invd = invd.p;
+    }
+    return a;
+  };
   cudaEvent_t e0, e1;
   LG_CUDA(cudaEventCreate(&e0));
   LG_CUDA(cudaEventCreate(&e1));
@@ -393,8 +419,7 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
         m.tb = tb;
         if (half) m.krow_lanes = lanes ? lanes : 32;
         else if (lanes) m.lanes_per_row = lanes;
-        EpiArgs a;
-        a.y = Y.p;
+        EpiArgs a = bench_args();
         spmm<T>(m, X.p, k, epi, a, s);
         LG_CUDA(cudaEventRecord(e0, s));
         for (int r = 0; r < 3; r++) spmm<T>(m, X.p, k, epi, a, s);
@@ -428,8 +453,7 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
           MatView<T> m = base;
           cand.fill(m);
           m.stream_blocks = sb;
-          EpiArgs a;
-          a.y = Y.p;
+          EpiArgs a = bench_args();
           spmm<T>(m, X.p, k, epi, a, s);
           LG_CUDA(cudaEventRecord(e0, s));
           for (int r = 0; r < 3; r++) spmm<T>(m, X.p, k, epi, a, s);
@@ -463,8 +487,7 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
     if (cand.ntiles > 0) {
       MatView<T> m = base;
       cand.fill(m);
-      EpiArgs a;
-      a.y = Y.p;
+      EpiArgs a = bench_args();
       spmm<T>(m, X.p, k, epi, a, s);
       LG_CUDA(cudaEventRecord(e0, s));
       for (int r = 0; r < 3; r++) spmm<T>(m, X.p, k, epi, a, s);
@@ -492,8 +515,7 @@ void build_plan(const Level &L, int which, int k, HubPlan<T> &best, bool autotun
         MatView<T> m = base;
         cand.fill(m);
         m.tile_pipe = pipe;
-        EpiArgs a;
-        a.y = Y.p;
+        EpiArgs a = bench_args();
         spmm<T>(m, X.p, k, epi, a, s);
         LG_CUDA(cudaEventRecord(e0, s));
         for (int r = 0; r < 3; r++) spmm<T>(m, X.p, k, epi, a, s);
